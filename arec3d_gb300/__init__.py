@@ -1,0 +1,389 @@
+"""arec3d_gb300 — GB300 (sm_103a) implementation of the AREC3D reconstruction
+path, behind a C ABI (include/arec_gb300.h, include/arec_compat.h).
+
+This module is the Python host-side mirror of that ABI (ctypes):
+
+* ``Plan``: a geometry plan with device-resident projectors and solvers that
+  take raw CUDA device pointers (for example ``torch.Tensor.data_ptr()``) in
+  the device layouts (volume ``[nrays][ys]``, sinogram ``[nangles][nx][ys]``).
+* The reference's own entry points with the reference's argument meaning over
+  host numpy arrays: ``arecProject2D[_KB|_SQ]``, ``arecBackProject2D[_KB|_SQ]``,
+  ``cyl_sirt[_KB|_SQ]``, ``cyl_cgls[_KB|_SQ]``, ``arecCCImages``, ``ccorr2d``,
+  ``speak``, and the data model (``arecAllocateCylImage`` ...).
+
+There is no CPU fallback: importing works anywhere, but every call goes to the
+CUDA library and raises ``RuntimeError`` when it is missing.
+"""
+import ctypes as C
+import os
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "libarec_gb300.so")
+
+LIN, KB, SQ = 1, 2, 3
+ERR_ARG, ERR_NOMEM, ERR_CUDA_BASE = -90, -91, -100
+
+
+class SolveInfo(C.Structure):
+    _fields_ = [("iterations", C.c_int), ("iterbest", C.c_int), ("restarts", C.c_int),
+                ("status", C.c_int), ("lam_final", C.c_float), ("rnorm0", C.c_double),
+                ("rel_final", C.c_double)]
+
+
+class ArecImage(C.Structure):
+    """The reference's ``arecImage`` (AREC3D/AREC3D/arecImage.h:5-18)."""
+    _fields_ = [("nx", C.c_int), ("ny", C.c_int), ("nz", C.c_int), ("radius", C.c_double),
+                ("height", C.c_int), ("nnz", C.c_int), ("nrays", C.c_int),
+                ("cord", C.POINTER(C.c_int)), ("is_cyl", C.c_int),
+                ("data", C.POINTER(C.c_float))]
+
+
+_lib = None
+
+
+def build(force=False):
+    """Compile libarec_gb300.so (nvcc, sm_103a)."""
+    from . import builder
+
+    return builder.build(force=force)
+
+
+def lib():
+    """The loaded CUDA library; raises if it has not been built."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            raise RuntimeError("libarec_gb300.so is not built (run arec3d_gb300.build()); "
+                               "there is no CPU fallback")
+        L = C.CDLL(LIB_PATH)
+        vp, ip, dp, fp = C.c_void_p, C.POINTER(C.c_int), C.POINTER(C.c_double), C.POINTER(C.c_float)
+        L.arecgb_last_error.restype = C.c_char_p
+        L.arecgb_plan_create.argtypes = [C.POINTER(vp), C.c_int, C.c_double, C.c_int, C.c_int, fp]
+        L.arecgb_plan_destroy.argtypes = [vp]
+        L.arecgb_plan_info.argtypes = [vp, ip, ip, ip]
+        L.arecgb_project.argtypes = [vp, vp, vp, vp, vp]
+        L.arecgb_backproject.argtypes = [vp, vp, vp, vp, vp]
+        L.arecgb_cgls.argtypes = [vp, vp, vp, C.c_int, C.c_int, C.c_float, C.c_double, dp,
+                                  C.POINTER(SolveInfo), vp]
+        L.arecgb_sirt.argtypes = [vp, vp, vp, C.c_float, C.c_int, C.c_float, dp,
+                                  C.POINTER(SolveInfo), vp]
+        for n in ("arecgb_sino_from_reference", "arecgb_sino_to_reference"):
+            getattr(L, n).argtypes = [vp, vp, C.c_int, C.c_int, C.c_int, C.c_int, vp]
+        L.arecgb_cc_shifts.argtypes = [vp, vp, C.c_int, C.c_int, C.c_int, vp, vp, vp, vp, vp]
+        L.arecgb_ccorr2d_device.argtypes = [vp, vp, vp, C.c_int, C.c_int, vp]
+        img, pimg = ArecImage, C.POINTER(ArecImage)
+        for n in ("arecProject2D", "arecProject2D_KB", "arecProject2D_SQ", "arecBackProject2D",
+                  "arecBackProject2D_KB", "arecBackProject2D_SQ"):
+            f = getattr(L, "arecgb_" + n)
+            f.argtypes = [img, fp, C.c_int, pimg]
+            f.restype = C.c_int
+        for n in ("cyl_sirt", "cyl_sirt_KB", "cyl_sirt_SQ", "cyl_cgls", "cyl_cgls_KB",
+                  "cyl_cgls_SQ"):
+            f = getattr(L, "arecgb_" + n)
+            f.argtypes = [C.c_int, img, fp, pimg, C.c_float, C.c_int, C.c_float]
+            f.restype = C.c_int
+        L.arecgb_arecCCImages.argtypes = [C.c_int, img, img, fp, fp]
+        L.arecgb_ccorr2d.argtypes = [C.c_int, C.c_int, fp, fp, fp]
+        L.arecgb_ccorr2d.restype = None
+        L.arecgb_speak.argtypes = [C.c_int, C.c_int, fp, fp, fp]
+        L.arecgb_speak.restype = None
+        L.arecgb_arecAllocateCylImage.argtypes = [pimg, C.c_double, C.c_int]
+        L.arecgb_arecAllocateCBImage.argtypes = [pimg, C.c_int, C.c_int, C.c_int]
+        L.arecgb_arecImageFree.argtypes = [pimg]
+        L.arecgb_arecImageFree.restype = None
+        L.arecgb_ImageCyl2CB.argtypes = [img, img, C.c_int, C.c_int, C.c_int]
+        L.arecgb_ImageCB2Cyl.argtypes = [img, img, C.c_int, C.c_int, C.c_double, C.c_int]
+        L.arecgb_reset.argtypes = [pimg]
+        L.arecgb_reset.restype = None
+        L.arecgb_soft_noneg.argtypes = [pimg]
+        L.arecgb_soft_noneg.restype = None
+        L.arecgb_last_trace.argtypes = [dp, C.c_int, C.POINTER(SolveInfo)]
+        _lib = L
+    return _lib
+
+
+def last_error():
+    return lib().arecgb_last_error().decode()
+
+
+def _check(rc, what):
+    if rc != 0:
+        raise RuntimeError("%s failed (status %d): %s" % (what, rc, last_error()))
+
+
+def _ptr(t):
+    """Device pointer of a torch tensor, or an int pointer as given."""
+    if t is None:
+        return None
+    if isinstance(t, int):
+        return t
+    return t.data_ptr()
+
+
+def _stream(s):
+    if s is None:
+        return None
+    if isinstance(s, int):
+        return s
+    return s.cuda_stream
+
+
+# ---------------------------------------------------------------------------------------------
+class Plan:
+    """Geometry plan of one cylinder (radius, ny slices, float radian angles)."""
+
+    def __init__(self, weighting, radius, ny, angles):
+        self.weighting = int(weighting)
+        self.radius = float(radius)
+        self.ny = int(ny)
+        self.angles = np.ascontiguousarray(angles, dtype=np.float32)
+        h = C.c_void_p()
+        rc = lib().arecgb_plan_create(C.byref(h), self.weighting, self.radius, self.ny,
+                                      len(self.angles),
+                                      self.angles.ctypes.data_as(C.POINTER(C.c_float)))
+        _check(rc, "arecgb_plan_create")
+        self._h = h
+        nx, nr, ys = C.c_int(), C.c_int(), C.c_int()
+        lib().arecgb_plan_info(h, C.byref(nx), C.byref(nr), C.byref(ys))
+        self.nx, self.nrays, self.ys = nx.value, nr.value, ys.value
+        self.nangles = len(self.angles)
+
+    def close(self):
+        if getattr(self, "_h", None):
+            lib().arecgb_plan_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    @property
+    def vol_shape(self):
+        return (self.nrays, self.ys)
+
+    @property
+    def sino_shape(self):
+        return (self.nangles, self.nx, self.ys)
+
+    def project(self, x, q, norm2=None, stream=None):
+        _check(lib().arecgb_project(self._h, _ptr(x), _ptr(q), _ptr(norm2), _stream(stream)),
+               "arecgb_project")
+
+    def backproject(self, s, g, norm2=None, stream=None):
+        _check(lib().arecgb_backproject(self._h, _ptr(s), _ptr(g), _ptr(norm2), _stream(stream)),
+               "arecgb_backproject")
+
+    def cgls(self, b, x, maxit, tol, warm=False, rnorm_ref=0.0, stream=None):
+        hist = np.zeros(max(maxit, 1), np.float64)
+        info = SolveInfo()
+        rc = lib().arecgb_cgls(self._h, _ptr(b), _ptr(x), int(bool(warm)), int(maxit), float(tol),
+                               float(rnorm_ref), hist.ctypes.data_as(C.POINTER(C.c_double)),
+                               C.byref(info), _stream(stream))
+        _check(rc, "arecgb_cgls")
+        return hist[:info.iterations].copy(), info
+
+    def sirt(self, b, x, lam, maxit, tol, stream=None):
+        hist = np.zeros(max(maxit, 1), np.float64)
+        info = SolveInfo()
+        rc = lib().arecgb_sirt(self._h, _ptr(b), _ptr(x), float(lam), int(maxit), float(tol),
+                               hist.ctypes.data_as(C.POINTER(C.c_double)), C.byref(info),
+                               _stream(stream))
+        _check(rc, "arecgb_sirt")
+        return hist[:min(info.iterations, maxit)].copy(), info
+
+    def sino_from_reference(self, ref, dev, stream=None):
+        _check(lib().arecgb_sino_from_reference(_ptr(ref), _ptr(dev), self.nangles, self.ny,
+                                                self.nx, self.ys, _stream(stream)),
+               "arecgb_sino_from_reference")
+
+    def sino_to_reference(self, dev, ref, stream=None):
+        _check(lib().arecgb_sino_to_reference(_ptr(dev), _ptr(ref), self.nangles, self.ny,
+                                              self.nx, self.ys, _stream(stream)),
+               "arecgb_sino_to_reference")
+
+
+def cc_shifts(img1, img2, sx, sy, ix=None, iy=None, stream=None):
+    """Shift search over device image stacks [nz][ny][nx] (torch tensors)."""
+    nz, ny, nx = img1.shape
+    _check(lib().arecgb_cc_shifts(_ptr(img1), _ptr(img2), nz, ny, nx, _ptr(sx), _ptr(sy),
+                                  _ptr(ix), _ptr(iy), _stream(stream)), "arecgb_cc_shifts")
+
+
+def ccorr2d_device(x, y, c, stream=None):
+    ny, nx = x.shape
+    _check(lib().arecgb_ccorr2d_device(_ptr(x), _ptr(y), _ptr(c), ny, nx, _stream(stream)),
+           "arecgb_ccorr2d_device")
+
+
+# ---------------------------------------------------------------------------------------------
+# The reference's entry points over host arrays (reference layouts).
+def _f32p(a):
+    return a.ctypes.data_as(C.POINTER(C.c_float))
+
+
+def _cb_image(arr):
+    """arecImage view of a C-contiguous float32 [nz][ny][nx] array (caller keeps it alive)."""
+    im = ArecImage()
+    im.nz, im.ny, im.nx = arr.shape
+    im.is_cyl = 0
+    im.data = _f32p(arr)
+    return im
+
+
+def arecAllocateCylImage(radius, height):
+    """arecImage allocated by the library (free with arecImageFree)."""
+    im = ArecImage()
+    _check(lib().arecgb_arecAllocateCylImage(C.byref(im), float(radius), int(height)),
+           "arecAllocateCylImage")
+    return im
+
+
+def arecImageFree(im):
+    lib().arecgb_arecImageFree(C.byref(im))
+
+
+def cyl_data(im):
+    """numpy view [nrays][ny] of a cylindrical arecImage's data."""
+    return np.ctypeslib.as_array(im.data, shape=(im.nrays, im.ny))
+
+
+def cyl_cord(im):
+    return np.ctypeslib.as_array(im.cord, shape=(im.nrays, 2))
+
+
+def _project(name, radius, x, angles):
+    x = np.ascontiguousarray(x, dtype=np.float32)
+    angles = np.ascontiguousarray(angles, dtype=np.float32)
+    cyl = arecAllocateCylImage(radius, x.shape[1])
+    try:
+        if cyl.nrays != x.shape[0]:
+            raise ValueError("x has %d rays, the cylinder %d" % (x.shape[0], cyl.nrays))
+        cyl_data(cyl)[:] = x
+        q = np.zeros((len(angles), x.shape[1], cyl.nx), np.float32)
+        out = _cb_image(q)
+        st = getattr(lib(), "arecgb_" + name)(cyl, _f32p(angles), len(angles), C.byref(out))
+    finally:
+        arecImageFree(cyl)
+    return q, st
+
+
+def _backproject(name, radius, q, angles):
+    q = np.ascontiguousarray(q, dtype=np.float32)
+    angles = np.ascontiguousarray(angles, dtype=np.float32)
+    img = _cb_image(q)
+    vol = arecAllocateCylImage(radius, q.shape[1])
+    try:
+        st = getattr(lib(), "arecgb_" + name)(img, _f32p(angles), len(angles), C.byref(vol))
+        g = cyl_data(vol).copy()
+    finally:
+        arecImageFree(vol)
+    return g, st
+
+
+def arecProject2D(radius, x, angles):
+    """(q[nangles][ny][nx], status) for volume x[nrays][ny] (pmethod=1)."""
+    return _project("arecProject2D", radius, x, angles)
+
+
+def arecProject2D_KB(radius, x, angles):
+    return _project("arecProject2D_KB", radius, x, angles)
+
+
+def arecProject2D_SQ(radius, x, angles):
+    return _project("arecProject2D_SQ", radius, x, angles)
+
+
+def arecBackProject2D(radius, q, angles):
+    return _backproject("arecBackProject2D", radius, q, angles)
+
+
+def arecBackProject2D_KB(radius, q, angles):
+    return _backproject("arecBackProject2D_KB", radius, q, angles)
+
+
+def arecBackProject2D_SQ(radius, q, angles):
+    return _backproject("arecBackProject2D_SQ", radius, q, angles)
+
+
+def _solve(name, b, angles, lam, maxit, tol, x0=None):
+    b = np.ascontiguousarray(b, dtype=np.float32)
+    angles = np.ascontiguousarray(angles, dtype=np.float32)
+    img = _cb_image(b)
+    if x0 is None:
+        vol = ArecImage()
+        vol.data = C.POINTER(C.c_float)()
+    else:
+        nx = b.shape[2]
+        radius = (nx // 2) if name == "cyl_cgls_KB" else 0.5 * (nx - 1)
+        vol = arecAllocateCylImage(radius, b.shape[1])
+        cyl_data(vol)[:] = np.asarray(x0, np.float32)
+    st = getattr(lib(), "arecgb_" + name)(0, img, _f32p(angles), C.byref(vol), float(lam),
+                                          int(maxit), float(tol))
+    x = cyl_data(vol).copy() if vol.data else None
+    if vol.data:
+        arecImageFree(vol)
+    return x, st
+
+
+def last_trace(cap=4096):
+    """(relative residuals, SolveInfo) of the last solver call on this thread."""
+    rel = np.zeros(cap, np.float64)
+    info = SolveInfo()
+    n = lib().arecgb_last_trace(rel.ctypes.data_as(C.POINTER(C.c_double)), cap, C.byref(info))
+    return rel[:n].copy(), info
+
+
+def cyl_sirt(b, angles, lam=5e-6, maxit=10, tol=1e-3):
+    """(x[nrays][ny], status) — reference cyl_sirt over b[nangles][ny][nx]."""
+    return _solve("cyl_sirt", b, angles, lam, maxit, tol)
+
+
+def cyl_sirt_KB(b, angles, lam=5e-6, maxit=10, tol=1e-3):
+    return _solve("cyl_sirt_KB", b, angles, lam, maxit, tol)
+
+
+def cyl_sirt_SQ(b, angles, lam=5e-6, maxit=10, tol=1e-3):
+    return _solve("cyl_sirt_SQ", b, angles, lam, maxit, tol)
+
+
+def cyl_cgls(b, angles, maxit=10, tol=1e-3, x0=None):
+    return _solve("cyl_cgls", b, angles, 0.0, maxit, tol, x0)
+
+
+def cyl_cgls_KB(b, angles, maxit=10, tol=1e-3, x0=None):
+    return _solve("cyl_cgls_KB", b, angles, 0.0, maxit, tol, x0)
+
+
+def cyl_cgls_SQ(b, angles, maxit=10, tol=1e-3, x0=None):
+    return _solve("cyl_cgls_SQ", b, angles, 0.0, maxit, tol, x0)
+
+
+def arecCCImages(images1, images2):
+    """(sx, sy, status): shift of each images2[i] against images1[i] ([nz][ny][nx])."""
+    a = np.ascontiguousarray(images1, dtype=np.float32)
+    b = np.ascontiguousarray(images2, dtype=np.float32)
+    sx = np.zeros(a.shape[0], np.float32)
+    sy = np.zeros(a.shape[0], np.float32)
+    st = lib().arecgb_arecCCImages(0, _cb_image(a), _cb_image(b), _f32p(sx), _f32p(sy))
+    return sx, sy, st
+
+
+def ccorr2d(x, y):
+    x = np.ascontiguousarray(x, dtype=np.float32).copy()
+    y = np.ascontiguousarray(y, dtype=np.float32).copy()
+    ny, nx = x.shape
+    c = np.zeros_like(x)
+    lib().arecgb_ccorr2d(nx, ny, _f32p(x), _f32p(y), _f32p(c))
+    return c
+
+
+def speak(c):
+    c = np.ascontiguousarray(c, dtype=np.float32).copy()
+    ny, nx = c.shape
+    xt, yt = C.c_float(), C.c_float()
+    lib().arecgb_speak(nx, ny, _f32p(c), C.byref(xt), C.byref(yt))
+    return xt.value, yt.value

@@ -1,0 +1,688 @@
+// C ABI of libarec_gb300 (include/arec_gb300.h) and the reference-compatible
+// layer (include/arec_compat.h): the reference's own entry points over host
+// `arecImage` buffers, backed by the device kernels.
+#include <math.h>
+#include <stdio.h>
+#include <stdlib.h>
+#include <string.h>
+
+#include <algorithm>
+#include <cmath>
+#include <map>
+#include <memory>
+#include <mutex>
+#include <tuple>
+#include <vector>
+
+#include "arec_compat.h"
+#include "arec_internal.cuh"
+
+namespace arecgb {
+const char *last_error();
+int cgls(Plan *p, const float *d_b, float *d_x, int warm, int maxit, float tol, double rnorm_ref,
+         double *hist_host, arecgb_solve_info *info, cudaStream_t st);
+int sirt(Plan *p, const float *d_b, float *d_x, float lam, int maxit, float tol,
+         double *hist_host, arecgb_solve_info *info, int verbose, cudaStream_t st);
+int cc_shifts(const float *d1, const float *d2, int nz, int ny, int nx, float *sx, float *sy,
+              int *ix, int *iy, cudaStream_t st);
+int ccorr_image(const float *dx, const float *dy, float *dc, int ny, int nx, cudaStream_t st);
+int peak_search(const float *dc, int nz, int ny, int nx, float *sx, float *sy, int *ix, int *iy,
+                cudaStream_t st);
+}  // namespace arecgb
+
+using namespace arecgb;
+
+static Plan *P(arecgb_plan *p) { return reinterpret_cast<Plan *>(p); }
+static const Plan *P(const arecgb_plan *p) { return reinterpret_cast<const Plan *>(p); }
+
+static int bind_device(const Plan *p) {
+    int cur = -1;
+    cudaGetDevice(&cur);
+    if (cur != p->device) ARECGB_CUDA(cudaSetDevice(p->device));
+    return 0;
+}
+
+// ===========================================================================
+// Core C ABI.
+extern "C" {
+
+const char *arecgb_last_error(void) { return last_error(); }
+int arecgb_version(void) { return 10000; }
+
+int arecgb_plan_create(arecgb_plan **plan, int weighting, double radius, int ny, int nangles,
+                       const float *angles) {
+    if (!plan) {
+        set_error("arecgb_plan_create: null plan pointer");
+        return ARECGB_ERR_ARG;
+    }
+    Plan *p = nullptr;
+    int rc = plan_create(&p, weighting, radius, ny, nangles, angles);
+    *plan = reinterpret_cast<arecgb_plan *>(p);
+    return rc;
+}
+
+int arecgb_plan_destroy(arecgb_plan *plan) {
+    plan_destroy(P(plan));
+    return ARECGB_OK;
+}
+
+int arecgb_plan_info(const arecgb_plan *plan, int *nx, int *nrays, int *ys) {
+    if (!plan) {
+        set_error("arecgb_plan_info: null plan");
+        return ARECGB_ERR_ARG;
+    }
+    if (nx) *nx = P(plan)->nx;
+    if (nrays) *nrays = P(plan)->nrays;
+    if (ys) *ys = P(plan)->ys;
+    return ARECGB_OK;
+}
+
+int arecgb_project(arecgb_plan *plan, const float *d_x, float *d_q, double *d_norm2,
+                   void *stream) {
+    if (!plan || !d_x || !d_q) {
+        set_error("arecgb_project: null argument");
+        return ARECGB_ERR_ARG;
+    }
+    int rc = bind_device(P(plan));
+    if (rc) return rc;
+    return forward_project(P(plan), d_x, d_q, d_norm2, nullptr, (cudaStream_t)stream);
+}
+
+int arecgb_backproject(arecgb_plan *plan, const float *d_s, float *d_g, double *d_norm2,
+                       void *stream) {
+    if (!plan || !d_s || !d_g) {
+        set_error("arecgb_backproject: null argument");
+        return ARECGB_ERR_ARG;
+    }
+    int rc = bind_device(P(plan));
+    if (rc) return rc;
+    return back_project(P(plan), d_s, d_g, d_norm2, nullptr, (cudaStream_t)stream);
+}
+
+int arecgb_cgls(arecgb_plan *plan, const float *d_b, float *d_x, int warm, int maxit, float tol,
+                double rnorm_ref, double *rel_history, arecgb_solve_info *info, void *stream) {
+    if (!plan || !d_b || !d_x || maxit < 0) {
+        set_error("arecgb_cgls: bad argument");
+        return ARECGB_ERR_ARG;
+    }
+    int rc = bind_device(P(plan));
+    if (rc) return rc;
+    return cgls(P(plan), d_b, d_x, warm, maxit, tol, rnorm_ref, rel_history, info,
+                (cudaStream_t)stream);
+}
+
+int arecgb_sirt(arecgb_plan *plan, const float *d_b, float *d_x, float lam, int maxit, float tol,
+                double *rel_history, arecgb_solve_info *info, void *stream) {
+    if (!plan || !d_b || !d_x || maxit < 0) {
+        set_error("arecgb_sirt: bad argument");
+        return ARECGB_ERR_ARG;
+    }
+    int rc = bind_device(P(plan));
+    if (rc) return rc;
+    return sirt(P(plan), d_b, d_x, lam, maxit, tol, rel_history, info, 0, (cudaStream_t)stream);
+}
+
+int arecgb_sino_from_reference(const float *d_ref, float *d_dev, int na, int ny, int nx, int ys,
+                               void *stream) {
+    return sino_to_device_layout(d_ref, d_dev, na, ny, nx, ys, (cudaStream_t)stream);
+}
+
+int arecgb_sino_to_reference(const float *d_dev, float *d_ref, int na, int ny, int nx, int ys,
+                             void *stream) {
+    return sino_to_reference_layout(d_dev, d_ref, na, ny, nx, ys, (cudaStream_t)stream);
+}
+
+int arecgb_cc_shifts(const float *d_img1, const float *d_img2, int nz, int ny, int nx,
+                     float *d_sx, float *d_sy, int *d_ix, int *d_iy, void *stream) {
+    return cc_shifts(d_img1, d_img2, nz, ny, nx, d_sx, d_sy, d_ix, d_iy, (cudaStream_t)stream);
+}
+
+int arecgb_ccorr2d_device(const float *d_x, const float *d_y, float *d_c, int ny, int nx,
+                          void *stream) {
+    return ccorr_image(d_x, d_y, d_c, ny, nx, (cudaStream_t)stream);
+}
+
+}  // extern "C"
+
+// ===========================================================================
+// Reference-compatible layer.
+
+namespace {
+
+std::mutex g_mu;
+
+bool quiet() {
+    const char *q = getenv("ARECGB_QUIET");
+    return q && q[0] && q[0] != '0';
+}
+
+// Plans keyed by geometry; the compatible entry points rebuild nothing when
+// called again on the same cylinder and angles.
+struct Key {
+    int w;
+    double r;
+    int ny, dev;
+    std::vector<float> ang;
+    bool operator<(const Key &o) const {
+        return std::tie(w, r, ny, dev, ang) < std::tie(o.w, o.r, o.ny, o.dev, o.ang);
+    }
+};
+std::map<Key, Plan *> g_plans;
+std::vector<Key> g_lru;
+constexpr size_t kMaxPlans = 6;
+
+int cached_plan(Plan **out, int w, double radius, int ny, int na, const float *angles) {
+    int dev = 0;
+    cudaGetDevice(&dev);
+    Key k{w, radius, ny, dev, std::vector<float>(angles, angles + na)};
+    auto it = g_plans.find(k);
+    if (it != g_plans.end()) {
+        *out = it->second;
+        auto pos = std::find_if(g_lru.begin(), g_lru.end(),
+                                [&](const Key &x) { return !(x < k) && !(k < x); });
+        if (pos != g_lru.end()) {
+            g_lru.erase(pos);
+            g_lru.push_back(k);
+        }
+        return 0;
+    }
+    while (g_plans.size() >= kMaxPlans && !g_lru.empty()) {
+        auto old = g_plans.find(g_lru.front());
+        if (old != g_plans.end()) {
+            plan_destroy(old->second);
+            g_plans.erase(old);
+        }
+        g_lru.erase(g_lru.begin());
+    }
+    Plan *p = nullptr;
+    int rc = plan_create(&p, w, radius, ny, na, angles);
+    if (rc) return rc;
+    g_plans[k] = p;
+    g_lru.push_back(k);
+    *out = p;
+    return 0;
+}
+
+int ensure(float **buf, size_t n) {
+    if (*buf) return 0;
+    ARECGB_CUDA(cudaMalloc(buf, sizeof(float) * std::max<size_t>(n, 1)));
+    ARECGB_CUDA(cudaMemset(*buf, 0, sizeof(float) * std::max<size_t>(n, 1)));
+    return 0;
+}
+
+int ensure_stage(Plan *p, size_t n) {
+    if (p->d_stage && p->stage_floats >= n) return 0;
+    cudaFree(p->d_stage);
+    p->d_stage = nullptr;
+    p->stage_floats = 0;
+    ARECGB_CUDA(cudaMalloc(&p->d_stage, sizeof(float) * std::max<size_t>(n, 1)));
+    p->stage_floats = n;
+    return 0;
+}
+
+// Host -> device volume ([nrays][ny] -> [nrays][ys]).
+int upload_volume(Plan *p, const float *h, float *d) {
+    ARECGB_CUDA(cudaMemcpy2DAsync(d, sizeof(float) * p->ys, h, sizeof(float) * p->ny,
+                                  sizeof(float) * p->ny, p->nrays, cudaMemcpyHostToDevice,
+                                  p->stream));
+    return 0;
+}
+
+int download_volume(Plan *p, const float *d, float *h) {
+    ARECGB_CUDA(cudaMemcpy2DAsync(h, sizeof(float) * p->ny, d, sizeof(float) * p->ys,
+                                  sizeof(float) * p->ny, p->nrays, cudaMemcpyDeviceToHost,
+                                  p->stream));
+    return 0;
+}
+
+// Host [na][ny][nx] -> device [na][nx][ys].
+int upload_sino(Plan *p, const float *h, float *d) {
+    const size_t n = (size_t)p->na * p->ny * p->nx;
+    int rc = ensure_stage(p, n);
+    if (rc) return rc;
+    ARECGB_CUDA(cudaMemcpyAsync(p->d_stage, h, sizeof(float) * n, cudaMemcpyHostToDevice,
+                                p->stream));
+    return sino_to_device_layout(p->d_stage, d, p->na, p->ny, p->nx, p->ys, p->stream);
+}
+
+int download_sino(Plan *p, const float *d, float *h) {
+    const size_t n = (size_t)p->na * p->ny * p->nx;
+    int rc = ensure_stage(p, n);
+    if (rc) return rc;
+    rc = sino_to_reference_layout(d, p->d_stage, p->na, p->ny, p->nx, p->ys, p->stream);
+    if (rc) return rc;
+    ARECGB_CUDA(cudaMemcpyAsync(h, p->d_stage, sizeof(float) * n, cudaMemcpyDeviceToHost,
+                                p->stream));
+    return 0;
+}
+
+int sync_plan(Plan *p) {
+    ARECGB_CUDA(cudaStreamSynchronize(p->stream));
+    ARECGB_CUDA(cudaGetLastError());
+    return 0;
+}
+
+// Host replica of arecAllocateCylImage (AREC3D/AREC3D/arecImage.cpp:29-86).
+int alloc_cyl(arecImage *im, double radius, int height) {
+    int nx = (int)std::round(2 * radius + 1);
+    im->nx = nx;
+    im->ny = height;
+    im->nz = nx;
+    im->radius = radius;
+    im->height = height;
+    int r2 = (int)(radius * radius);
+    int nr = 0;
+    for (int iz = 0; iz < nx; iz++) {
+        int zs = (int)(iz - radius);
+        for (int ix = 0; ix < nx; ix++) {
+            int xs = (int)(ix - radius);
+            if (zs * zs + xs * xs <= r2) nr++;
+        }
+    }
+    im->nrays = nr;
+    im->nnz = nr * height;
+    im->data = (float *)calloc((size_t)nr * height, sizeof(float));
+    im->cord = (int *)calloc((size_t)nr * 2, sizeof(int));
+    im->is_cyl = 1;
+    if (!im->data || !im->cord) return -1;
+    int k = 0;
+    for (int iz = 0; iz < nx; iz++) {
+        int zs = (int)(iz - radius);
+        for (int ix = 0; ix < nx; ix++) {
+            int xs = (int)(ix - radius);
+            if (zs * zs + xs * xs <= r2) {
+                im->cord[2 * k] = ix;
+                im->cord[2 * k + 1] = iz;
+                k++;
+            }
+        }
+    }
+    return 0;
+}
+
+thread_local std::vector<double> g_trace;
+thread_local arecgb_solve_info g_trace_info;
+
+// arecProject2D[_KB|_SQ] (AREC3D/AREC3D/arecproject.cpp:19,351,540).
+int compat_project(int w, const arecImage &cyl, const float *angles, int nangles,
+                   arecImage *proj) {
+    if (!cyl.is_cyl) {
+        if (!quiet()) fprintf(stderr, "invalid input volume format. Must be cylindrical!\n");
+        return 1;
+    }
+    if (proj->nx != cyl.nx || proj->ny != cyl.ny) {
+        if (!quiet()) fprintf(stderr, "arecProject2D: inconsistent dimension!\n");
+        return 2;
+    }
+    if (cyl.nnz != cyl.nrays * cyl.ny || nangles > proj->nz || nangles < 0) {
+        if (!quiet()) fprintf(stderr, "arecProject2D: problem with nnz count!\n");
+        return 2;
+    }
+    const size_t per = (size_t)proj->nx * proj->ny;
+    if (nangles == 0) {
+        memset(proj->data, 0, sizeof(float) * per * proj->nz);
+        return 0;
+    }
+    std::lock_guard<std::mutex> lk(g_mu);
+    Plan *p = nullptr;
+    int rc = cached_plan(&p, w, cyl.radius, cyl.ny, nangles, angles);
+    if (rc) return rc;
+    if (p->nrays != cyl.nrays || p->nx != cyl.nx) {
+        set_error("arecProject2D: cylinder does not match its radius");
+        return 2;
+    }
+    if ((rc = ensure(&p->d_vol[3], vol_floats(p))) || (rc = ensure(&p->d_sin[2], sin_floats(p))))
+        return rc;
+    if ((rc = upload_volume(p, cyl.data, p->d_vol[3]))) return rc;
+    if ((rc = forward_project(p, p->d_vol[3], p->d_sin[2], nullptr, nullptr, p->stream)))
+        return rc;
+    if ((rc = download_sino(p, p->d_sin[2], proj->data))) return rc;
+    if ((rc = sync_plan(p))) return rc;
+    if (proj->nz > nangles)
+        memset(proj->data + per * nangles, 0, sizeof(float) * per * (proj->nz - nangles));
+    return 0;
+}
+
+// arecBackProject2D[_KB|_SQ] (arecproject.cpp:109,447,650).
+int compat_backproject(int w, const arecImage &img, const float *angles, int nangles,
+                       arecImage *vol) {
+    if (img.nz != nangles) return 1;
+    if (vol->nx != img.nx || vol->ny != img.ny) {
+        if (!quiet()) fprintf(stderr, "arecBackProject2D: image and volume sizes don't match\n");
+        return -1;
+    }
+    if (!vol->is_cyl) {
+        if (!quiet())
+            fprintf(stderr, "arecBackProject2D: cylindrical volume not properly set!\n");
+        return -1;
+    }
+    if (vol->nnz != vol->nrays * vol->ny) {
+        if (!quiet()) fprintf(stderr, "arecProject2D: problem with nnz count!\n");
+        return 2;
+    }
+    if (nangles == 0) {
+        memset(vol->data, 0, sizeof(float) * vol->nnz);
+        return 0;
+    }
+    std::lock_guard<std::mutex> lk(g_mu);
+    Plan *p = nullptr;
+    int rc = cached_plan(&p, w, vol->radius, vol->ny, nangles, angles);
+    if (rc) return rc;
+    if (p->nrays != vol->nrays || p->nx != vol->nx) {
+        set_error("arecBackProject2D: cylinder does not match its radius");
+        return -1;
+    }
+    if ((rc = ensure(&p->d_vol[3], vol_floats(p))) || (rc = ensure(&p->d_sin[2], sin_floats(p))))
+        return rc;
+    if ((rc = upload_sino(p, img.data, p->d_sin[2]))) return rc;
+    if ((rc = back_project(p, p->d_sin[2], p->d_vol[3], nullptr, nullptr, p->stream))) return rc;
+    if ((rc = download_volume(p, p->d_vol[3], vol->data))) return rc;
+    return sync_plan(p);
+}
+
+// cyl_cgls[_KB|_SQ] and cyl_sirt[_KB|_SQ].
+int compat_solve(bool is_cgls, int w, const arecImage &images, const float *angles,
+                 arecImage *xvol, float lam, int maxit, float tol) {
+    const int nx = images.nx, ny = images.ny, nz = images.nz;
+    // radius = 0.5*(nx-1) (areccgls.cpp:49, arecsirt.cpp:37); the KB CGLS uses
+    // the integer nx/2 (areccgls_KB.cpp:37), which fails for even nx.
+    const bool kb_int_radius = is_cgls && w == ARECGB_KB;
+    const double radius = kb_int_radius ? (double)(nx / 2) : 0.5 * (nx - 1);
+    const bool v = !quiet();
+    const bool warm = xvol->data != NULL;
+    if (!warm) {
+        if (is_cgls && v) printf("mypid = 0, null data\n");
+        if (alloc_cyl(xvol, radius, ny)) {
+            set_error("solver: host allocation failed");
+            return ARECGB_ERR_NOMEM;
+        }
+    }
+    if (kb_int_radius && (nx % 2 == 0)) {
+        // The reference's gradient volume then has nx+1 columns and the first
+        // back-projection returns -1 (areccgls_KB.cpp:112-113).
+        return -1;
+    }
+    if (xvol->nrays <= 0 || xvol->nnz != xvol->nrays * ny) {
+        set_error("solver: xvol does not match the images");
+        return 2;
+    }
+    std::lock_guard<std::mutex> lk(g_mu);
+    Plan *p = nullptr;
+    int rc = cached_plan(&p, w, radius, ny, nz, angles);
+    if (rc) return rc;
+    if (p->nrays != xvol->nrays) {
+        set_error("solver: xvol does not match the images");
+        return 2;
+    }
+    if ((rc = ensure(&p->d_vol[3], vol_floats(p))) || (rc = ensure(&p->d_sin[2], sin_floats(p))))
+        return rc;
+    if ((rc = upload_sino(p, images.data, p->d_sin[2]))) return rc;
+    if (is_cgls && warm && (rc = upload_volume(p, xvol->data, p->d_vol[3]))) return rc;
+    if (v) {
+        printf("%snrays = %d, nnz = %d\n", is_cgls && w == ARECGB_SQ ? "cyl: " : "", xvol->nrays,
+               xvol->nnz);
+        if (kb_int_radius)
+            printf("nx = %d, ny = %d, radius = %d, height = %d\n", nx, ny, (int)radius, ny);
+        else
+            printf("nx = %d, ny = %d, radius = %4.2f, height = %d\n", nx, ny, radius, ny);
+    }
+    std::vector<double> hist((size_t)std::max(maxit, 1), 0.0);
+    arecgb_solve_info info;
+    memset(&info, 0, sizeof(info));
+    if (is_cgls)
+        rc = cgls(p, p->d_sin[2], p->d_vol[3], warm ? 1 : 0, maxit, tol, 0.0, hist.data(), &info,
+                  p->stream);
+    else
+        rc = sirt(p, p->d_sin[2], p->d_vol[3], lam, maxit, tol, hist.data(), &info, v ? 1 : 0,
+                  p->stream);
+    if (rc) return rc;
+    if ((rc = download_volume(p, p->d_vol[3], xvol->data))) return rc;
+    if ((rc = sync_plan(p))) return rc;
+    g_trace.assign(hist.begin(), hist.begin() + std::min(info.iterations, maxit));
+    g_trace_info = info;
+    if (is_cgls && v) {
+        printf("CG iter = 0, resnrm = %11.3e\n", info.rnorm0);
+        for (int i = 0; i < std::min(info.iterations, maxit); i++)
+            printf("CG iter = %3d, rnorm / bnorm = %11.3e, rnorm = %11.3e\n", i + 1, hist[i],
+                   hist[i] * info.rnorm0);
+        if (info.iterations > 0 && hist[info.iterations - 1] < tol)
+            printf("Terminating with rnorm/bnorm = %11.3e, tol = %11.3e, ",
+                   hist[info.iterations - 1], tol);
+        if (info.iterbest < maxit - 1) printf("retrieve the best solution\n");
+    }
+    return 0;
+}
+
+}  // namespace
+
+// ---------------------------------------------------------------------------
+// extern "C" aliases for C/FFI callers.
+extern "C" {
+
+int arecgb_arecAllocateCBImage(arecImage *cb, int nx, int ny, int nz) {
+    cb->nx = nx;
+    cb->ny = ny;
+    cb->nz = nz;
+    cb->data = (float *)calloc((size_t)nx * ny * nz, sizeof(float));
+    cb->is_cyl = 0;
+    cb->cord = NULL;
+    return cb->data ? 0 : -1;
+}
+
+int arecgb_arecAllocateCylImage(arecImage *cyl, double radius, int height) {
+    return alloc_cyl(cyl, radius, height);
+}
+
+// ImageCyl2CB (AREC3D/AREC3D/arecImage.cpp:163-232): scatter [ray][y] into the cube.
+int arecgb_ImageCyl2CB(arecImage cyl, arecImage cb, int nx, int ny, int nz) {
+    if (!cyl.data) return -1;
+    if (nx != cb.nx || ny != cb.ny || nz != cb.nz) return 1;
+    if (nx != 2 * cyl.radius + 1 || nz != 2 * cyl.radius + 1 || ny != cyl.height) return 1;
+    if (!cb.data) return -1;
+    for (int j = 0; j < cyl.nrays; j++) {
+        int ix = cyl.cord[2 * j], iz = cyl.cord[2 * j + 1];
+        if (iz >= nz || ix >= nx) return -2;
+        for (int iy = 0; iy < ny; iy++)
+            cb.data[((size_t)iz * ny + iy) * nx + ix] = cyl.data[(size_t)j * ny + iy];
+    }
+    return 0;
+}
+
+// ImageCB2Cyl (arecImage.cpp:88-161): gather the disk of the cube into [ray][y].
+int arecgb_ImageCB2Cyl(arecImage cb, arecImage cyl, int xcent, int zcent, double radius,
+                       int height) {
+    (void)xcent;
+    (void)zcent;
+    (void)radius;
+    (void)height;
+    if (!cyl.data) return -1;
+    radius = cyl.radius;
+    height = cyl.height;
+    if (cyl.nnz <= 0 || cyl.nrays <= 0 || radius <= 0 || height <= 0) return 1;
+    if (!cyl.cord) return -1;
+    const int nx = cb.nx, ny = cb.ny, nz = cb.nz;
+    int r2 = (int)(radius * radius), nnz = 0, nr = 0;
+    for (int iz = 0; iz < nz; iz++) {
+        int zs = (int)(iz - radius);
+        for (int ix = 0; ix < nx; ix++) {
+            int xs = (int)(ix - radius);
+            if (xs * xs + zs * zs <= r2) {
+                for (int iy = 0; iy < ny; iy++)
+                    cyl.data[nnz++] = cb.data[((size_t)iz * ny + iy) * nx + ix];
+                cyl.cord[2 * nr] = ix;
+                cyl.cord[2 * nr + 1] = iz;
+                nr++;
+            }
+        }
+    }
+    return (nnz != cyl.nnz || nr != cyl.nrays) ? -2 : 0;
+}
+
+void arecgb_arecImageFree(arecImage *im) {
+    if (im->is_cyl) {
+        free(im->cord);
+        im->cord = NULL;
+    }
+    free(im->data);
+    im->data = NULL;
+}
+
+// reset / soft_noneg (arecImage.cpp:796-826).
+void arecgb_reset(arecImage *im) {
+    size_t n = im->is_cyl ? (size_t)im->nnz : (size_t)im->nx * im->ny * im->nz;
+    memset(im->data, 0, sizeof(float) * n);
+}
+
+void arecgb_soft_noneg(arecImage *im) {
+    size_t n = im->is_cyl ? (size_t)im->nnz : (size_t)im->nx * im->ny * im->nz;
+    for (size_t i = 0; i < n; i++)
+        if (im->data[i] < 0.0f) im->data[i] *= 0.5f;
+}
+
+int arecgb_arecProject2D(arecImage c, float *a, int n, arecImage *p) {
+    return compat_project(ARECGB_LIN, c, a, n, p);
+}
+int arecgb_arecProject2D_KB(arecImage c, float *a, int n, arecImage *p) {
+    return compat_project(ARECGB_KB, c, a, n, p);
+}
+int arecgb_arecProject2D_SQ(arecImage c, float *a, int n, arecImage *p) {
+    return compat_project(ARECGB_SQ, c, a, n, p);
+}
+int arecgb_arecBackProject2D(arecImage i, float *a, int n, arecImage *v) {
+    return compat_backproject(ARECGB_LIN, i, a, n, v);
+}
+int arecgb_arecBackProject2D_KB(arecImage i, float *a, int n, arecImage *v) {
+    return compat_backproject(ARECGB_KB, i, a, n, v);
+}
+int arecgb_arecBackProject2D_SQ(arecImage i, float *a, int n, arecImage *v) {
+    return compat_backproject(ARECGB_SQ, i, a, n, v);
+}
+
+int arecgb_cyl_sirt(MPI_Comm, arecImage im, float *a, arecImage *x, float lam, int maxit,
+                    float tol) {
+    return compat_solve(false, ARECGB_LIN, im, a, x, lam, maxit, tol);
+}
+int arecgb_cyl_sirt_KB(MPI_Comm, arecImage im, float *a, arecImage *x, float lam, int maxit,
+                       float tol) {
+    return compat_solve(false, ARECGB_KB, im, a, x, lam, maxit, tol);
+}
+int arecgb_cyl_sirt_SQ(MPI_Comm, arecImage im, float *a, arecImage *x, float lam, int maxit,
+                       float tol) {
+    return compat_solve(false, ARECGB_SQ, im, a, x, lam, maxit, tol);
+}
+int arecgb_cyl_cgls(MPI_Comm, arecImage im, float *a, arecImage *x, float lam, int maxit,
+                    float tol) {
+    return compat_solve(true, ARECGB_LIN, im, a, x, lam, maxit, tol);
+}
+int arecgb_cyl_cgls_KB(MPI_Comm, arecImage im, float *a, arecImage *x, float lam, int maxit,
+                       float tol) {
+    return compat_solve(true, ARECGB_KB, im, a, x, lam, maxit, tol);
+}
+int arecgb_cyl_cgls_SQ(MPI_Comm, arecImage im, float *a, arecImage *x, float lam, int maxit,
+                       float tol) {
+    return compat_solve(true, ARECGB_SQ, im, a, x, lam, maxit, tol);
+}
+
+// arecCCImages (AREC3D/AREC3D/arecImage.cpp:384-434): shifts of each image of
+// images2 against the same-index image of images1.
+int arecgb_arecCCImages(MPI_Comm, arecImage i1, arecImage i2, float *sx, float *sy) {
+    if (i1.nx != i2.nx || i1.ny != i2.ny || i1.nz != i2.nz) {
+        if (!quiet()) fprintf(stderr, "arecCCImages: mismatch in dimension:\n");
+        return -1;
+    }
+    const int nx = i1.nx, ny = i1.ny, nz = i1.nz;
+    if (nz <= 0) return 0;
+    std::lock_guard<std::mutex> lk(g_mu);
+    const size_t n = (size_t)nx * ny * nz;
+    float *d1 = nullptr, *d2 = nullptr, *dsx = nullptr;
+    cudaStream_t st = nullptr;
+    int rc = 0;
+    cudaError_t e = cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaMalloc(&d1, sizeof(float) * n);
+    if (e == cudaSuccess) e = cudaMalloc(&d2, sizeof(float) * n);
+    if (e == cudaSuccess) e = cudaMalloc(&dsx, sizeof(float) * 2 * nz);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(d1, i1.data, sizeof(float) * n, cudaMemcpyHostToDevice, st);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(d2, i2.data, sizeof(float) * n, cudaMemcpyHostToDevice, st);
+    if (e != cudaSuccess) {
+        set_error(std::string("arecCCImages: ") + cudaGetErrorString(e));
+        rc = cuda_status(e);
+    }
+    if (!rc) rc = cc_shifts(d1, d2, nz, ny, nx, dsx, dsx + nz, nullptr, nullptr, st);
+    if (!rc) {
+        e = cudaMemcpyAsync(sx, dsx, sizeof(float) * nz, cudaMemcpyDeviceToHost, st);
+        if (e == cudaSuccess)
+            e = cudaMemcpyAsync(sy, dsx + nz, sizeof(float) * nz, cudaMemcpyDeviceToHost, st);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+        if (e != cudaSuccess) {
+            set_error(std::string("arecCCImages: ") + cudaGetErrorString(e));
+            rc = cuda_status(e);
+        }
+    }
+    if (st) cudaStreamSynchronize(st);
+    cudaFree(d1);
+    cudaFree(d2);
+    cudaFree(dsx);
+    if (st) cudaStreamDestroy(st);
+    return rc;
+}
+
+// ccorr2d (AREC3D/AREC3D/align2dstack.cpp:480-521).
+void arecgb_ccorr2d(int nx, int ny, float *x, float *y, float *c) {
+    std::lock_guard<std::mutex> lk(g_mu);
+    const size_t n = (size_t)nx * ny;
+    float *d = nullptr;
+    if (cudaMalloc(&d, sizeof(float) * 3 * n) != cudaSuccess) {
+        set_error("ccorr2d: device allocation failed");
+        return;
+    }
+    cudaMemcpy(d, x, sizeof(float) * n, cudaMemcpyHostToDevice);
+    cudaMemcpy(d + n, y, sizeof(float) * n, cudaMemcpyHostToDevice);
+    if (ccorr_image(d, d + n, d + 2 * n, ny, nx, 0) == 0)
+        cudaMemcpy(c, d + 2 * n, sizeof(float) * n, cudaMemcpyDeviceToHost);
+    cudaFree(d);
+}
+
+// speak (AREC3D/AREC3D/align2dstack.cpp:1059-1105).
+void arecgb_speak(int nx, int ny, float *data, float *xt, float *yt) {
+    std::lock_guard<std::mutex> lk(g_mu);
+    const size_t n = (size_t)nx * ny;
+    float *d = nullptr;
+    if (cudaMalloc(&d, sizeof(float) * (n + 2)) != cudaSuccess) {
+        set_error("speak: device allocation failed");
+        return;
+    }
+    cudaMemcpy(d, data, sizeof(float) * n, cudaMemcpyHostToDevice);
+    if (peak_search(d, 1, ny, nx, d + n, d + n + 1, nullptr, nullptr, 0) == 0) {
+        cudaMemcpy(xt, d + n, sizeof(float), cudaMemcpyDeviceToHost);
+        cudaMemcpy(yt, d + n + 1, sizeof(float), cudaMemcpyDeviceToHost);
+    }
+    cudaFree(d);
+}
+
+int arecgb_last_trace(double *rel, int cap, arecgb_solve_info *info) {
+    int n = std::min<int>(cap, (int)g_trace.size());
+    if (rel)
+        for (int i = 0; i < n; i++) rel[i] = g_trace[i];
+    if (info) *info = g_trace_info;
+    return n;
+}
+
+}  // extern "C"
+
+// ---------------------------------------------------------------------------
+// The reference's own C++ symbols (same mangled names as its headers declare).
+int arecProject2D(arecImage c, float *a, int n, arecImage *p) { return arecgb_arecProject2D(c, a, n, p); }
+int arecProject2D_KB(arecImage c, float *a, int n, arecImage *p) { return arecgb_arecProject2D_KB(c, a, n, p); }
+int arecProject2D_SQ(arecImage c, float *a, int n, arecImage *p) { return arecgb_arecProject2D_SQ(c, a, n, p); }
+int arecBackProject2D(arecImage i, float *a, int n, arecImage *v) { return arecgb_arecBackProject2D(i, a, n, v); }
+int arecBackProject2D_KB(arecImage i, float *a, int n, arecImage *v) { return arecgb_arecBackProject2D_KB(i, a, n, v); }
+int arecBackProject2D_SQ(arecImage i, float *a, int n, arecImage *v) { return arecgb_arecBackProject2D_SQ(i, a, n, v); }
+int cyl_sirt(MPI_Comm m, arecImage i, float *a, arecImage *x, float l, int it, float t) { return arecgb_cyl_sirt(m, i, a, x, l, it, t); }
+int cyl_sirt_KB(MPI_Comm m, arecImage i, float *a, arecImage *x, float l, int it, float t) { return arecgb_cyl_sirt_KB(m, i, a, x, l, it, t); }
+int cyl_sirt_SQ(MPI_Comm m, arecImage i, float *a, arecImage *x, float l, int it, float t) { return arecgb_cyl_sirt_SQ(m, i, a, x, l, it, t); }
+int cyl_cgls(MPI_Comm m, arecImage i, float *a, arecImage *x, float l, int it, float t) { return arecgb_cyl_cgls(m, i, a, x, l, it, t); }
+int cyl_cgls_KB(MPI_Comm m, arecImage i, float *a, arecImage *x, float l, int it, float t) { return arecgb_cyl_cgls_KB(m, i, a, x, l, it, t); }
+int cyl_cgls_SQ(MPI_Comm m, arecImage i, float *a, arecImage *x, float l, int it, float t) { return arecgb_cyl_cgls_SQ(m, i, a, x, l, it, t); }
+int arecCCImages(MPI_Comm m, arecImage a, arecImage b, float *sx, float *sy) { return arecgb_arecCCImages(m, a, b, sx, sy); }
+void ccorr2d(int nx, int ny, float *x, float *y, float *c) { arecgb_ccorr2d(nx, ny, x, y, c); }
+void speak(int nx, int ny, float *d, float *xt, float *yt) { arecgb_speak(nx, ny, d, xt, yt); }

@@ -1,0 +1,557 @@
+// FFT cross-correlation shift search (reference arecCCImages,
+// AREC3D/AREC3D/arecImage.cpp:384-434 = ccorr2d + speak per image pair,
+// AREC3D/AREC3D/align2dstack.cpp:480-521, 1059-1166).
+//
+//   c = IDFT2( conj(DFT2 x) * DFT2 y )   (unnormalised, [ny][nx], real)
+//   peak = speak(c): |c| argmax with the reference's scan-order rules,
+//          3x3 paraboloid fit, wrap to (-n/2, n/2].
+//
+// Pipeline per batch of image pairs (all FP32, power-of-two sizes 16..4096):
+//   1. rows:    z = x + i*y, complex FFT of each row (one transform gives the
+//               row spectra of both real images), split into the half spectra
+//               Xh, Yh [ny][nx/2+1] (Hermitian symmetry).
+//   2. columns: column FFTs of Xh and Yh, C = conj(X)*Y, inverse column FFT,
+//               written back over Xh (each block owns its columns).
+//   3. rows:    Hermitian row -> inverse complex FFT -> c (real part), with
+//               per-row peak statistics fused.
+//   4. peak:    one block per pair reduces the row statistics exactly in the
+//               reference's x-major scan order and fits the paraboloid in FP64.
+// FFTs run in shared memory: mixed-radix Stockham passes (radix 16 and one
+// radix-2/4/8 pass), one radix-16 butterfly per thread per pass held in
+// registers, twiddles from a per-length table computed in double on the host.
+#include <math.h>
+
+#include <algorithm>
+#include <climits>
+#include <cmath>
+#include <map>
+#include <mutex>
+#include <vector>
+
+#include "arec_internal.cuh"
+
+namespace arecgb {
+
+__device__ __forceinline__ float2 cmul(float2 a, float2 b) {
+    return make_float2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
+}
+
+// In-register radix-R DFT (forward sign) of v[off .. off+R), iterative DIT.
+template <int R>
+__device__ __forceinline__ void dft_reg(float2 *v) {
+    constexpr int LOG = R == 2 ? 1 : R == 4 ? 2 : R == 8 ? 3 : 4;
+    // cos/sin(2*pi*m/16), m = 0..7
+    const float C16[8] = {1.0f, 0.92387953251128676f, 0.70710678118654752f,
+                          0.38268343236508977f, 0.0f, -0.38268343236508977f,
+                          -0.70710678118654752f, -0.92387953251128676f};
+    const float S16[8] = {0.0f, 0.38268343236508977f, 0.70710678118654752f,
+                          0.92387953251128676f, 1.0f, 0.92387953251128676f,
+                          0.70710678118654752f, 0.38268343236508977f};
+#pragma unroll
+    for (int i = 0; i < R; i++) {
+        int j = 0;
+#pragma unroll
+        for (int bbit = 0; bbit < LOG; bbit++) j |= ((i >> bbit) & 1) << (LOG - 1 - bbit);
+        if (i < j) {
+            float2 t = v[i];
+            v[i] = v[j];
+            v[j] = t;
+        }
+    }
+#pragma unroll
+    for (int len = 2; len <= R; len <<= 1) {
+        const int half = len >> 1;
+#pragma unroll
+        for (int s = 0; s < R; s += len) {
+#pragma unroll
+            for (int k = 0; k < half; k++) {
+                const int m = k * (16 / len);
+                const float c = C16[m], sn = S16[m];
+                const float2 a = v[s + k], b = v[s + k + half];
+                // b * exp(-2*pi*i*k/len)
+                const float2 bw = make_float2(b.x * c + b.y * sn, b.y * c - b.x * sn);
+                v[s + k] = make_float2(a.x + bw.x, a.y + bw.y);
+                v[s + k + half] = make_float2(a.x - bw.x, a.y - bw.y);
+            }
+        }
+    }
+}
+
+template <int R>
+__device__ __forceinline__ void stockham_pass(float2 *L, int N, int Ns, int b, bool active,
+                                              const float2 *__restrict__ tw) {
+    constexpr int NBT = 16 / R;
+    const int NR = N / R;
+    float2 v[16];
+    if (active) {
+#pragma unroll
+        for (int i = 0; i < NBT; i++) {
+            const int j = b * NBT + i;
+            const int k = j % Ns;
+            const int step = N / (Ns * R);
+#pragma unroll
+            for (int r = 0; r < R; r++) {
+                const float2 x = L[j + r * NR];
+                const float2 w = __ldg(&tw[(r * k * step) & (N - 1)]);
+                v[i * R + r] = cmul(x, w);
+            }
+        }
+    }
+    __syncthreads();
+    if (active) {
+#pragma unroll
+        for (int i = 0; i < NBT; i++) {
+            dft_reg<R>(v + i * R);
+            const int j = b * NBT + i;
+            const int k = j % Ns;
+            const int d = (j / Ns) * Ns * R + k;
+#pragma unroll
+            for (int r = 0; r < R; r++) L[d + r * Ns] = v[i * R + r];
+        }
+    }
+    __syncthreads();
+}
+
+// In-place forward FFT of G lines of length N (power of two, 16..4096) held in
+// shared memory at buf + l*lstride.  N/16 threads per line; all threads of the
+// block must call it.
+__device__ void fft_lines(float2 *buf, int N, int lstride, int G, const float2 *tw) {
+    const int tpl = N / 16;
+    const int line = threadIdx.x / tpl, b = threadIdx.x % tpl;
+    const bool active = line < G;
+    float2 *L = buf + (size_t)(active ? line : 0) * lstride;
+    for (int Ns = 1; Ns < N;) {
+        const int R = min(16, N / Ns);
+        if (R == 16) stockham_pass<16>(L, N, Ns, b, active, tw);
+        else if (R == 8) stockham_pass<8>(L, N, Ns, b, active, tw);
+        else if (R == 4) stockham_pass<4>(L, N, Ns, b, active, tw);
+        else stockham_pass<2>(L, N, Ns, b, active, tw);
+        Ns *= R;
+    }
+}
+
+// ---------------------------------------------------------------------------
+struct RowStat {
+    float m;   // max |c| over the row
+    int xpos;  // first x with c == +m (INT_MAX if none)
+    int xneg;  // last x with c == -m (-1 if none)
+    int pad;
+};
+
+// Pass 1: rows of z = x + i*y -> half spectra of x and y.
+__global__ void __launch_bounds__(256) k_cc_rows_fwd(const float *__restrict__ x,
+                                                     const float *__restrict__ y,
+                                                     float2 *__restrict__ Xh,
+                                                     float2 *__restrict__ Yh, int nx, int ny,
+                                                     const float2 *__restrict__ tw) {
+    extern __shared__ float2 sm[];
+    const int G = 4096 / nx < 256 / (nx / 16) ? 4096 / nx : 256 / (nx / 16);
+    const int row0 = blockIdx.x * G, pair = blockIdx.y;
+    const int H = nx / 2 + 1;
+    const size_t img = (size_t)pair * nx * ny;
+    for (int i = threadIdx.x; i < G * nx; i += blockDim.x) {
+        const int l = i / nx, c = i % nx, row = row0 + l;
+        float2 z = make_float2(0.f, 0.f);
+        if (row < ny) z = make_float2(x[img + (size_t)row * nx + c], y[img + (size_t)row * nx + c]);
+        sm[l * nx + c] = z;
+    }
+    __syncthreads();
+    fft_lines(sm, nx, nx, G, tw);
+    const size_t half = (size_t)pair * ny * H;
+    for (int i = threadIdx.x; i < G * H; i += blockDim.x) {
+        const int l = i / H, k = i % H, row = row0 + l;
+        if (row >= ny) continue;
+        const float2 Z = sm[l * nx + k], Zm = sm[l * nx + ((nx - k) & (nx - 1))];
+        Xh[half + (size_t)row * H + k] = make_float2(0.5f * (Z.x + Zm.x), 0.5f * (Z.y - Zm.y));
+        Yh[half + (size_t)row * H + k] = make_float2(0.5f * (Z.y + Zm.y), -0.5f * (Z.x - Zm.x));
+    }
+}
+
+// Pass 2: columns.  CT columns of Xh and Yh per block; W = IDFT_col(conj(X)*Y)
+// overwrites Xh.
+constexpr int kColTile = 4;
+__global__ void __launch_bounds__(256) k_cc_cols(float2 *__restrict__ Xh,
+                                                 const float2 *__restrict__ Yh, int nx, int ny,
+                                                 const float2 *__restrict__ tw) {
+    extern __shared__ float2 sm[];
+    const int H = nx / 2 + 1;
+    const int c0 = blockIdx.x * kColTile, pair = blockIdx.y;
+    const int nc = min(kColTile, H - c0);
+    const size_t half = (size_t)pair * ny * H;
+    float2 *sx = sm, *sy = sm + kColTile * ny;
+    for (int i = threadIdx.x; i < kColTile * ny; i += blockDim.x) {
+        const int row = i / kColTile, c = i % kColTile;
+        float2 a = make_float2(0.f, 0.f), b = a;
+        if (c < nc) {
+            a = Xh[half + (size_t)row * H + c0 + c];
+            b = Yh[half + (size_t)row * H + c0 + c];
+        }
+        sx[c * ny + row] = a;
+        sy[c * ny + row] = b;
+    }
+    __syncthreads();
+    const int G = max(1, 256 / (ny / 16));
+    for (int l0 = 0; l0 < 2 * kColTile; l0 += G)
+        fft_lines(sm + (size_t)l0 * ny, ny, ny, min(G, 2 * kColTile - l0), tw);
+    // conj(X)*Y, conjugated again for the inverse transform (IDFT = conj DFT conj)
+    for (int i = threadIdx.x; i < kColTile * ny; i += blockDim.x) {
+        const float2 a = sx[i], b = sy[i];
+        const float2 cc = make_float2(a.x * b.x + a.y * b.y, a.x * b.y - a.y * b.x);
+        sx[i] = make_float2(cc.x, -cc.y);
+    }
+    __syncthreads();
+    for (int l0 = 0; l0 < kColTile; l0 += G)
+        fft_lines(sm + (size_t)l0 * ny, ny, ny, min(G, kColTile - l0), tw);
+    for (int i = threadIdx.x; i < kColTile * ny; i += blockDim.x) {
+        const int row = i / kColTile, c = i % kColTile;
+        if (c < nc) {
+            const float2 w = sx[c * ny + row];
+            Xh[half + (size_t)row * H + c0 + c] = make_float2(w.x, -w.y);
+        }
+    }
+}
+
+// Combine two row statistics in favour of the reference's scan order.
+__device__ __forceinline__ RowStat stat_merge(RowStat a, RowStat b) {
+    if (b.m > a.m) return b;
+    if (a.m > b.m) return a;
+    RowStat r = a;
+    r.xpos = min(a.xpos, b.xpos);
+    r.xneg = max(a.xneg, b.xneg);
+    return r;
+}
+
+// Pass 3: inverse row transforms -> c rows, with per-row peak statistics.
+__global__ void __launch_bounds__(256) k_cc_rows_inv(const float2 *__restrict__ Wh,
+                                                     float *__restrict__ c, RowStat *stats,
+                                                     int nx, int ny,
+                                                     const float2 *__restrict__ tw) {
+    extern __shared__ float2 sm[];
+    const int G = 4096 / nx < 256 / (nx / 16) ? 4096 / nx : 256 / (nx / 16);
+    const int row0 = blockIdx.x * G, pair = blockIdx.y;
+    const int H = nx / 2 + 1;
+    const size_t half = (size_t)pair * ny * H;
+    for (int i = threadIdx.x; i < G * nx; i += blockDim.x) {
+        const int l = i / nx, k = i % nx, row = row0 + l;
+        float2 w = make_float2(0.f, 0.f);
+        if (row < ny) {
+            if (k < H) {
+                w = Wh[half + (size_t)row * H + k];
+                w.y = -w.y;  // conj for the inverse
+            } else {
+                w = Wh[half + (size_t)row * H + (nx - k)];  // conj(conj(W[nx-k]))
+            }
+        }
+        sm[l * nx + k] = w;
+    }
+    __syncthreads();
+    fft_lines(sm, nx, nx, G, tw);
+    // one warp per row for the statistics
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const size_t img = (size_t)pair * nx * ny;
+    for (int l = warp; l < G; l += blockDim.x / 32) {
+        const int row = row0 + l;
+        if (row >= ny) continue;
+        RowStat s{-1.0f, INT_MAX, -1, 0};
+        for (int i = lane; i < nx; i += 32) {
+            const float v = sm[l * nx + i].x;
+            if (c) c[img + (size_t)row * nx + i] = v;
+            const float a = fabsf(v);
+            RowStat t{a, v == a && a == a ? i : INT_MAX, v == -a && v != a ? i : -1, 0};
+            if (!(a == a)) t = RowStat{-1.0f, INT_MAX, -1, 0};  // NaN never wins
+            s = stat_merge(s, t);
+        }
+        for (int o = 16; o > 0; o >>= 1) {
+            RowStat t;
+            t.m = __shfl_down_sync(0xffffffffu, s.m, o);
+            t.xpos = __shfl_down_sync(0xffffffffu, s.xpos, o);
+            t.xneg = __shfl_down_sync(0xffffffffu, s.xneg, o);
+            t.pad = 0;
+            s = stat_merge(s, t);
+        }
+        if (lane == 0) stats[(size_t)pair * ny + row] = s;
+    }
+}
+
+// Row statistics of an existing image (for speak on a given correlation map).
+__global__ void __launch_bounds__(256) k_row_stats(const float *__restrict__ c, RowStat *stats,
+                                                   int nx, int ny) {
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int row = blockIdx.x * 8 + warp, pair = blockIdx.y;
+    if (row >= ny) return;
+    const float *cr = c + ((size_t)pair * ny + row) * nx;
+    RowStat s{-1.0f, INT_MAX, -1, 0};
+    for (int i = lane; i < nx; i += 32) {
+        const float v = cr[i];
+        const float a = fabsf(v);
+        RowStat t{a, v == a ? i : INT_MAX, (v == -a && v != a) ? i : -1, 0};
+        if (!(a == a)) t = RowStat{-1.0f, INT_MAX, -1, 0};
+        s = stat_merge(s, t);
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+        RowStat t;
+        t.m = __shfl_down_sync(0xffffffffu, s.m, o);
+        t.xpos = __shfl_down_sync(0xffffffffu, s.xpos, o);
+        t.xneg = __shfl_down_sync(0xffffffffu, s.xneg, o);
+        t.pad = 0;
+        s = stat_merge(s, t);
+    }
+    if (lane == 0) stats[(size_t)pair * ny + row] = s;
+}
+
+// quad2dfit (align2dstack.cpp:1125-1166) in double.
+__device__ void quad2dfit_dev(const float *z, float *xsh, float *ysh) {
+#define Z(i, j) ((double)z[((j)-1) * 3 + (i)-1])
+    const double c2 = (8. * Z(1, 1) - 8. * Z(1, 2) + 5. * Z(2, 1) - 8. * Z(2, 2) + 3. * Z(2, 3) +
+                       2. * Z(3, 1) - 8. * Z(3, 2) + 6. * Z(3, 3)) /
+                      (-6.);
+    const double c3 = (Z(1, 1) - 2. * Z(1, 2) + Z(1, 3) + Z(2, 1) - 2. * Z(2, 2) + Z(2, 3) +
+                       Z(3, 1) - 2. * Z(3, 2) + Z(3, 3)) /
+                      6.0;
+    const double c4 = (8. * Z(1, 1) + 5. * Z(1, 2) + 2. * Z(1, 3) - 8. * Z(2, 1) - 8. * Z(2, 2) -
+                       8. * Z(2, 3) + 3. * Z(3, 2) + 6. * Z(3, 3)) /
+                      (-6.0);
+    const double c5 = (Z(1, 1) - Z(1, 3) - Z(3, 1) + Z(3, 3)) / 4.0;
+    const double c6 = (Z(1, 1) + Z(1, 2) + Z(1, 3) - 2. * Z(2, 1) - 2. * Z(2, 2) - 2. * Z(2, 3) +
+                       Z(3, 1) + Z(3, 2) + Z(3, 3)) /
+                      6.0;
+#undef Z
+    float ys = 0.0f, xs = 0.0f;
+    const double den = 4. * c3 * c6 - c5 * c5;
+    if (den != 0.0) {
+        ys = (float)((c4 * c5 - 2. * c2 * c6) / den - 2.0);
+        xs = (float)((c2 * c5 - 2. * c4 * c3) / den - 2.0);
+        if (ys < -1.0f) ys = -1.0f;
+        if (ys > 1.0f) ys = 1.0f;
+        if (xs < -1.0f) xs = -1.0f;
+        if (xs > 1.0f) xs = 1.0f;
+    }
+    *xsh = xs;
+    *ysh = ys;
+}
+
+// Pass 4: the reference's peak (speak, align2dstack.cpp:1072-1079) scans x
+// outer, y inner, replacing the peak when |v| > pmax and then storing the
+// SIGNED v.  Hence: if +M (M = max|v|) occurs, the answer is its first
+// occurrence in that order; otherwise the scan passes the last -M and, with
+// pmax negative, continues from the next element; that rare case is replayed
+// element by element (bounded by the image size).
+__global__ void __launch_bounds__(256) k_peak(const float *__restrict__ c,
+                                              const RowStat *__restrict__ stats, int nx, int ny,
+                                              float *sx, float *sy, int *ixo, int *iyo) {
+    __shared__ float sm_m[256];
+    __shared__ long long sm_pos[256], sm_neg[256];
+    const int pair = blockIdx.x;
+    const RowStat *st = stats + (size_t)pair * ny;
+    const float *cp = c + (size_t)pair * nx * ny;
+    float m = -1.0f;
+    for (int r = threadIdx.x; r < ny; r += 256) m = fmaxf(m, st[r].m);
+    sm_m[threadIdx.x] = m;
+    __syncthreads();
+    for (int o = 128; o > 0; o >>= 1) {
+        if ((int)threadIdx.x < o) sm_m[threadIdx.x] = fmaxf(sm_m[threadIdx.x], sm_m[threadIdx.x + o]);
+        __syncthreads();
+    }
+    const float M = sm_m[0];
+    // order key in x-major scan order: x * ny + y
+    long long pos = LLONG_MAX, neg = -1;
+    for (int r = threadIdx.x; r < ny; r += 256) {
+        const RowStat s = st[r];
+        if (s.m == M) {
+            if (s.xpos != INT_MAX) pos = min(pos, (long long)s.xpos * ny + r);
+            if (s.xneg >= 0) neg = max(neg, (long long)s.xneg * ny + r);
+        }
+    }
+    sm_pos[threadIdx.x] = pos;
+    sm_neg[threadIdx.x] = neg;
+    __syncthreads();
+    for (int o = 128; o > 0; o >>= 1) {
+        if ((int)threadIdx.x < o) {
+            sm_pos[threadIdx.x] = min(sm_pos[threadIdx.x], sm_pos[threadIdx.x + o]);
+            sm_neg[threadIdx.x] = max(sm_neg[threadIdx.x], sm_neg[threadIdx.x + o]);
+        }
+        __syncthreads();
+    }
+    if (threadIdx.x != 0) return;
+    long long t;
+    if (!(M > 0.0f)) {
+        t = 0;  // nothing exceeds pmax = 0 (the reference leaves the peak undefined)
+    } else if (sm_pos[0] != LLONG_MAX) {
+        t = sm_pos[0];
+    } else {
+        // replay the reference's state machine after the last -M
+        t = sm_neg[0];
+        float pmax = -M;
+        const long long n = (long long)nx * ny;
+        for (long long u = t + 1; u < n; u++) {
+            const int xx = (int)(u / ny), yy = (int)(u % ny);
+            const float v = cp[(size_t)yy * nx + xx];
+            if (fabsf(v) > pmax) {
+                pmax = v;
+                t = u;
+            }
+        }
+    }
+    const int ix = (int)(t / ny), iy = (int)(t % ny);  // 0-based
+    float z[9];
+    for (int j = -1; j <= 1; j++)
+        for (int i = -1; i <= 1; i++) {
+            const int xc = (ix + i + nx) % nx, yc = (iy + j + ny) % ny;
+            z[(j + 1) * 3 + (i + 1)] = cp[(size_t)yc * nx + xc];
+        }
+    float xsh, ysh;
+    quad2dfit_dev(z, &xsh, &ysh);
+    float xt = xsh + (float)ix, yt = ysh + (float)iy;
+    if (xt > (float)(nx / 2)) xt = xt - (float)nx;
+    if (yt > (float)(ny / 2)) yt = yt - (float)ny;
+    sx[pair] = xt;
+    sy[pair] = yt;
+    if (ixo) ixo[pair] = ix;
+    if (iyo) iyo[pair] = iy;
+}
+
+// ---------------------------------------------------------------------------
+// Host side.
+
+static std::mutex g_tw_mu;
+static std::map<std::pair<int, int>, float2 *> g_tw;  // (device, N) -> table
+
+static int twiddles(int N, const float2 **out) {
+    int dev = 0;
+    cudaGetDevice(&dev);
+    std::lock_guard<std::mutex> lk(g_tw_mu);
+    auto it = g_tw.find({dev, N});
+    if (it != g_tw.end()) {
+        *out = it->second;
+        return 0;
+    }
+    std::vector<float2> h(N);
+    for (int k = 0; k < N; k++) {
+        const double a = 2.0 * M_PI * (double)k / (double)N;
+        h[k] = make_float2((float)std::cos(a), (float)-std::sin(a));
+    }
+    float2 *d = nullptr;
+    ARECGB_CUDA(cudaMalloc(&d, sizeof(float2) * N));
+    ARECGB_CUDA(cudaMemcpy(d, h.data(), sizeof(float2) * N, cudaMemcpyHostToDevice));
+    g_tw[{dev, N}] = d;
+    *out = d;
+    return 0;
+}
+
+static bool pow2_ok(int n) { return n >= 16 && n <= 4096 && (n & (n - 1)) == 0; }
+
+static int rows_per_block(int nx) { return std::min(4096 / nx, 256 / (nx / 16)); }
+
+static int set_smem(const void *fn, size_t bytes) {
+    ARECGB_CUDA(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes));
+    return 0;
+}
+
+// Correlate `np` pairs; optionally keep the correlation images in `c`
+// (np*ny*nx floats) and/or reduce them to peaks.
+static int correlate_batch(const float *d1, const float *d2, int np, int ny, int nx, float *c,
+                           RowStat *stats, float2 *Xh, float2 *Yh, cudaStream_t st) {
+    const float2 *twx, *twy;
+    int rc = twiddles(nx, &twx);
+    if (!rc) rc = twiddles(ny, &twy);
+    if (rc) return rc;
+    const int G = rows_per_block(nx);
+    const size_t row_smem = sizeof(float2) * (size_t)G * nx;
+    const size_t col_smem = sizeof(float2) * 2 * kColTile * (size_t)ny;
+    if ((rc = set_smem((const void *)k_cc_rows_fwd, row_smem))) return rc;
+    if ((rc = set_smem((const void *)k_cc_rows_inv, row_smem))) return rc;
+    if ((rc = set_smem((const void *)k_cc_cols, col_smem))) return rc;
+    const int H = nx / 2 + 1;
+    k_cc_rows_fwd<<<dim3((ny + G - 1) / G, np), 256, row_smem, st>>>(d1, d2, Xh, Yh, nx, ny, twx);
+    k_cc_cols<<<dim3((H + kColTile - 1) / kColTile, np), 256, col_smem, st>>>(Xh, Yh, nx, ny, twy);
+    k_cc_rows_inv<<<dim3((ny + G - 1) / G, np), 256, row_smem, st>>>(Xh, c, stats, nx, ny, twx);
+    ARECGB_CUDA(cudaGetLastError());
+    return 0;
+}
+
+struct CcScratch {
+    float2 *Xh = nullptr, *Yh = nullptr;
+    float *c = nullptr;
+    RowStat *stats = nullptr;
+};
+
+static void cc_free(CcScratch &s) {
+    cudaFree(s.Xh);
+    cudaFree(s.Yh);
+    cudaFree(s.c);
+    cudaFree(s.stats);
+}
+
+static int cc_alloc(CcScratch &s, int np, int ny, int nx, bool need_c) {
+    const size_t H = nx / 2 + 1;
+    ARECGB_CUDA(cudaMalloc(&s.Xh, sizeof(float2) * H * ny * np));
+    ARECGB_CUDA(cudaMalloc(&s.Yh, sizeof(float2) * H * ny * np));
+    if (need_c) ARECGB_CUDA(cudaMalloc(&s.c, sizeof(float) * (size_t)nx * ny * np));
+    ARECGB_CUDA(cudaMalloc(&s.stats, sizeof(RowStat) * (size_t)ny * np));
+    return 0;
+}
+
+int cc_shifts(const float *d1, const float *d2, int nz, int ny, int nx, float *sx, float *sy,
+              int *ix, int *iy, cudaStream_t st) {
+    if (!pow2_ok(nx) || !pow2_ok(ny) || nz < 0 || !d1 || !d2 || !sx || !sy) {
+        set_error("cc_shifts: nx and ny must be powers of two in [16, 4096]");
+        return ARECGB_ERR_ARG;
+    }
+    if (nz == 0) return 0;
+    // pairs per batch: keep the scratch near 1 GiB
+    const size_t per_pair = (size_t)ny * ((size_t)(nx / 2 + 1) * 16 + (size_t)nx * 4 + 16);
+    const int batch = (int)std::max<size_t>(1, std::min<size_t>(nz, (1ull << 30) / per_pair));
+    CcScratch s;
+    int rc = cc_alloc(s, batch, ny, nx, true);
+    for (int p0 = 0; !rc && p0 < nz; p0 += batch) {
+        const int np = std::min(batch, nz - p0);
+        const size_t off = (size_t)p0 * nx * ny;
+        rc = correlate_batch(d1 + off, d2 + off, np, ny, nx, s.c, s.stats, s.Xh, s.Yh, st);
+        if (rc) break;
+        k_peak<<<np, 256, 0, st>>>(s.c, s.stats, nx, ny, sx + p0, sy + p0, ix ? ix + p0 : nullptr,
+                                   iy ? iy + p0 : nullptr);
+        cudaError_t e = cudaGetLastError();
+        if (e != cudaSuccess) {
+            set_error(std::string("cc_shifts: ") + cudaGetErrorString(e));
+            rc = cuda_status(e);
+        }
+    }
+    cudaStreamSynchronize(st);
+    cc_free(s);
+    return rc;
+}
+
+int ccorr_image(const float *dx, const float *dy, float *dc, int ny, int nx, cudaStream_t st) {
+    if (!pow2_ok(nx) || !pow2_ok(ny)) {
+        set_error("ccorr2d: nx and ny must be powers of two in [16, 4096]");
+        return ARECGB_ERR_ARG;
+    }
+    CcScratch s;
+    int rc = cc_alloc(s, 1, ny, nx, false);
+    if (!rc) rc = correlate_batch(dx, dy, 1, ny, nx, dc, s.stats, s.Xh, s.Yh, st);
+    cudaStreamSynchronize(st);
+    cc_free(s);
+    return rc;
+}
+
+int peak_search(const float *dc, int nz, int ny, int nx, float *sx, float *sy, int *ix, int *iy,
+                cudaStream_t st) {
+    if (nx < 1 || ny < 1 || nz < 1) {
+        set_error("speak: bad shape");
+        return ARECGB_ERR_ARG;
+    }
+    RowStat *stats = nullptr;
+    ARECGB_CUDA(cudaMalloc(&stats, sizeof(RowStat) * (size_t)ny * nz));
+    k_row_stats<<<dim3((ny + 7) / 8, nz), 256, 0, st>>>(dc, stats, nx, ny);
+    k_peak<<<nz, 256, 0, st>>>(dc, stats, nx, ny, sx, sy, ix, iy);
+    cudaError_t e = cudaGetLastError();
+    cudaStreamSynchronize(st);
+    cudaFree(stats);
+    if (e != cudaSuccess) {
+        set_error(std::string("speak: ") + cudaGetErrorString(e));
+        return cuda_status(e);
+    }
+    return 0;
+}
+
+}  // namespace arecgb

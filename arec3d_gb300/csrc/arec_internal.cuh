@@ -1,0 +1,127 @@
+// Internal definitions shared by the CUDA translation units of libarec_gb300.
+//
+// Data layout in HBM (slice index fastest everywhere, `ys` = slice count padded
+// to a multiple of 8 so every row starts on 32 bytes and a lane's vector of
+// 1/2/4/8 slices never straddles the padded end):
+//   volume     x[ray][ys]        rays of the cylinder in the reference's order
+//                                (iz-major, ix-minor; AREC3D/AREC3D/arecImage.cpp:72-84)
+//   sinogram   q[angle][bin][ys] detector bin before slice (the reference keeps
+//                                [angle][slice][bin]; the boundary transposes)
+// Padding slices are zero on input and stay zero through every operator.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "arec_gb300.h"
+
+namespace arecgb {
+
+// ---------------------------------------------------------------------------
+// Per-angle constants, computed on the host in double like the reference and
+// rounded once to float.
+struct AngleParams {
+    float c, s;          // cosf/sinf of the float angle: exact floats (see arec_geometry.cu)
+    float sq_a, sq_b;    // square-pixel footprint breakpoints (arecproject.h:11-22)
+    float sq_aeps;       // a + 1e-3: the linear piece's test bound (arecproject.h:34)
+    float sq_ymax;       // plateau height 1/(b+a)
+    float sq_c2;         // 0.5*ymax*(b+a): intercept of the linear piece
+    float sq_k1;         // 0.5*ymax/(b-a): curvature of the quadratic pieces
+    int orient;          // 0: sweep rows (|c| >= |s|), 1: sweep columns
+    float pad[3];
+};
+
+struct RowInfo {
+    int start;  // ray index of the first pixel of row iz
+    int lo, hi; // first/last ix of the row inside the cylinder
+    int pad;
+};
+
+struct ColInfo {
+    int lo, hi; // first/last iz of column ix inside the cylinder
+};
+
+struct Plan {
+    int weighting = 0;   // ARECGB_LIN / ARECGB_KB / ARECGB_SQ
+    double radius = 0;
+    int nx = 0, nrays = 0, ny = 0, ys = 0, na = 0;
+    float r_hi = 0, r_lo = 0;   // centre (radius, or (int)radius+1 for LIN) as a float pair
+    std::vector<float> angles;
+    int device = 0;
+
+    // device tables
+    float4 *d_ray = nullptr;      // per ray: (xc_hi, zc_hi, xc_lo, zc_lo) offsets from the centre
+    AngleParams *d_ang = nullptr;
+    RowInfo *d_rows = nullptr;    // nx rows
+    ColInfo *d_cols = nullptr;    // nx columns
+    int4 *d_groups = nullptr;     // forward-projection angle groups: (first, count, orient, 0)
+    int ngroups = 0;
+    int2 *d_tiles = nullptr;      // back-projection ray tiles: (ix0, iz0) of 8x4-pixel tiles
+    int ntiles = 0;
+    int *d_err = nullptr;         // device error flag (nonzero: a kernel saw an impossible case)
+
+    // launch shapes (set at creation; see arec_project.cu)
+    int vec = 4;                  // floats per lane along slices
+    int fp_bins = 16;             // detector bins per forward-projection block
+    int bp_rays = 32;             // rays per back-projection block
+
+    // FP64 reduction partial sums (one per block of FP / BP)
+    double *d_partials = nullptr;
+    int n_partials = 0;
+
+    // scratch owned by the plan for the reference-compatible entry points
+    float *d_vol[4] = {nullptr, nullptr, nullptr, nullptr};
+    float *d_sin[3] = {nullptr, nullptr, nullptr};
+    float *d_stage = nullptr;      // staging buffer in the reference layout
+    size_t stage_floats = 0;
+    float *h_pinned = nullptr;     // pinned host staging
+    size_t pinned_floats = 0;
+
+    cudaStream_t stream = nullptr; // plan-owned stream for the compatible entry points
+};
+
+constexpr int kTileX = 8, kTileZ = 4;  // back-projection ray tile (32 rays)
+constexpr int kGroupAngles = 4;        // angles per forward-projection block
+constexpr int kFpBins = 8;             // detector bins per forward-projection block
+
+// Geometry / plans (arec_geometry.cu)
+int plan_create(Plan **out, int weighting, double radius, int ny, int nangles,
+                const float *angles_host);
+void plan_destroy(Plan *p);
+size_t vol_floats(const Plan *p);
+size_t sin_floats(const Plan *p);
+
+// Operators (arec_project.cu)
+int forward_project(const Plan *p, const float *d_x, float *d_q, double *d_norm2,
+                    const int *d_skip, cudaStream_t st);
+int back_project(const Plan *p, const float *d_s, float *d_g, double *d_norm2,
+                 const int *d_skip, cudaStream_t st);
+int fp_grid_blocks(const Plan *p);
+int bp_grid_blocks(const Plan *p);
+
+// Layout kernels and vector ops (arec_vector.cu)
+int sino_to_device_layout(const float *d_ref, float *d_dev, int na, int ny, int nx, int ys,
+                          cudaStream_t st);
+int sino_to_reference_layout(const float *d_dev, float *d_ref, int na, int ny, int nx, int ys,
+                             cudaStream_t st);
+int reduce_partials(const double *d_partials, int n, double *d_out, cudaStream_t st);
+
+// error helpers
+int cuda_status(cudaError_t e);
+void set_error(const std::string &msg);
+
+#define ARECGB_CUDA(call)                                        \
+    do {                                                         \
+        cudaError_t e__ = (call);                                \
+        if (e__ != cudaSuccess) {                                \
+            ::arecgb::set_error(std::string(#call) + ": " +      \
+                                cudaGetErrorString(e__));        \
+            return ::arecgb::cuda_status(e__);                   \
+        }                                                        \
+    } while (0)
+
+}  // namespace arecgb

@@ -1,0 +1,16 @@
+// Projector instantiations for weighting ARECGB_SQ (see arec_project_impl.cuh).
+#include "arec_project_impl.cuh"
+
+namespace arecgb {
+
+int launch_bp_sq(const OpArgs &A, int vec, int nsc, dim3 grid, const float *s, float *g,
+               cudaStream_t st) {
+    return launch_bp<ARECGB_SQ>(A, vec, nsc, grid, s, g, st);
+}
+
+int launch_fp_sq(const OpArgs &A, int vec, int nsc, dim3 grid, const float *x, float *q,
+               cudaStream_t st) {
+    return launch_fp<ARECGB_SQ, kFpBins>(A, vec, nsc, grid, x, q, st);
+}
+
+}  // namespace arecgb

@@ -1,0 +1,599 @@
+// Layout conversion, FP64 reductions and the element-wise solver updates.
+// All of these are HBM-bound: grid-stride loops over float4 where the layout
+// allows, sized to a multiple of the SM count.
+#include "arec_internal.cuh"
+#include "arec_vector.cuh"
+
+#include <math.h>
+#include <stdio.h>
+
+#include <algorithm>
+#include <cmath>
+
+namespace arecgb {
+
+// ---------------------------------------------------------------------------
+// Sinogram layout: reference [na][ny][nx]  <->  device [na][nx][ys].
+// 32x32 tiles through shared memory; both sides coalesced.
+__global__ void __launch_bounds__(256)
+    k_sino_to_dev(const float *__restrict__ in, float *__restrict__ out, int ny, int nx, int ys) {
+    __shared__ float t[32][33];
+    const int a = blockIdx.z;
+    const int x0 = blockIdx.x * 32, y0 = blockIdx.y * 32;
+    const float *ia = in + (size_t)a * ny * nx;
+    float *oa = out + (size_t)a * nx * ys;
+    for (int j = threadIdx.y; j < 32; j += 8) {
+        const int y = y0 + j, x = x0 + threadIdx.x;
+        t[j][threadIdx.x] = (y < ny && x < nx) ? ia[(size_t)y * nx + x] : 0.f;
+    }
+    __syncthreads();
+    for (int j = threadIdx.y; j < 32; j += 8) {
+        const int x = x0 + j, y = y0 + threadIdx.x;
+        if (x < nx && y < ys) oa[(size_t)x * ys + y] = t[threadIdx.x][j];
+    }
+}
+
+__global__ void __launch_bounds__(256)
+    k_sino_to_ref(const float *__restrict__ in, float *__restrict__ out, int ny, int nx, int ys) {
+    __shared__ float t[32][33];
+    const int a = blockIdx.z;
+    const int x0 = blockIdx.x * 32, y0 = blockIdx.y * 32;
+    const float *ia = in + (size_t)a * nx * ys;
+    float *oa = out + (size_t)a * ny * nx;
+    for (int j = threadIdx.y; j < 32; j += 8) {
+        const int x = x0 + j, y = y0 + threadIdx.x;
+        t[j][threadIdx.x] = (x < nx && y < ny) ? ia[(size_t)x * ys + y] : 0.f;
+    }
+    __syncthreads();
+    for (int j = threadIdx.y; j < 32; j += 8) {
+        const int y = y0 + j, x = x0 + threadIdx.x;
+        if (y < ny && x < nx) oa[(size_t)y * nx + x] = t[threadIdx.x][j];
+    }
+}
+
+int sino_to_device_layout(const float *d_ref, float *d_dev, int na, int ny, int nx, int ys,
+                          cudaStream_t st) {
+    if (na <= 0 || ny <= 0 || nx <= 0 || ys < ny || na > 65535) {
+        set_error("sino_to_device_layout: bad shape");
+        return ARECGB_ERR_ARG;
+    }
+    dim3 grid((nx + 31) / 32, (ys + 31) / 32, na);
+    k_sino_to_dev<<<grid, dim3(32, 8), 0, st>>>(d_ref, d_dev, ny, nx, ys);
+    ARECGB_CUDA(cudaGetLastError());
+    return ARECGB_OK;
+}
+
+int sino_to_reference_layout(const float *d_dev, float *d_ref, int na, int ny, int nx, int ys,
+                             cudaStream_t st) {
+    if (na <= 0 || ny <= 0 || nx <= 0 || ys < ny || na > 65535) {
+        set_error("sino_to_reference_layout: bad shape");
+        return ARECGB_ERR_ARG;
+    }
+    dim3 grid((nx + 31) / 32, (ny + 31) / 32, na);
+    k_sino_to_ref<<<grid, dim3(32, 8), 0, st>>>(d_dev, d_ref, ny, nx, ys);
+    ARECGB_CUDA(cudaGetLastError());
+    return ARECGB_OK;
+}
+
+// ---------------------------------------------------------------------------
+// Reductions.  Partial sums are combined in a fixed order, so results are
+// reproducible run to run.
+__global__ void __launch_bounds__(256) k_reduce_partials(const double *__restrict__ p, int n,
+                                                         double *__restrict__ out) {
+    __shared__ double red[256];
+    double s = 0.0;
+    for (int i = threadIdx.x; i < n; i += 256) s += p[i];
+    red[threadIdx.x] = s;
+    __syncthreads();
+    for (int o = 128; o > 0; o >>= 1) {
+        if ((int)threadIdx.x < o) red[threadIdx.x] += red[threadIdx.x + o];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) *out = red[0];
+}
+
+int reduce_partials(const double *d_partials, int n, double *d_out, cudaStream_t st) {
+    k_reduce_partials<<<1, 256, 0, st>>>(d_partials, n, d_out);
+    ARECGB_CUDA(cudaGetLastError());
+    return ARECGB_OK;
+}
+
+// sum(v*v): float products accumulated in double (reference areccgls.cpp:390-391).
+__global__ void __launch_bounds__(256) k_sumsq(const float *__restrict__ v, size_t n,
+                                               double *__restrict__ partials) {
+    __shared__ double red[8];
+    double s = 0.0;
+    for (size_t i = (size_t)blockIdx.x * 256 + threadIdx.x; i < n; i += (size_t)gridDim.x * 256)
+        s += (double)__fmul_rn(v[i], v[i]);
+    for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = s;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double t = 0.0;
+        for (int w = 0; w < 8; w++) t += red[w];
+        partials[blockIdx.x] = t;
+    }
+}
+
+int sumsq_partials(const float *d_v, size_t n, double *d_partials, int nblocks, cudaStream_t st) {
+    k_sumsq<<<nblocks, 256, 0, st>>>(d_v, n, d_partials);
+    ARECGB_CUDA(cudaGetLastError());
+    return ARECGB_OK;
+}
+
+// ---------------------------------------------------------------------------
+// CGLS (reference cyl_cgls_SQ, AREC3D/AREC3D/areccgls.cpp:375-456).  The scalar
+// state lives in device memory; every kernel of an iteration returns at once
+// when the solve has finished, so extra queued iterations cost nothing.
+
+// p = g (first iteration) or p = g + beta*p, evaluated in double, stored float
+// (areccgls.cpp:376-384).
+__global__ void __launch_bounds__(256) k_cgls_p(SolveState *S, const float *__restrict__ g,
+                                                float *__restrict__ p, size_t n4) {
+    if (S->done) return;
+    const bool first = S->iter == 1;
+    const double beta = first ? 0.0 : S->gamma / S->gamma0;
+    const float4 *g4 = reinterpret_cast<const float4 *>(g);
+    float4 *p4 = reinterpret_cast<float4 *>(p);
+    for (size_t i = (size_t)blockIdx.x * 256 + threadIdx.x; i < n4; i += (size_t)gridDim.x * 256) {
+        float4 gv = g4[i];
+        if (first) {
+            p4[i] = gv;
+        } else {
+            float4 pv = p4[i];
+            pv.x = (float)((double)gv.x + beta * (double)pv.x);
+            pv.y = (float)((double)gv.y + beta * (double)pv.y);
+            pv.z = (float)((double)gv.z + beta * (double)pv.z);
+            pv.w = (float)((double)gv.w + beta * (double)pv.w);
+            p4[i] = pv;
+        }
+    }
+}
+
+// alpha = gamma / ||A p||^2 (areccgls.cpp:389-396).
+__global__ void k_cgls_alpha(SolveState *S) {
+    if (S->done) return;
+    S->alpha = S->gamma / S->qnorm2;
+}
+
+// x += alpha*p over the volume and s -= alpha*q over the sinogram, in double,
+// stored float (areccgls.cpp:398-404).  One launch covers both arrays.
+__global__ void __launch_bounds__(256) k_cgls_xs(SolveState *S, float *__restrict__ x,
+                                                 const float *__restrict__ p, size_t nv4,
+                                                 float *__restrict__ s,
+                                                 const float *__restrict__ q, size_t ns4) {
+    if (S->done) return;
+    const double alpha = S->alpha;
+    const size_t stride = (size_t)gridDim.x * 256;
+    for (size_t i = (size_t)blockIdx.x * 256 + threadIdx.x; i < nv4 + ns4; i += stride) {
+        float4 *dst;
+        const float4 *src;
+        double a;
+        size_t j;
+        if (i < nv4) {
+            dst = reinterpret_cast<float4 *>(x);
+            src = reinterpret_cast<const float4 *>(p);
+            a = alpha;
+            j = i;
+        } else {
+            dst = reinterpret_cast<float4 *>(s);
+            src = reinterpret_cast<const float4 *>(q);
+            a = -alpha;
+            j = i - nv4;
+        }
+        float4 d = dst[j];
+        const float4 v = src[j];
+        d.x = (float)((double)d.x + a * (double)v.x);
+        d.y = (float)((double)d.y + a * (double)v.y);
+        d.z = (float)((double)d.z + a * (double)v.z);
+        d.w = (float)((double)d.w + a * (double)v.w);
+        dst[j] = d;
+    }
+}
+
+// New gamma, relative residual, best-iterate tracking and the stopping test
+// (areccgls.cpp:409-453).
+__global__ void k_cgls_gamma(SolveState *S, double *history) {
+    if (S->done) return;
+    S->gamma0 = S->gamma;
+    S->gamma = S->gnorm2;
+    const double rnorm = sqrt(S->gamma);
+    const double rel = rnorm / S->denom;
+    const int it = S->iter;
+    if (history) history[it - 1] = rel;
+    S->rel = rel;
+    S->iterations = it;
+    if (rnorm < S->rnorm_min) {
+        S->rnorm_min = rnorm;
+        S->iterbest = it;
+        S->save = 1;
+    }
+    if (rel < (double)S->tol || it >= S->maxit) S->done = 1;
+    S->iter = it + 1;
+}
+
+// xsave = x when the previous iteration improved on the best residual
+// (areccgls.cpp:423-428).  Runs at the start of the next iteration (x is
+// unchanged in between) and once more after the last one.
+__global__ void __launch_bounds__(256) k_cgls_save(SolveState *S, const float *__restrict__ x,
+                                                   float *__restrict__ xs, size_t n4) {
+    if (!S->save) return;
+    const float4 *x4 = reinterpret_cast<const float4 *>(x);
+    float4 *s4 = reinterpret_cast<float4 *>(xs);
+    for (size_t i = (size_t)blockIdx.x * 256 + threadIdx.x; i < n4; i += (size_t)gridDim.x * 256)
+        s4[i] = x4[i];
+}
+
+__global__ void k_cgls_save_done(SolveState *S) { S->save = 0; }
+
+// ---------------------------------------------------------------------------
+// SIRT (reference cyl_sirt_SQ, AREC3D/AREC3D/arecsirt.cpp:277-362).
+
+// First iteration: grad = A^T b; partial sums of float b*b and double grad^2
+// (arecsirt.cpp:285-306).
+__global__ void __launch_bounds__(256) k_sirt_first(const float *__restrict__ bvol,
+                                                    float *__restrict__ grad, size_t n,
+                                                    double *__restrict__ pb,
+                                                    double *__restrict__ pr) {
+    __shared__ double rb[8], rr[8];
+    double sb = 0.0, sr = 0.0;
+    for (size_t i = (size_t)blockIdx.x * 256 + threadIdx.x; i < n; i += (size_t)gridDim.x * 256) {
+        const float b = bvol[i];
+        grad[i] = b;
+        sb += (double)__fmul_rn(b, b);
+        sr += (double)b * (double)b;
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+        sb += __shfl_down_sync(0xffffffffu, sb, o);
+        sr += __shfl_down_sync(0xffffffffu, sr, o);
+    }
+    if ((threadIdx.x & 31) == 0) {
+        rb[threadIdx.x >> 5] = sb;
+        rr[threadIdx.x >> 5] = sr;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double tb = 0.0, tr = 0.0;
+        for (int w = 0; w < 8; w++) {
+            tb += rb[w];
+            tr += rr[w];
+        }
+        pb[blockIdx.x] = tb;
+        pr[blockIdx.x] = tr;
+    }
+}
+
+// Later iterations: grad = bvol - pvol (float); partial sums of grad^2 in double
+// (arecsirt.cpp:298-306).
+__global__ void __launch_bounds__(256) k_sirt_grad(const float *__restrict__ bvol,
+                                                   const float *__restrict__ pvol,
+                                                   float *__restrict__ grad, size_t n,
+                                                   double *__restrict__ pr) {
+    __shared__ double rr[8];
+    double sr = 0.0;
+    for (size_t i = (size_t)blockIdx.x * 256 + threadIdx.x; i < n; i += (size_t)gridDim.x * 256) {
+        const float gv = __fsub_rn(bvol[i], pvol[i]);
+        grad[i] = gv;
+        sr += (double)gv * (double)gv;
+    }
+    for (int o = 16; o > 0; o >>= 1) sr += __shfl_down_sync(0xffffffffu, sr, o);
+    if ((threadIdx.x & 31) == 0) rr[threadIdx.x >> 5] = sr;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double tr = 0.0;
+        for (int w = 0; w < 8; w++) tr += rr[w];
+        pr[blockIdx.x] = tr;
+    }
+}
+
+// x += lam*grad in float, product rounded before the sum (arecsirt.cpp:354-355).
+__global__ void __launch_bounds__(256) k_sirt_update(float *__restrict__ x,
+                                                     const float *__restrict__ grad, float lam,
+                                                     size_t n) {
+    for (size_t i = (size_t)blockIdx.x * 256 + threadIdx.x; i < n; i += (size_t)gridDim.x * 256)
+        x[i] = __fadd_rn(x[i], __fmul_rn(lam, grad[i]));
+}
+
+// ---------------------------------------------------------------------------
+int grid_for(size_t n, int per_thread) {
+    int dev = 0, sms = 152;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    size_t want = (n / per_thread + 255) / 256;
+    size_t cap = (size_t)sms * 8;
+    if (want < 1) want = 1;
+    return (int)(want < cap ? want : cap);
+}
+
+}  // namespace arecgb
+
+// ===========================================================================
+// Solver drivers.
+namespace arecgb {
+
+__global__ void k_sub(const float *__restrict__ a, const float *__restrict__ b,
+                      float *__restrict__ out, size_t n) {
+    for (size_t i = (size_t)blockIdx.x * 256 + threadIdx.x; i < n; i += (size_t)gridDim.x * 256)
+        out[i] = __fsub_rn(a[i], b[i]);
+}
+
+__global__ void k_cgls_init(SolveState *S, int maxit, float tol, double rnorm_ref) {
+    S->gamma = S->gnorm2;
+    S->gamma0 = 0.0;
+    S->alpha = 0.0;
+    S->rnorm0 = sqrt(S->gamma);
+    S->denom = rnorm_ref > 0.0 ? rnorm_ref : S->rnorm0;
+    S->rnorm_min = S->rnorm0;
+    S->rel = 1.0;
+    S->tol = tol;
+    S->iter = 1;
+    S->maxit = maxit;
+    S->iterbest = maxit - 1;
+    S->iterations = 0;
+    S->done = maxit < 1 ? 1 : 0;
+    S->save = 0;
+}
+
+static int ensure_workspace(Plan *p, int nvol, int nsin) {
+    const size_t nv = vol_floats(p), ns = sin_floats(p);
+    for (int i = 0; i < nvol; i++)
+        if (!p->d_vol[i]) {
+            ARECGB_CUDA(cudaMalloc(&p->d_vol[i], sizeof(float) * nv));
+            ARECGB_CUDA(cudaMemset(p->d_vol[i], 0, sizeof(float) * nv));
+        }
+    for (int i = 0; i < nsin; i++)
+        if (!p->d_sin[i]) {
+            ARECGB_CUDA(cudaMalloc(&p->d_sin[i], sizeof(float) * ns));
+            ARECGB_CUDA(cudaMemset(p->d_sin[i], 0, sizeof(float) * ns));
+        }
+    return ARECGB_OK;
+}
+
+struct SolverScratch {
+    SolveState *state = nullptr;
+    double *hist = nullptr;
+    double *red = nullptr;  // 2 x kRedBlocks partials + 2 scalars
+    int hist_cap = 0;
+    SolveState *h_state = nullptr;  // pinned mirror
+};
+constexpr int kRedBlocks = 1024;
+
+static int scratch_get(Plan *p, SolverScratch &sc, int maxit) {
+    // Per-call scratch: small (a few KB plus the residual history).
+    ARECGB_CUDA(cudaMalloc(&sc.state, sizeof(SolveState)));
+    sc.hist_cap = maxit > 0 ? maxit : 1;
+    ARECGB_CUDA(cudaMalloc(&sc.hist, sizeof(double) * sc.hist_cap));
+    ARECGB_CUDA(cudaMalloc(&sc.red, sizeof(double) * (2 * kRedBlocks + 2)));
+    ARECGB_CUDA(cudaMallocHost(&sc.h_state, sizeof(SolveState)));
+    (void)p;
+    return ARECGB_OK;
+}
+
+static void scratch_free(SolverScratch &sc) {
+    cudaFree(sc.state);
+    cudaFree(sc.hist);
+    cudaFree(sc.red);
+    if (sc.h_state) cudaFreeHost(sc.h_state);
+}
+
+// One CGLS iteration (reference areccgls.cpp:375-456) as a fixed launch sequence.
+static int cgls_iteration(Plan *p, SolveState *S, double *hist, float *x, float *s, float *q,
+                          float *g, float *pd, float *xs, cudaStream_t st) {
+    const size_t nv = vol_floats(p), ns = sin_floats(p);
+    const int gv = grid_for(nv, 16), gs = grid_for(nv + ns, 16);
+    k_cgls_save<<<gv, 256, 0, st>>>(S, x, xs, nv / 4);
+    k_cgls_save_done<<<1, 1, 0, st>>>(S);
+    k_cgls_p<<<gv, 256, 0, st>>>(S, g, pd, nv / 4);
+    int rc = forward_project(p, pd, q, &S->qnorm2, &S->done, st);
+    if (rc) return rc;
+    k_cgls_alpha<<<1, 1, 0, st>>>(S);
+    k_cgls_xs<<<gs, 256, 0, st>>>(S, x, pd, nv / 4, s, q, ns / 4);
+    rc = back_project(p, s, g, &S->gnorm2, &S->done, st);
+    if (rc) return rc;
+    k_cgls_gamma<<<1, 1, 0, st>>>(S, hist);
+    ARECGB_CUDA(cudaGetLastError());
+    return ARECGB_OK;
+}
+
+int cgls(Plan *p, const float *d_b, float *d_x, int warm, int maxit, float tol, double rnorm_ref,
+         double *hist_host, arecgb_solve_info *info, cudaStream_t st) {
+    int rc = ensure_workspace(p, 3, 2);
+    if (rc) return rc;
+    const size_t nv = vol_floats(p), ns = sin_floats(p);
+    float *s = p->d_sin[0], *q = p->d_sin[1];
+    float *g = p->d_vol[0], *pd = p->d_vol[1], *xs = p->d_vol[2];
+    SolverScratch sc;
+    rc = scratch_get(p, sc, maxit);
+    if (rc) {
+        scratch_free(sc);
+        return rc;
+    }
+    SolveState *S = sc.state;
+    // s = b - A x0 (areccgls.cpp:323-346); x0 = 0 unless warm.
+    if (warm) {
+        rc = forward_project(p, d_x, q, nullptr, nullptr, st);
+        if (rc) goto done;
+        k_sub<<<grid_for(ns, 16), 256, 0, st>>>(d_b, q, s, ns);
+    } else {
+        cudaMemsetAsync(d_x, 0, sizeof(float) * nv, st);
+        cudaMemcpyAsync(s, d_b, sizeof(float) * ns, cudaMemcpyDeviceToDevice, st);
+    }
+    // g = A^T s; gamma = ||g||^2 (areccgls.cpp:358-372).
+    cudaMemsetAsync(S, 0, sizeof(SolveState), st);
+    rc = back_project(p, s, g, &S->gnorm2, nullptr, st);
+    if (rc) goto done;
+    k_cgls_init<<<1, 1, 0, st>>>(S, maxit, tol, rnorm_ref);
+    {
+        // Iterations are queued in batches; the stopping test runs on the device
+        // and later queued iterations return at once.
+        int launched = 0;
+        int batch = 1;
+        while (launched < maxit) {
+            const int nb = std::min(batch, maxit - launched);
+            for (int i = 0; i < nb; i++) {
+                rc = cgls_iteration(p, S, sc.hist, d_x, s, q, g, pd, xs, st);
+                if (rc) goto done;
+            }
+            launched += nb;
+            cudaError_t e =
+                cudaMemcpyAsync(sc.h_state, S, sizeof(SolveState), cudaMemcpyDeviceToHost, st);
+            if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+            if (e != cudaSuccess) {
+                set_error(std::string("cgls: ") + cudaGetErrorString(e));
+                rc = cuda_status(e);
+                goto done;
+            }
+            if (sc.h_state->done) break;
+            batch = std::min(batch * 2, 8);
+        }
+        // flush a pending best-iterate copy, then restore it if the reference would
+        k_cgls_save<<<grid_for(nv, 16), 256, 0, st>>>(S, d_x, xs, nv / 4);
+        k_cgls_save_done<<<1, 1, 0, st>>>(S);
+        cudaError_t e =
+            cudaMemcpyAsync(sc.h_state, S, sizeof(SolveState), cudaMemcpyDeviceToHost, st);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+        if (e != cudaSuccess) {
+            set_error(std::string("cgls: ") + cudaGetErrorString(e));
+            rc = cuda_status(e);
+            goto done;
+        }
+        const SolveState &H = *sc.h_state;
+        if (H.iterbest < maxit - 1)
+            cudaMemcpyAsync(d_x, xs, sizeof(float) * nv, cudaMemcpyDeviceToDevice, st);
+        if (hist_host && H.iterations > 0)
+            cudaMemcpyAsync(hist_host, sc.hist, sizeof(double) * H.iterations,
+                            cudaMemcpyDeviceToHost, st);
+        e = cudaStreamSynchronize(st);
+        if (e != cudaSuccess) {
+            set_error(std::string("cgls: ") + cudaGetErrorString(e));
+            rc = cuda_status(e);
+            goto done;
+        }
+        if (info) {
+            info->iterations = H.iterations;
+            info->iterbest = H.iterbest;
+            info->restarts = 0;
+            info->status = 0;
+            info->lam_final = 0.f;
+            info->rnorm0 = H.rnorm0;
+            info->rel_final = H.rel;
+        }
+    }
+done:
+    scratch_free(sc);
+    if (rc == 0) {
+        cudaError_t e = cudaGetLastError();
+        if (e != cudaSuccess) {
+            set_error(std::string("cgls: ") + cudaGetErrorString(e));
+            rc = cuda_status(e);
+        }
+    }
+    return rc;
+}
+
+// SIRT with the reference's control flow (arecsirt.cpp:267-362): the step size
+// is halved and the solve restarted from zero (at most 20 times) whenever the
+// relative gradient norm grows; the squared norm of A^T b keeps accumulating
+// across restarts as in the reference.  The decision needs the norms on the
+// host, one small copy per iteration.
+int sirt(Plan *p, const float *d_b, float *d_x, float lam, int maxit, float tol,
+         double *hist_host, arecgb_solve_info *info, int verbose, cudaStream_t st) {
+    int rc = ensure_workspace(p, 3, 1);
+    if (rc) return rc;
+    const size_t nv = vol_floats(p);
+    float *bvol = p->d_vol[0], *pvol = p->d_vol[1], *grad = p->d_vol[2], *proj = p->d_sin[0];
+    double *red = nullptr, *h_red = nullptr;
+    ARECGB_CUDA(cudaMalloc(&red, sizeof(double) * (2 * kRedBlocks + 2)));
+    if (cudaMallocHost(&h_red, sizeof(double) * 2) != cudaSuccess) {
+        cudaFree(red);
+        set_error("sirt: pinned allocation failed");
+        return ARECGB_ERR_NOMEM;
+    }
+    double relnrm0 = 1.00001, bnorm2 = 0.0, bnorm = 0.0;
+    int restarts = 0, iter = 1, count = 0;
+    const int nblk = std::min(kRedBlocks, grid_for(nv, 8));
+    cudaMemsetAsync(d_x, 0, sizeof(float) * nv, st);
+    while (iter <= maxit) {
+        double rn2;
+        if (iter == 1) {
+            if (restarts == 0) {
+                rc = back_project(p, d_b, bvol, nullptr, nullptr, st);
+                if (rc) break;
+            }
+            k_sirt_first<<<nblk, 256, 0, st>>>(bvol, grad, nv, red, red + kRedBlocks);
+            k_reduce_partials<<<1, 256, 0, st>>>(red, nblk, red + 2 * kRedBlocks);
+            k_reduce_partials<<<1, 256, 0, st>>>(red + kRedBlocks, nblk, red + 2 * kRedBlocks + 1);
+        } else {
+            rc = forward_project(p, d_x, proj, nullptr, nullptr, st);
+            if (rc) break;
+            rc = back_project(p, proj, pvol, nullptr, nullptr, st);
+            if (rc) break;
+            k_sirt_grad<<<nblk, 256, 0, st>>>(bvol, pvol, grad, nv, red + kRedBlocks);
+            k_reduce_partials<<<1, 256, 0, st>>>(red + kRedBlocks, nblk, red + 2 * kRedBlocks + 1);
+        }
+        cudaError_t e = cudaMemcpyAsync(h_red, red + 2 * kRedBlocks, sizeof(double) * 2,
+                                        cudaMemcpyDeviceToHost, st);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+        if (e != cudaSuccess) {
+            set_error(std::string("sirt: ") + cudaGetErrorString(e));
+            rc = cuda_status(e);
+            break;
+        }
+        if (iter == 1) {
+            bnorm2 += h_red[0];
+            bnorm = std::sqrt(bnorm2);
+        }
+        rn2 = h_red[1];
+        const double rnorm = std::sqrt(rn2);
+        const double relnrm = rnorm / bnorm;
+        if (hist_host && count < maxit) hist_host[count] = relnrm;
+        count++;
+        if (verbose)
+            printf("iter = %3d, rnorm / bnorm = %11.3e, rnorm = %11.3e\n", iter, relnrm, rnorm);
+        if (relnrm > relnrm0) {
+            if (restarts > 20) {
+                if (verbose) printf("Failure to converge, even with lam = %11.3e\n", lam);
+                break;
+            }
+            ++restarts;
+            iter = 1;
+            lam /= 2.0;
+            relnrm0 = 1.0001;
+            cudaMemsetAsync(d_x, 0, sizeof(float) * nv, st);
+            if (verbose) printf("reducing lam to %11.3e, restarting\n", lam);
+            continue;
+        }
+        if (relnrm < tol || relnrm > relnrm0) {
+            if (verbose) {
+                printf("Terminating with rnorm/bnorm = %11.3e, tol = %11.3e, ", relnrm, tol);
+                printf("relnrm0 = %11.3e\n", relnrm0);
+            }
+            break;
+        }
+        relnrm0 = relnrm;
+        k_sirt_update<<<grid_for(nv, 8), 256, 0, st>>>(d_x, grad, lam, nv);
+        ++iter;
+    }
+    if (rc == 0) {
+        cudaError_t e = cudaStreamSynchronize(st);
+        if (e == cudaSuccess) e = cudaGetLastError();
+        if (e != cudaSuccess) {
+            set_error(std::string("sirt: ") + cudaGetErrorString(e));
+            rc = cuda_status(e);
+        }
+    }
+    if (info) {
+        info->iterations = count;
+        info->iterbest = 0;
+        info->restarts = restarts;
+        info->status = 0;
+        info->lam_final = lam;
+        info->rnorm0 = 0.0;
+        info->rel_final = 0.0;
+    }
+    cudaFree(red);
+    cudaFreeHost(h_red);
+    return rc;
+}
+
+}  // namespace arecgb

@@ -1,0 +1,100 @@
+/*
+ * Reference-compatible layer of libarec_gb300.
+ *
+ * The library defines the reference's own C++ entry points with the reference's
+ * signatures (so a program built against the reference's headers links against
+ * this library unchanged):
+ *
+ *   arecProject2D, arecProject2D_KB, arecProject2D_SQ        AREC3D/AREC3D/arecproject.h:55-62
+ *   arecBackProject2D, arecBackProject2D_KB, arecBackProject2D_SQ
+ *   cyl_sirt, cyl_sirt_SQ                                    AREC3D/AREC3D/arecsirt.h:6-10
+ *   cyl_sirt_KB                                              AREC3D/AREC3D/arecsirt_KB.h:6-7
+ *   cyl_cgls, cyl_cgls_SQ                                    AREC3D/AREC3D/areccgls.h:6-10
+ *   cyl_cgls_KB                                              AREC3D/AREC3D/areccgls_KB.h:6-7
+ *   arecCCImages                                             AREC3D/AREC3D/arecImage.h:36
+ *   ccorr2d, speak                                           AREC3D/AREC3D/align2dstack.h:9,25
+ *
+ * and, for C and FFI callers, the extern "C" aliases declared below (same
+ * arguments, `arecgb_` prefix).  Arguments, ownership and status codes are the
+ * reference's: input images are passed by value and owned by the caller;
+ * projection outputs are caller-allocated and overwritten; a solver allocates
+ * *xvol (calloc) when xvol->data == NULL and otherwise warm-starts CGLS from it.
+ * CUDA failures return ARECGB_ERR_* codes (arec_gb300.h) where the reference
+ * would call MPI_Abort.  The communicator is accepted and ignored: the whole
+ * problem runs on the current GPU.
+ */
+#pragma once
+
+#include "arec_gb300.h"
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#ifndef MPI_VERSION
+/* No <mpi.h> in this translation unit: MPICH's integer communicator handle. */
+typedef int MPI_Comm;
+#endif
+
+#ifndef ARECGB_IMAGE_DEFINED
+#define ARECGB_IMAGE_DEFINED
+/* Same layout as the reference's `arecImage` (AREC3D/AREC3D/arecImage.h:5-18). */
+typedef struct Image {
+    int nx;
+    int ny;
+    int nz;
+    double radius;
+    int height;
+    int nnz;
+    int nrays;
+    int *cord;
+    int is_cyl;
+    float *data;
+} arecImage;
+#endif
+
+/* Host data model (AREC3D/AREC3D/arecImage.cpp:15-241, 796-826). */
+int arecgb_arecAllocateCBImage(arecImage *cbimage, int nx, int ny, int nz);
+int arecgb_arecAllocateCylImage(arecImage *cylimage, double radius, int height);
+int arecgb_ImageCyl2CB(arecImage cylimage, arecImage cbimage, int nx, int ny, int nz);
+int arecgb_ImageCB2Cyl(arecImage cbimage, arecImage cylimage, int xcent, int zcent, double radius,
+                       int height);
+void arecgb_arecImageFree(arecImage *image);
+void arecgb_reset(arecImage *image);
+void arecgb_soft_noneg(arecImage *image);
+
+/* Projectors. */
+int arecgb_arecProject2D(arecImage cylvol, float *angles, int nangles, arecImage *projstack);
+int arecgb_arecProject2D_KB(arecImage cylvol, float *angles, int nangles, arecImage *projstack);
+int arecgb_arecProject2D_SQ(arecImage cylvol, float *angles, int nangles, arecImage *projstack);
+int arecgb_arecBackProject2D(arecImage images, float *angles, int nangles, arecImage *bvol);
+int arecgb_arecBackProject2D_KB(arecImage images, float *angles, int nangles, arecImage *bvol);
+int arecgb_arecBackProject2D_SQ(arecImage images, float *angles, int nangles, arecImage *bvol);
+
+/* Solvers. */
+int arecgb_cyl_sirt(MPI_Comm comm, arecImage images, float *angles, arecImage *xvol, float lam,
+                    int maxit, float tol);
+int arecgb_cyl_sirt_KB(MPI_Comm comm, arecImage images, float *angles, arecImage *xvol,
+                       float lam, int maxit, float tol);
+int arecgb_cyl_sirt_SQ(MPI_Comm comm, arecImage images, float *angles, arecImage *xvol,
+                       float lam, int maxit, float tol);
+int arecgb_cyl_cgls(MPI_Comm comm, arecImage images, float *angles, arecImage *xvol, float lam,
+                    int maxit, float tol);
+int arecgb_cyl_cgls_KB(MPI_Comm comm, arecImage images, float *angles, arecImage *xvol,
+                       float lam, int maxit, float tol);
+int arecgb_cyl_cgls_SQ(MPI_Comm comm, arecImage images, float *angles, arecImage *xvol,
+                       float lam, int maxit, float tol);
+
+/* Alignment. */
+int arecgb_arecCCImages(MPI_Comm comm, arecImage images1, arecImage images2, float *sx,
+                        float *sy);
+void arecgb_ccorr2d(int nx, int ny, float *x, float *y, float *c);
+void arecgb_speak(int nx, int ny, float *data, float *xt, float *yt);
+
+/* Residual trace of the last solver call on this thread (relative residuals,
+ * oldest first); returns the number of entries written (<= cap). */
+int arecgb_last_trace(double *rel, int cap, arecgb_solve_info *info);
+
+#ifdef __cplusplus
+}
+#endif

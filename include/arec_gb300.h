@@ -1,0 +1,110 @@
+/*
+ * libarec_gb300 — C ABI of the GB300 (sm_103a) implementation of the AREC3D
+ * reconstruction path.  Plain pointers and sizes only.
+ *
+ * Two layers:
+ *   1. This header: a device-resident core API over an opaque geometry plan.
+ *      Arrays are CUDA device memory in the device layouts:
+ *        volume    [nrays][ys]         (ys = slice stride, see arecgb_plan_info)
+ *        sinogram  [nangles][nx][ys]   (bin before slice; padding slices zero)
+ *   2. arec_compat.h: the reference's own entry points (arecProject2D_SQ,
+ *      cyl_cgls_SQ, arecCCImages, ...) over host `arecImage` buffers, plus
+ *      extern "C" aliases of them for FFI callers.
+ *
+ * Status codes follow the reference where it defines them (0 = OK; projector
+ * 1 = volume not cylindrical / nz != nangles, 2 = shape mismatch, -1 = shape
+ * mismatch in back-projection; AREC3D/AREC3D/arecproject.cpp:40-44,63-66,
+ * 120-141).  Failures the reference handles with MPI_Abort or does not have
+ * return negative codes instead:
+ *   ARECGB_ERR_ARG       invalid argument (message in arecgb_last_error())
+ *   ARECGB_ERR_NOMEM     device or host allocation failed
+ *   ARECGB_ERR_CUDA_BASE - cudaError_t   any other CUDA runtime error
+ */
+#pragma once
+
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* Projector weightings, numbered like the reference's `pmethod`
+ * (AREC3D/AREC3D/AREC3D.cpp:145-169). */
+#define ARECGB_LIN 1 /* 2-tap linear (arecProject2D, arecproject.cpp:19-183) */
+#define ARECGB_KB 2  /* Kaiser-Bessel table (arecproject.cpp:192-535) */
+#define ARECGB_SQ 3  /* square-pixel footprint (arecproject.cpp:540-765) */
+
+#define ARECGB_OK 0
+#define ARECGB_ERR_ARG (-90)
+#define ARECGB_ERR_NOMEM (-91)
+#define ARECGB_ERR_CUDA_BASE (-100)
+
+typedef struct arecgb_plan arecgb_plan;
+
+typedef struct {
+    int iterations; /* iterations whose residual was computed */
+    int iterbest;   /* CGLS best iterate, reference convention (areccgls.cpp:423-428) */
+    int restarts;   /* SIRT step-size restarts (arecsirt.cpp:318-338) */
+    int status;     /* reference-style status of the solve */
+    float lam_final;
+    double rnorm0;    /* initial residual norm */
+    double rel_final; /* last relative residual */
+} arecgb_solve_info;
+
+/* Last error message of the calling thread ("" if none). */
+const char *arecgb_last_error(void);
+int arecgb_version(void);
+
+/* Geometry plan for one cylinder: radius (pixels, as arecAllocateCylImage,
+ * AREC3D/AREC3D/arecImage.cpp:29), ny slices, nangles float radians (copied).
+ * Allocates device tables on the current device. */
+int arecgb_plan_create(arecgb_plan **plan, int weighting, double radius, int ny, int nangles,
+                       const float *angles);
+int arecgb_plan_destroy(arecgb_plan *plan);
+/* nx = detector width = round(2r+1), nrays = pixels in the disk, ys = slice stride. */
+int arecgb_plan_info(const arecgb_plan *plan, int *nx, int *nrays, int *ys);
+
+/* q = A x (replaces arecProject2D[_KB|_SQ], arecproject.cpp:19,351,540).
+ * d_norm2 (device, optional) receives sum(q*q) accumulated in double. */
+int arecgb_project(arecgb_plan *plan, const float *d_x, float *d_q, double *d_norm2,
+                   void *stream);
+/* g = A^T s (replaces arecBackProject2D[_KB|_SQ], arecproject.cpp:109,447,650). */
+int arecgb_backproject(arecgb_plan *plan, const float *d_s, float *d_g, double *d_norm2,
+                       void *stream);
+
+/* CGLS on device arrays (replaces cyl_cgls[_KB|_SQ], areccgls.cpp:12,245,
+ * areccgls_KB.cpp:12).  b: sinogram (device layout); x: volume, used as the
+ * initial guess when warm != 0.  rnorm_ref > 0 fixes the denominator of the
+ * relative normal-equation residual (0 = the reference's initial residual).
+ * rel_history (host, optional, maxit entries) receives the residual trace. */
+int arecgb_cgls(arecgb_plan *plan, const float *d_b, float *d_x, int warm, int maxit, float tol,
+                double rnorm_ref, double *rel_history, arecgb_solve_info *info, void *stream);
+
+/* SIRT/Landweber with the reference's restart rule (replaces cyl_sirt[_KB|_SQ],
+ * arecsirt.cpp:11,193, arecsirt_KB.cpp:11).  x is always started from zero. */
+int arecgb_sirt(arecgb_plan *plan, const float *d_b, float *d_x, float lam, int maxit, float tol,
+                double *rel_history, arecgb_solve_info *info, void *stream);
+
+/* Layout conversion between the reference's [na][ny][nx] stack and the device
+ * sinogram layout [na][nx][ys]. */
+int arecgb_sino_from_reference(const float *d_ref, float *d_dev, int na, int ny, int nx, int ys,
+                               void *stream);
+int arecgb_sino_to_reference(const float *d_dev, float *d_ref, int na, int ny, int nx, int ys,
+                             void *stream);
+
+/* Cross-correlation shift search over nz image pairs of ny x nx floats, device
+ * memory, reference layout [nz][ny][nx] (replaces the loop of arecCCImages,
+ * AREC3D/AREC3D/arecImage.cpp:414-428: ccorr2d + speak per pair).
+ * sx, sy (device, nz floats): sub-pixel shifts; ix, iy (device, optional):
+ * 0-based integer peak positions.  nx and ny must be powers of two in [16, 4096]. */
+int arecgb_cc_shifts(const float *d_img1, const float *d_img2, int nz, int ny, int nx,
+                     float *d_sx, float *d_sy, int *d_ix, int *d_iy, void *stream);
+
+/* Full correlation image (replaces ccorr2d, AREC3D/AREC3D/align2dstack.cpp:480):
+ * c = IDFT(conj(DFT x) * DFT y), unnormalised, device memory [ny][nx]. */
+int arecgb_ccorr2d_device(const float *d_x, const float *d_y, float *d_c, int ny, int nx,
+                          void *stream);
+
+#ifdef __cplusplus
+}
+#endif

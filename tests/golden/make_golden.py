@@ -1,0 +1,102 @@
+"""Generates the golden fixtures in tests/golden/*.npz by running the reference
+itself (AREC3D, compiled from its own sources into oracle/_ref by
+oracle/build_ref.sh) on small seeded inputs.  Run in the container that has the
+reference checkout:
+
+    bash oracle/build_ref.sh && python tests/golden/make_golden.py
+
+The reference's linear weighting (pmethod=1) reads two entries past its
+coordinate table; to make those reads return zero (as they do for large tables
+served by mmap), this script first lowers glibc's mmap threshold so every table
+of 4 KiB or more gets its own zero-filled pages.
+"""
+import ctypes
+import os
+import sys
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, ROOT)
+
+M_MMAP_THRESHOLD = -3
+
+
+def main():
+    ctypes.CDLL("libc.so.6").mallopt(M_MMAP_THRESHOLD, 4096)
+    import oracle as O
+
+    R = O.Reference()
+    rng = np.random.default_rng(20261203)
+    out = {}
+
+    # geometry (arecAllocateCylImage)
+    for r in (0.5, 1.0, 1.5, 7.5, 12.0, 31.5):
+        im = R._cyl(r, 1)
+        nr = im.nrays
+        out["cyl_%g_cord" % r] = np.ctypeslib.as_array(im.cord, shape=(nr, 2)).copy()
+        out["cyl_%g_nx" % r] = np.array(im.nx)
+
+    # solvers (nx 64, 4 slices, 24 angles), seeded noisy data
+    nx, ny, na = 64, 4, 24
+    ang = (np.arange(na) * np.pi / na).astype(np.float32)
+    _, nr, _ = O.cyl(0.5 * (nx - 1))
+    xt = rng.random((nr, ny), dtype=np.float32)
+    for tag, w in (("lin", 1), ("kb", 2), ("sq", 3)):
+        b = O.project(w, 0.5 * (nx - 1), xt, ang)
+        b = (b + 0.01 * rng.standard_normal(b.shape)).astype(np.float32)
+        out["solve_%s_b" % tag] = b
+        nm = {"lin": "", "kb": "_KB", "sq": "_SQ"}[tag]
+        xs, st = R.solve("cyl_sirt" + nm, b, ang, 2e-4, 12, 0.0)
+        assert st == 0
+        out["solve_%s_sirt" % tag] = xs
+        if w == 1:
+            xo, _ = O.sirt(w, b, ang, lam=2e-4, maxit=12, tol=0.0)
+            assert np.array_equal(xo, xs), "reference read nonzero memory past its table"
+        xc, st = R.solve("cyl_cgls" + nm, b, ang, 0.0, 10, 1e-7)
+        out["solve_%s_cgls" % tag] = xc
+        out["solve_%s_cgls_status" % tag] = np.array(st)
+    out["solve_angles"] = ang
+
+    # projectors (radius 31.5 -> nx 64; tables > 4 KiB so pmethod=1 reads zeros)
+    radius, ny = 31.5, 3
+    ang = np.array([0.0, 0.31, 0.7853982, 1.2, 1.5707964, 2.4, 3.0, 4.1, 21.123], np.float32)
+    _, nr, _ = O.cyl(radius)
+    x = rng.standard_normal((nr, ny)).astype(np.float32)
+    s = rng.standard_normal((len(ang), ny, 64)).astype(np.float32)
+    out["proj_angles"] = ang
+    out["proj_x"] = x
+    out["proj_s"] = s
+    for tag, fp, bp in (("lin", "arecProject2D", "arecBackProject2D"),
+                        ("kb", "arecProject2D_KB", "arecBackProject2D_KB"),
+                        ("sq", "arecProject2D_SQ", "arecBackProject2D_SQ")):
+        q, st = R.project(fp, radius, x, ang)
+        assert st == 0
+        g, st = R.backproject(bp, radius, s, ang)
+        assert st == 0
+        out["proj_%s_q" % tag] = q
+        out["proj_%s_g" % tag] = g
+
+    # cross-correlation (FFT of the FFTW-API stand-in, see oracle/shim)
+    ny2, nx2 = 32, 64
+    a = rng.random((3, ny2, nx2), dtype=np.float32)
+    bb = np.stack([np.roll(a[0], (2, -7), axis=(0, 1)), np.roll(a[1], (-5, 11), axis=(0, 1)),
+                   -np.roll(a[2], (1, 1), axis=(0, 1))]).astype(np.float32)
+    bb += (0.01 * rng.standard_normal(bb.shape)).astype(np.float32)
+    out["cc_a"] = a
+    out["cc_b"] = bb
+    out["cc_c0"] = R.ccorr2d(a[0], bb[0])
+    sx, sy, st = R.cc_images(a, bb)
+    out["cc_sx"], out["cc_sy"] = sx, sy
+    pk = rng.standard_normal((16, 16)).astype(np.float32)
+    pk[4, 9] = -20.0
+    out["speak_neg_c"] = pk
+    out["speak_neg_xy"] = np.array(R.speak(pk), np.float32)
+
+    np.savez_compressed(os.path.join(HERE, "reference_small.npz"), **out)
+    print("wrote", os.path.join(HERE, "reference_small.npz"))
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,121 @@
+"""The C-ABI library: it builds for sm_103a, loads without a GPU, exports
+every entry point include/*.h declares plus the reference's own C++ symbols,
+and its host-side data model matches the reference (no device calls here)."""
+import ctypes as C
+import os
+import re
+import subprocess
+
+import numpy as np
+import pytest
+
+from conftest import ROOT
+
+
+@pytest.fixture(scope="module")
+def lib():
+    import arec3d_gb300
+
+    arec3d_gb300.build()
+    return arec3d_gb300
+
+
+def declared_functions():
+    names = set()
+    for h in ("arec_gb300.h", "arec_compat.h"):
+        text = open(os.path.join(ROOT, "include", h)).read()
+        names |= set(re.findall(r"^\s*(?:const\s+char\s*\*|int|void)\s+\**\s*(arecgb_\w+)\s*\(",
+                                text, re.M))
+    return sorted(names)
+
+
+def exported(path):
+    out = subprocess.run(["nm", "-D", "--defined-only", path], capture_output=True, text=True)
+    return {ln.split()[-1] for ln in out.stdout.splitlines() if ln.strip()}
+
+
+def test_every_declared_symbol_is_exported(lib):
+    names = declared_functions()
+    assert len(names) > 30
+    syms = exported(lib.LIB_PATH)
+    missing = [n for n in names if n not in syms]
+    assert not missing, missing
+    L = lib.lib()  # loads on a machine without a GPU
+    for n in names:
+        assert getattr(L, n) is not None
+
+
+# The reference's C++ entry points (g++ Itanium mangling, MPICH-style int MPI_Comm).
+REF_SYMBOLS = [
+    "_Z13arecProject2D5ImagePfiPS_", "_Z16arecProject2D_KB5ImagePfiPS_",
+    "_Z16arecProject2D_SQ5ImagePfiPS_", "_Z17arecBackProject2D5ImagePfiPS_",
+    "_Z20arecBackProject2D_KB5ImagePfiPS_", "_Z20arecBackProject2D_SQ5ImagePfiPS_",
+    "_Z8cyl_sirti5ImagePfPS_fif", "_Z11cyl_sirt_KBi5ImagePfPS_fif",
+    "_Z11cyl_sirt_SQi5ImagePfPS_fif", "_Z8cyl_cglsi5ImagePfPS_fif",
+    "_Z11cyl_cgls_KBi5ImagePfPS_fif", "_Z11cyl_cgls_SQi5ImagePfPS_fif",
+    "_Z12arecCCImagesi5ImageS_PfS0_", "_Z7ccorr2diiPfS_S_", "_Z5speakiiPfS_S_",
+]
+
+
+def test_reference_cxx_symbols(lib):
+    syms = exported(lib.LIB_PATH)
+    missing = [s for s in REF_SYMBOLS if s not in syms]
+    assert not missing, missing
+
+
+def test_architecture_is_sm103a(lib):
+    out = subprocess.run(["cuobjdump", "--list-elf", lib.LIB_PATH], capture_output=True, text=True)
+    if out.returncode != 0:
+        pytest.skip("cuobjdump unavailable")
+    assert "sm_103a" in out.stdout
+
+
+@pytest.mark.parametrize("r", [0.5, 1.0, 1.5, 7.5, 12.0, 31.5, 100.0])
+def test_cylinder_allocation_matches_oracle(lib, oc, r):
+    im = lib.arecAllocateCylImage(r, 3)
+    nx, nr, cord = oc.cyl(r)
+    assert (im.nx, im.nrays, im.nnz, im.is_cyl) == (nx, nr, 3 * nr, 1)
+    np.testing.assert_array_equal(lib.cyl_cord(im), cord)
+    lib.arecImageFree(im)
+
+
+def test_image_cyl2cb_roundtrip(lib):
+    """"ImageCyl2CB" (AREC3D_test.cpp:326-363)."""
+    L = lib.lib()
+    cyl = lib.arecAllocateCylImage(1.0, 2)
+    d = lib.cyl_data(cyl)
+    d[:] = np.arange(cyl.nnz, dtype=np.float32).reshape(d.shape)
+    cube = np.zeros((cyl.nz, cyl.ny, cyl.nx), np.float32)
+    cb = lib._cb_image(cube)
+    assert L.arecgb_ImageCyl2CB(cyl, cb, cyl.nx, cyl.ny, cyl.nz) == 0
+    assert cube.sum() == d.sum()
+    cyl2 = lib.arecAllocateCylImage(1.0, 2)
+    assert L.arecgb_ImageCB2Cyl(cb, cyl2, 2, 2, 2.0, 2) == 0
+    np.testing.assert_array_equal(lib.cyl_data(cyl2), d)
+    lib.arecImageFree(cyl)
+    lib.arecImageFree(cyl2)
+
+
+def test_reset_and_soft_noneg(lib):
+    L = lib.lib()
+    cyl = lib.arecAllocateCylImage(2.0, 2)
+    d = lib.cyl_data(cyl)
+    d[:] = np.linspace(-1, 1, d.size, dtype=np.float32).reshape(d.shape)
+    before = d.copy()
+    L.arecgb_soft_noneg(C.byref(cyl))
+    np.testing.assert_array_equal(d, np.where(before < 0, before * 0.5, before))
+    L.arecgb_reset(C.byref(cyl))
+    assert not d.any()
+    lib.arecImageFree(cyl)
+
+
+def test_no_cpu_fallback(tmp_path, monkeypatch):
+    """Without the built library every call raises instead of computing on the CPU."""
+    import importlib
+
+    import arec3d_gb300
+
+    monkeypatch.setattr(arec3d_gb300, "LIB_PATH", str(tmp_path / "missing.so"))
+    monkeypatch.setattr(arec3d_gb300, "_lib", None)
+    with pytest.raises(RuntimeError):
+        arec3d_gb300.lib()

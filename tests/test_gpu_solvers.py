@@ -1,0 +1,92 @@
+"""GPU SIRT / CGLS parity against the oracle (reference cyl_sirt[_KB|_SQ],
+AREC3D/AREC3D/arecsirt.cpp; cyl_cgls[_KB|_SQ], AREC3D/AREC3D/areccgls.cpp)."""
+import numpy as np
+import pytest
+
+from conftest import rel_l2, uniform_angles
+from devutil import empty_vol, sino_to_dev, vol_from_dev, vol_to_dev
+
+pytestmark = pytest.mark.gpu
+
+TOL = 1e-5  # relative L2 on reconstructions
+
+
+def _problem(oc, w, nx, ny, na, seed, noise=0.01):
+    rng = np.random.default_rng(seed)
+    ang = uniform_angles(na)
+    radius = 0.5 * (nx - 1)
+    _, nr, _ = oc.cyl(radius)
+    xt = rng.random((nr, ny), dtype=np.float32)
+    b = oc.project(w, radius, xt, ang)
+    b = (b + noise * rng.standard_normal(b.shape)).astype(np.float32)
+    return b, ang, radius
+
+
+@pytest.mark.parametrize("w", [1, 2, 3])
+def test_sirt_parity(gb, oc, w):
+    b, ang, radius = _problem(oc, w, 49, 6, 30, seed=w)
+    x_ref, tr = oc.sirt(w, b, ang, lam=2e-4, maxit=20, tol=0.0)
+    plan = gb.Plan(w, radius, b.shape[1], ang)
+    xd = empty_vol(plan)
+    hist, info = plan.sirt(sino_to_dev(plan, b), xd, 2e-4, 20, 0.0)
+    x = vol_from_dev(plan, xd)
+    assert info.iterations == tr.iterations and info.restarts == tr.restarts
+    if w == 1:
+        x, x_ref = x[:-2], x_ref[:-2]
+    assert rel_l2(x, x_ref) < TOL
+    np.testing.assert_allclose(hist, tr.rel_history()[:len(hist)], rtol=1e-5)
+
+
+def test_sirt_restarts(gb, oc):
+    """A step size far above 2/||A||^2 diverges: the reference halves it and
+    restarts, accumulating ||A^T b||^2 (arecsirt.cpp:273-290, 318-338)."""
+    w = 3
+    b, ang, radius = _problem(oc, w, 33, 4, 20, seed=5)
+    x_ref, tr = oc.sirt(w, b, ang, lam=0.05, maxit=12, tol=0.0)
+    assert tr.restarts > 0
+    plan = gb.Plan(w, radius, b.shape[1], ang)
+    xd = empty_vol(plan)
+    hist, info = plan.sirt(sino_to_dev(plan, b), xd, 0.05, 12, 0.0)
+    assert info.restarts == tr.restarts
+    assert info.lam_final == pytest.approx(tr.lam_final, rel=0, abs=0)
+    assert rel_l2(vol_from_dev(plan, xd), x_ref) < TOL
+
+
+@pytest.mark.parametrize("w", [1, 2, 3])
+def test_cgls_parity(gb, oc, w):
+    b, ang, radius = _problem(oc, w, 49, 6, 30, seed=10 + w)
+    x_ref, tr = oc.cgls(w, b, ang, maxit=12, tol=1e-7)
+    plan = gb.Plan(w, radius, b.shape[1], ang)
+    xd = empty_vol(plan)
+    hist, info = plan.cgls(sino_to_dev(plan, b), xd, 12, 1e-7)
+    x = vol_from_dev(plan, xd)
+    assert info.iterations == tr.iterations
+    assert info.iterbest == tr.iterbest
+    if w == 1:
+        x, x_ref = x[:-2], x_ref[:-2]
+    assert rel_l2(x, x_ref) < TOL
+    np.testing.assert_allclose(hist, tr.rel_history(), rtol=1e-4)
+
+
+def test_cgls_tolerance_stop_and_warm_start(gb, oc):
+    w = 3
+    b, ang, radius = _problem(oc, w, 65, 8, 40, seed=21)
+    x0, _ = oc.sirt(w, b, ang, lam=2e-4, maxit=5, tol=0.0)
+    x_ref, tr = oc.cgls(w, b, ang, maxit=50, tol=2e-3, x0=x0)
+    plan = gb.Plan(w, radius, b.shape[1], ang)
+    xd = vol_to_dev(plan, x0)
+    hist, info = plan.cgls(sino_to_dev(plan, b), xd, 50, 2e-3, warm=True)
+    assert info.iterations == tr.iterations < 50
+    assert rel_l2(vol_from_dev(plan, xd), x_ref) < TOL
+
+
+def test_cgls_fixed_denominator(gb, oc):
+    w = 3
+    b, ang, radius = _problem(oc, w, 33, 4, 24, seed=3)
+    ref = 1234.5
+    x_ref, tr = oc.cgls(w, b, ang, maxit=8, tol=0.0, rnorm_ref=ref)
+    plan = gb.Plan(w, radius, b.shape[1], ang)
+    xd = empty_vol(plan)
+    hist, info = plan.cgls(sino_to_dev(plan, b), xd, 8, 0.0, rnorm_ref=ref)
+    np.testing.assert_allclose(hist, tr.rel_history(), rtol=1e-4)
+    assert rel_l2(vol_from_dev(plan, xd), x_ref) < TOL

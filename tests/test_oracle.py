@@ -1,0 +1,169 @@
+"""The oracle (oracle/arec_oracle.c, a CPU restatement of the reference path)
+pinned against the reference's own known answers (AREC3D/AREC3D_test/
+AREC3D_test.cpp), against golden fixtures produced by the reference itself
+(tests/golden/make_golden.py), and -- where the reference is built in this
+checkout -- against the reference directly."""
+import os
+import subprocess
+import sys
+
+import numpy as np
+import pytest
+
+from conftest import ROOT, rel_l2
+
+GOLD = os.path.join(ROOT, "tests", "golden", "reference_small.npz")
+
+
+@pytest.fixture(scope="module")
+def gold():
+    return np.load(GOLD)
+
+
+# ---- known answers of the reference's Catch suite -------------------------------------------
+def test_cylvol_odd(oc):
+    nx, nr, cord = oc.cyl(1.0)  # AREC3D_test.cpp:8-40
+    assert (nx, nr) == (3, 5)
+    assert cord.tolist() == [[1, 0], [0, 1], [1, 1], [2, 1], [1, 2]]
+
+
+def test_cylvol_even(oc):
+    nx, nr, cord = oc.cyl(0.5)  # AREC3D_test.cpp:42-70
+    assert (nx, nr) == (2, 4)
+    assert cord.tolist() == [[0, 0], [1, 0], [0, 1], [1, 1]]
+
+
+def test_projection_odd(oc):
+    x = np.zeros((5, 2), np.float32)  # AREC3D_test.cpp:97-147
+    x.ravel()[4], x.ravel()[5] = 1.0, 2.0
+    q = oc.project(oc.SQ, 1.0, x, np.zeros(1, np.float32))
+    assert q.sum() == pytest.approx(3.0)
+    assert q.ravel()[1] == pytest.approx(1.0, rel=1.2e-5)
+    assert q.ravel()[4] == pytest.approx(2.0, rel=1.2e-5)
+
+
+def test_backprojection_odd(oc):
+    q = np.zeros((1, 2, 3), np.float32)  # AREC3D_test.cpp:149-189
+    q.ravel()[1], q.ravel()[4] = 1.0, 2.0
+    g = oc.backproject(oc.SQ, 1.0, q, np.zeros(1, np.float32))
+    assert g.sum() == pytest.approx(9.0)
+
+
+@pytest.mark.parametrize("w,radius,ang,step", [
+    (3, 1.0, [1.475, 21.123, 2.123], 1),  # AREC3D_test.cpp:216-243
+    (3, 1.5, [0.698132, 1.22173], 3),     # :245-271
+    (2, 0.5, [0.698132, 1.22173], 3),     # :298-324
+])
+def test_exact_adjoint(oc, w, radius, ang, step):
+    ang = np.array(ang, np.float32)
+    ny = 2
+    nx, nr, _ = oc.cyl(radius)
+    nv, ns = nr * ny, len(ang) * ny * nx
+    for a in range(0, nv, step):
+        x = np.zeros(nv, np.float32)
+        x[a] = 1
+        q = oc.project(w, radius, x.reshape(nr, ny), ang).ravel()
+        for b in range(0, ns, step):
+            s = np.zeros(ns, np.float32)
+            s[b] = 1
+            g = oc.backproject(w, radius, s.reshape(len(ang), ny, nx), ang).ravel()
+            assert q[b] == g[a]
+
+
+# ---- golden fixtures made by the reference ---------------------------------------------------
+@pytest.mark.parametrize("r", [0.5, 1.0, 1.5, 7.5, 12.0, 31.5])
+def test_golden_cylinder(oc, gold, r):
+    nx, nr, cord = oc.cyl(r)
+    assert nx == int(gold["cyl_%g_nx" % r])
+    np.testing.assert_array_equal(cord, gold["cyl_%g_cord" % r])
+
+
+@pytest.mark.parametrize("tag,w", [("lin", 1), ("kb", 2), ("sq", 3)])
+def test_golden_projectors(oc, gold, tag, w):
+    ang, x, s = gold["proj_angles"], gold["proj_x"], gold["proj_s"]
+    q = oc.project(w, 31.5, x, ang)
+    g = oc.backproject(w, 31.5, s, ang)
+    np.testing.assert_array_equal(q, gold["proj_%s_q" % tag])
+    np.testing.assert_array_equal(g, gold["proj_%s_g" % tag])
+
+
+@pytest.mark.parametrize("tag,w", [("lin", 1), ("kb", 2), ("sq", 3)])
+def test_golden_solvers(oc, gold, tag, w):
+    ang, b = gold["solve_angles"], gold["solve_%s_b" % tag]
+    xs, _ = oc.sirt(w, b, ang, lam=2e-4, maxit=12, tol=0.0)
+    np.testing.assert_array_equal(xs, gold["solve_%s_sirt" % tag])
+    if tag == "kb":
+        # even nx: the reference's KB CGLS builds its volumes with radius nx/2 and
+        # returns -1 (areccgls_KB.cpp:37,112-113)
+        assert int(gold["solve_kb_cgls_status"]) == -1
+        return
+    xc, _ = oc.cgls(w, b, ang, maxit=10, tol=1e-7)
+    np.testing.assert_array_equal(xc, gold["solve_%s_cgls" % tag])
+
+
+def test_golden_ccorr(oc, gold):
+    a, b = gold["cc_a"], gold["cc_b"]
+    c = oc.ccorr2d(a[0], b[0])
+    assert rel_l2(c, gold["cc_c0"]) < 1e-6
+    sx, sy = oc.cc_images(a, b)
+    np.testing.assert_allclose(sx, gold["cc_sx"], atol=1e-4)
+    np.testing.assert_allclose(sy, gold["cc_sy"], atol=1e-4)
+    xt, yt, _, _ = oc.speak(gold["speak_neg_c"])
+    np.testing.assert_array_equal(np.array([xt, yt], np.float32), gold["speak_neg_xy"])
+
+
+def test_fft64_matches_numpy(oc):
+    rng = np.random.default_rng(0)
+    for ny, nx in ((16, 16), (12, 20), (64, 32), (7, 5)):
+        x = rng.standard_normal((ny, nx)).astype(np.float32)
+        y = rng.standard_normal((ny, nx)).astype(np.float32)
+        c = oc.ccorr2d(x, y)
+        ref = np.real(np.fft.ifft2(np.conj(np.fft.fft2(x)) * np.fft.fft2(y))) * nx * ny
+        assert rel_l2(c, ref) < 1e-6
+
+
+def test_quad2dfit_paraboloid(oc):
+    # exact paraboloid with its vertex at (+0.3, -0.2) is recovered
+    z = np.zeros(9, np.float32)
+    for j in (-1, 0, 1):
+        for i in (-1, 0, 1):
+            z[(j + 1) * 3 + (i + 1)] = 5.0 - (i - 0.3) ** 2 - 2 * (j + 0.2) ** 2
+    xs, ys, pv = oc.quad2dfit(z)
+    assert xs == pytest.approx(0.3, abs=1e-5) and ys == pytest.approx(-0.2, abs=1e-5)
+
+
+def test_threaded_slabs_agree(oc, gold):
+    """Slabs of slices on several threads (the reference's MPI ranks) give the
+    single-rank result up to the order of the scalar sums."""
+    ang, b = gold["solve_angles"], gold["solve_sq_b"]
+    x1, t1 = oc.cgls(3, b, ang, maxit=6, tol=0.0, nthreads=1)
+    x2, t2 = oc.cgls(3, b, ang, maxit=6, tol=0.0, nthreads=3)
+    assert rel_l2(x2, x1) < 1e-6
+
+
+# ---- the reference itself (only in a checkout where oracle/build_ref.sh ran) -----------------
+@pytest.mark.skipif(not os.path.exists(os.path.join(ROOT, "oracle", "_ref", "libarec_ref.so")),
+                    reason="reference not built here")
+def test_against_reference_build(oc):
+    code = r"""
+import ctypes, sys, numpy as np
+ctypes.CDLL("libc.so.6").mallopt(-3, 4096)
+sys.path.insert(0, %r)
+import oracle as O
+R = O.Reference()
+rng = np.random.default_rng(5)
+for radius in (7.5, 20.0, 40.5):
+    _, nr, _ = O.cyl(radius)
+    ang = rng.uniform(-4, 4, 11).astype(np.float32)
+    x = rng.standard_normal((nr, 5)).astype(np.float32)
+    for w, fp, bp in ((1, "arecProject2D", "arecBackProject2D"), (2, "arecProject2D_KB", "arecBackProject2D_KB"), (3, "arecProject2D_SQ", "arecBackProject2D_SQ")):
+        q = O.project(w, radius, x, ang); qr, _ = R.project(fp, radius, x, ang)
+        g = O.backproject(w, radius, q, ang); gr, _ = R.backproject(bp, radius, q, ang)
+        if w == 1:
+            g, gr = g[:-2], gr[:-2]
+        assert np.array_equal(q, qr) or w == 1 and np.array_equal(q[:, :, :], qr), (radius, w)
+        assert np.array_equal(g, gr), (radius, w)
+print("ok")
+""" % ROOT
+    r = subprocess.run([sys.executable, "-c", code], capture_output=True, text=True)
+    assert r.returncode == 0 and "ok" in r.stdout, r.stderr[-2000:]
