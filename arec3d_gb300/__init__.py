@@ -63,6 +63,7 @@ def lib():
         L.arecgb_plan_create.argtypes = [C.POINTER(vp), C.c_int, C.c_double, C.c_int, C.c_int, fp]
         L.arecgb_plan_destroy.argtypes = [vp]
         L.arecgb_plan_info.argtypes = [vp, ip, ip, ip]
+        L.arecgb_plan_check.argtypes = [vp]
         L.arecgb_project.argtypes = [vp, vp, vp, vp, vp]
         L.arecgb_backproject.argtypes = [vp, vp, vp, vp, vp]
         L.arecgb_cgls.argtypes = [vp, vp, vp, C.c_int, C.c_int, C.c_float, C.c_double, dp,
@@ -160,6 +161,10 @@ class Plan:
             self.close()
         except Exception:
             pass
+
+    def check(self):
+        """Device-side consistency flag since the last check (0 = fine); clears it."""
+        return lib().arecgb_plan_check(self._h)
 
     @property
     def vol_shape(self):

@@ -77,6 +77,16 @@ int arecgb_plan_info(const arecgb_plan *plan, int *nx, int *nrays, int *ys) {
     return ARECGB_OK;
 }
 
+int arecgb_plan_check(arecgb_plan *plan) {
+    if (!plan) return ARECGB_ERR_ARG;
+    int rc = bind_device(P(plan));
+    if (rc) return rc;
+    int flag = 0;
+    ARECGB_CUDA(cudaMemcpy(&flag, P(plan)->d_err, sizeof(int), cudaMemcpyDeviceToHost));
+    ARECGB_CUDA(cudaMemset(P(plan)->d_err, 0, sizeof(int)));
+    return flag;
+}
+
 int arecgb_project(arecgb_plan *plan, const float *d_x, float *d_q, double *d_norm2,
                    void *stream) {
     if (!plan || !d_x || !d_q) {

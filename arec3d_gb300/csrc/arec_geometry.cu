@@ -161,11 +161,19 @@ int plan_create(Plan **out, int weighting, double radius, int ny, int nangles,
     }
 
     // Forward-projection angle groups: runs of consecutive angles sharing a
-    // sweep orientation, at most kGroupAngles each.
+    // sweep orientation, at most kGroupAngles each, whose strips stay within a
+    // few pixels of each other on every line of the disk (so the union of their
+    // candidate pixels per line fits the kernel's 32-pixel stage).
     std::vector<int4> groups;
+    const double Rg = radius + 2.0;
     for (int a = 0; a < nangles;) {
         int o = ang[a].orient, n = 1;
-        while (a + n < nangles && n < kGroupAngles && ang[a + n].orient == o) n++;
+        while (a + n < nangles && n < kGroupAngles && ang[a + n].orient == o) {
+            const double spread = Rg * (std::fabs((double)ang[a + n].c - ang[a].c) +
+                                        std::fabs((double)ang[a + n].s - ang[a].s));
+            if (spread / 0.7071 > 10.0) break;
+            n++;
+        }
         groups.push_back(make_int4(a, n, o, 0));
         a += n;
     }

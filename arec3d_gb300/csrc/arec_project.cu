@@ -23,6 +23,7 @@ static OpArgs make_args(const Plan *p, const int *skip) {
     A.nrays = p->nrays;
     A.ys = p->ys;
     A.na = p->na;
+    A.ngroups = p->ngroups;
     A.r_hi = p->r_hi;
     A.r_lo = p->r_lo;
     A.partials = p->d_partials;
@@ -39,10 +40,12 @@ static int slice_blocks(const Plan *p) {
     return (p->ys + span - 1) / span;
 }
 
+static int fp_slice_blocks(const Plan *p) { return (p->ys + 32 * p->vec - 1) / (32 * p->vec); }
+
 int fp_grid_blocks(const Plan *p) {
     if (p->weighting == ARECGB_LIN) return 1024;  // sum-of-squares pass over q
     const int ntile = (p->nx + kFpBins - 1) / kFpBins;
-    return p->ngroups * ntile * slice_blocks(p);
+    return p->ngroups * ntile * fp_slice_blocks(p);
 }
 
 int bp_grid_blocks(const Plan *p) { return p->ntiles * slice_blocks(p); }
@@ -65,7 +68,7 @@ int forward_project(const Plan *p, const float *d_x, float *d_q, double *d_norm2
         return ARECGB_OK;
     }
     const int ntile = (p->nx + kFpBins - 1) / kFpBins;
-    dim3 grid(p->ngroups * ntile, slice_blocks(p));
+    dim3 grid(p->ngroups * ntile, fp_slice_blocks(p));
     rc = p->weighting == ARECGB_KB ? launch_fp_kb(A, p->vec, nsc, grid, d_x, d_q, st)
                                    : launch_fp_sq(A, p->vec, nsc, grid, d_x, d_q, st);
     ARECGB_CUDA(cudaGetLastError());

@@ -41,7 +41,7 @@ struct OpArgs {
     const ColInfo *cols;
     const int4 *groups;
     const int2 *tiles;
-    int nx, nrays, ys, na;
+    int nx, nrays, ys, na, ngroups;
     float r_hi, r_lo;
     double *partials;
     const int *skip;
@@ -80,6 +80,49 @@ __device__ __forceinline__ void stv(float *__restrict__ p, const float (&v)[VEC]
     }
 }
 
+// Slices held by a lane: VEC/4 float4 pieces at c*128 + lane*4 for VEC >= 4
+// (consecutive lanes read consecutive 16-byte pieces: conflict-free shared
+// memory and fully coalesced global rows), lane*VEC otherwise.
+template <int VEC>
+__device__ __forceinline__ int lane_piece(int lane, int c) {
+    return VEC >= 4 ? c * 128 + lane * 4 : lane * VEC;
+}
+
+template <int VEC>
+__device__ __forceinline__ void lds_lane(const float *base, int lane, float (&v)[VEC]) {
+    if constexpr (VEC >= 4) {
+#pragma unroll
+        for (int c = 0; c < VEC / 4; c++) {
+            const float4 t = *reinterpret_cast<const float4 *>(base + lane_piece<VEC>(lane, c));
+            v[4 * c] = t.x; v[4 * c + 1] = t.y; v[4 * c + 2] = t.z; v[4 * c + 3] = t.w;
+        }
+    } else if constexpr (VEC == 2) {
+        const float2 t = *reinterpret_cast<const float2 *>(base + lane * 2);
+        v[0] = t.x; v[1] = t.y;
+    } else {
+        v[0] = base[lane];
+    }
+}
+
+// Store a lane's slices; pieces at or beyond `limit` (slices left in the row)
+// are skipped.  Pieces are whole: limits are multiples of 8.
+template <int VEC>
+__device__ __forceinline__ void stg_lane(float *base, int lane, const float (&v)[VEC], int limit) {
+    if constexpr (VEC >= 4) {
+#pragma unroll
+        for (int c = 0; c < VEC / 4; c++) {
+            const int o = lane_piece<VEC>(lane, c);
+            if (o < limit)
+                *reinterpret_cast<float4 *>(base + o) =
+                    make_float4(v[4 * c], v[4 * c + 1], v[4 * c + 2], v[4 * c + 3]);
+        }
+    } else if constexpr (VEC == 2) {
+        if (lane * 2 < limit) *reinterpret_cast<float2 *>(base + lane * 2) = make_float2(v[0], v[1]);
+    } else {
+        if (lane < limit) base[lane] = v[0];
+    }
+}
+
 // Block-wide deterministic sum of one double per thread -> partials[slot].
 template <int NW>
 __device__ __forceinline__ void block_sum_to(double v, double *red, double *out) {
@@ -97,9 +140,154 @@ __device__ __forceinline__ void block_sum_to(double v, double *red, double *out)
 
 // ---------------------------------------------------------------------------
 // Back projection.
+
+__device__ __forceinline__ unsigned smem_u32(const void *p) {
+    return (unsigned)__cvta_generic_to_shared(p);
+}
+
+// 16-byte global -> shared copy, zero-filled when !valid (cp.async, sm_80+).
+__device__ __forceinline__ void cp_async16(void *dst, const void *src, bool valid) {
+    const unsigned n = valid ? 16u : 0u;
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;\n" ::"r"(smem_u32(dst)), "l"(src),
+                 "r"(n)
+                 : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+template <int N>
+__device__ __forceinline__ void cp_async_wait() {
+    asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory");
+}
+
+constexpr int kBpAngles = 32;  // angles per weight chunk
+constexpr int kBpFoot = 16;    // staged footprint width in bins (an 8x4 tile spans <= 12)
+
+template <int VEC, int NSC>
+constexpr size_t bp_smem_bytes() {
+    return sizeof(float4) * kBpAngles * 32 + sizeof(int) * kBpAngles +
+           sizeof(float) * 2 * kBpFoot * (NSC * 32 * VEC) + sizeof(double) * 4 * NSC;
+}
+
+// Square-pixel and Kaiser-Bessel weightings: the footprint of the tile at each
+// angle (<= 12 bins x the block's slices) is staged in shared memory with
+// double-buffered cp.async (bins outside the detector read as zero, which is
+// what skipping them gives), so the accumulation reads only shared memory.
 template <int W, int VEC, int NSC>
 __global__ void __launch_bounds__(128 * NSC)
     bp_kernel(OpArgs A, const float *__restrict__ s, float *__restrict__ g) {
+    constexpr int NT = 128 * NSC, NWARP = NT / 32, AC = kBpAngles, FW = kBpFoot;
+    constexpr int SPAN = NSC * 32 * VEC;  // slices per block
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    float4 *sw = reinterpret_cast<float4 *>(smem_raw);              // [AC][32]
+    int *fb = reinterpret_cast<int *>(sw + AC * 32);                 // [AC]
+    float *foot = reinterpret_cast<float *>(fb + AC);                // [2][FW][SPAN]
+    double *red = reinterpret_cast<double *>(foot + 2 * FW * SPAN);  // [NWARP]
+    if (A.skip && *A.skip) return;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int2 tile = A.tiles[blockIdx.x];
+    const int ix = tile.x + (lane & (kTileX - 1)), iz = tile.y + lane / kTileX;
+    int k = -1;
+    if (iz < A.nx) {
+        RowInfo ri = A.rows[iz];
+        if (ix >= ri.lo && ix <= ri.hi) k = ri.start + ix - ri.lo;
+    }
+    const float4 myray = k >= 0 ? A.ray[k] : make_float4(0.f, 0.f, 0.f, 0.f);
+    const int rg = warp & 3, sc = warp >> 2;
+    const int yb = blockIdx.y * SPAN;                  // first slice of the block
+    const int yw = sc * 32 * VEC;                        // this warp's slices within the block
+    const bool yok = yb + yw + lane_piece<VEC>(lane, 0) < A.ys;
+    const size_t ys = (size_t)A.ys;
+
+    float acc[8][VEC];
+#pragma unroll
+    for (int r = 0; r < 8; r++)
+#pragma unroll
+        for (int q = 0; q < VEC; q++) acc[r][q] = 0.f;
+
+    // stage the footprint of angle a0+ai into buffer buf
+    auto stage = [&](int a0, int ai, int buf) {
+        const int a = a0 + ai, b0 = fb[ai];
+        float *dst = foot + (size_t)buf * FW * SPAN;
+        constexpr int CHUNKS = FW * SPAN / 4;  // 16-byte pieces
+        for (int c = threadIdx.x; c < CHUNKS; c += NT) {
+            const int f = c / (SPAN / 4), col = (c % (SPAN / 4)) * 4;
+            const int bin = b0 + f, y = yb + col;
+            const bool ok = (unsigned)bin < (unsigned)A.nx && y < A.ys;
+            const float *src = s + ((size_t)a * A.nx + (ok ? bin : 0)) * ys + (ok ? y : 0);
+            cp_async16(dst + f * SPAN + col, src, ok);
+        }
+    };
+
+    for (int a0 = 0; a0 < A.na; a0 += AC) {
+        const int nac = min(AC, A.na - a0);
+        for (int ai = warp; ai < AC; ai += NWARP) {
+            const int a = a0 + ai;
+            float4 e = make_float4(__int_as_float(INT_MIN / 2), 0.f, 0.f, 0.f);
+            int lo = INT_MAX, hi = INT_MIN;
+            if (a < A.na && k >= 0) {
+                const Taps t = ray_taps<W>(myray, A.ang[a], A.r_hi, A.r_lo);
+                e = make_float4(__int_as_float(t.iqx - 1), t.w0, t.w1, t.w2);
+                lo = hi = t.iqx - 1;
+            }
+            sw[ai * 32 + lane] = e;
+            for (int o = 16; o > 0; o >>= 1) {
+                lo = min(lo, __shfl_xor_sync(0xffffffffu, lo, o));
+                hi = max(hi, __shfl_xor_sync(0xffffffffu, hi, o));
+            }
+            if (lane == 0) {
+                if (hi - lo + 3 > FW && lo != INT_MAX) atomicOr(A.err, 2);
+                fb[ai] = lo == INT_MAX ? 0 : lo;
+            }
+        }
+        __syncthreads();
+        stage(a0, 0, 0);
+        cp_async_commit();
+        for (int ai = 0; ai < nac; ai++) {
+            if (ai + 1 < nac) stage(a0, ai + 1, (ai + 1) & 1);
+            cp_async_commit();
+            cp_async_wait<1>();
+            __syncthreads();
+            if (yok) {
+                const float *F = foot + (size_t)(ai & 1) * FW * SPAN + yw;
+                const int fb0 = fb[ai];
+#pragma unroll
+                for (int r = 0; r < 8; r++) {
+                    const float4 e = sw[ai * 32 + rg * 8 + r];
+                    const int rb = __float_as_int(e.x) - fb0;
+                    if (rb >= 0 && rb <= FW - 3) {
+#pragma unroll
+                        for (int j = 0; j < 3; j++) {
+                            const float w = j == 0 ? e.y : (j == 1 ? e.z : e.w);
+                            float v[VEC];
+                            lds_lane<VEC>(F + (rb + j) * SPAN, lane, v);
+#pragma unroll
+                            for (int q = 0; q < VEC; q++) acc[r][q] = fmaf(w, v[q], acc[r][q]);
+                        }
+                    }
+                }
+            }
+            __syncthreads();
+        }
+    }
+
+    double s2 = 0.0;
+#pragma unroll
+    for (int r = 0; r < 8; r++) {
+        const int kr = __shfl_sync(0xffffffffu, k, rg * 8 + r);
+        if (kr >= 0 && yok) {
+            stg_lane<VEC>(g + (size_t)kr * ys + yb + yw, lane, acc[r], A.ys - (yb + yw));
+#pragma unroll
+            for (int q = 0; q < VEC; q++) s2 += (double)__fmul_rn(acc[r][q], acc[r][q]);
+        }
+    }
+    block_sum_to<NWARP>(s2, red, A.partials + (size_t)blockIdx.y * gridDim.x + blockIdx.x);
+}
+
+// Linear weighting: its ray coordinates are the reference's shifted table
+// entries, so a tile's footprint is not compact; this kernel reads the
+// sinogram directly (parity path).
+template <int VEC, int NSC>
+__global__ void __launch_bounds__(128 * NSC)
+    bp_lin_kernel(OpArgs A, const float *__restrict__ s, float *__restrict__ g) {
     constexpr int NT = 128 * NSC, NWARP = NT / 32, AC = 32;
     __shared__ float4 sw[AC][32];
     __shared__ double red[NWARP];
@@ -116,21 +304,19 @@ __global__ void __launch_bounds__(128 * NSC)
     const int rg = warp & 3, sc = warp >> 2;
     const int y0 = (blockIdx.y * NSC + sc) * 32 * VEC + lane * VEC;
     const bool yok = y0 < A.ys;
-    const size_t bin_stride = (size_t)A.ys;
-
+    const size_t ys = (size_t)A.ys;
     float acc[8][VEC];
 #pragma unroll
     for (int r = 0; r < 8; r++)
 #pragma unroll
         for (int q = 0; q < VEC; q++) acc[r][q] = 0.f;
-
     for (int a0 = 0; a0 < A.na; a0 += AC) {
         for (int ai = warp; ai < AC; ai += NWARP) {
             const int a = a0 + ai;
             float4 e = make_float4(__int_as_float(INT_MIN / 2), 0.f, 0.f, 0.f);
             if (a < A.na && k >= 0) {
-                Taps t = ray_taps<W>(myray, A.ang[a], A.r_hi, A.r_lo);
-                e = make_float4(__int_as_float(t.iqx - 1), t.w0, t.w1, t.w2);
+                const Taps t = ray_taps<ARECGB_LIN>(myray, A.ang[a], A.r_hi, A.r_lo);
+                e = make_float4(__int_as_float(t.iqx - 1), t.w0, t.w1, 0.f);
             }
             sw[ai][lane] = e;
         }
@@ -138,18 +324,18 @@ __global__ void __launch_bounds__(128 * NSC)
         const int nac = min(AC, A.na - a0);
         if (yok) {
             for (int ai = 0; ai < nac; ai++) {
-                const float *sa = s + (size_t)(a0 + ai) * A.nx * bin_stride + y0;
+                const float *sa = s + (size_t)(a0 + ai) * A.nx * ys + y0;
 #pragma unroll
                 for (int r = 0; r < 8; r++) {
                     const float4 e = sw[ai][rg * 8 + r];
                     const int b0 = __float_as_int(e.x);
 #pragma unroll
-                    for (int j = 0; j < 3; j++) {
+                    for (int j = 0; j < 2; j++) {
                         const int b = b0 + j;
-                        const float w = j == 0 ? e.y : (j == 1 ? e.z : e.w);
+                        const float w = j == 0 ? e.y : e.z;
                         if ((unsigned)b < (unsigned)A.nx) {
                             float v[VEC];
-                            ldv<VEC>(sa + (size_t)b * bin_stride, v);
+                            ldv<VEC>(sa + (size_t)b * ys, v);
 #pragma unroll
                             for (int q = 0; q < VEC; q++) acc[r][q] = fmaf(w, v[q], acc[r][q]);
                         }
@@ -159,13 +345,12 @@ __global__ void __launch_bounds__(128 * NSC)
         }
         __syncthreads();
     }
-
     double s2 = 0.0;
 #pragma unroll
     for (int r = 0; r < 8; r++) {
         const int kr = __shfl_sync(0xffffffffu, k, rg * 8 + r);
         if (kr >= 0 && yok) {
-            stv<VEC>(g + (size_t)kr * bin_stride + y0, acc[r]);
+            stv<VEC>(g + (size_t)kr * ys + y0, acc[r]);
 #pragma unroll
             for (int q = 0; q < VEC; q++) s2 += (double)__fmul_rn(acc[r][q], acc[r][q]);
         }
@@ -198,64 +383,113 @@ __device__ __forceinline__ bool strip_line_extent(float ca, float cl, float T1, 
     return true;
 }
 
-template <int W, int VEC, int NSC, int BT>
-__global__ void __launch_bounds__(32 * kGroupAngles * NSC)
+constexpr int kFpStage = 32;  // staged pixels per line: the union of the group's candidates
+
+template <int VEC>
+constexpr size_t fp_smem_bytes() {
+    return sizeof(float) * 2 * kFpStage * (32 * VEC) + sizeof(float4) * kGroupAngles * 32 +
+           sizeof(int) * kGroupAngles * (kFpBins + 3) + sizeof(int) * (kGroupAngles * 4 + 8) +
+           sizeof(double) * kGroupAngles;
+}
+
+// Candidate pixel range [clo, chi] on line li for one angle: pixels whose
+// centre bin may fall in [b0-1, b0+BT] (a margin of one pixel each side; the
+// exact test is the centre bin itself).
+__device__ __forceinline__ void line_candidates(const OpArgs &A, int orient, float ca, float cl,
+                                                float T1, float T2, float r, int li, int &clo,
+                                                int &chi) {
+    int plo, phi;
+    if (orient == 0) {
+        const RowInfo ri = A.rows[li];
+        plo = ri.lo;
+        phi = ri.hi;
+    } else {
+        const ColInfo ci = A.cols[li];
+        plo = ci.lo;
+        phi = ci.hi;
+    }
+    const float Lv = (float)li - r;
+    float pa = (T1 - Lv * cl) / ca, pb = (T2 - Lv * cl) / ca;
+    if (pa > pb) {
+        const float t = pa;
+        pa = pb;
+        pb = t;
+    }
+    clo = max(plo, (int)floorf(pa + r) - 1);
+    chi = min(phi, (int)ceilf(pb + r) + 1);
+}
+
+__device__ __forceinline__ int line_pixel_ray(const OpArgs &A, int orient, int li, int p) {
+    if (orient == 0) {
+        const RowInfo ri = A.rows[li];
+        return ri.start + p - ri.lo;
+    }
+    const RowInfo ri = A.rows[p];
+    return ri.start + li - ri.lo;
+}
+
+// Square-pixel and Kaiser-Bessel weightings.  Block = one angle group (<= 4
+// angles, one warp each) x BT bins x 32*VEC slices.  Per line of the strip, the
+// x rows of the union of the angles' candidate pixels are staged in shared
+// memory (double-buffered cp.async, one line ahead); each warp computes its
+// angle's weights for those pixels (lanes = pixels), buckets them by centre bin
+// with warp votes, and accumulates BT bins x VEC slices in registers from the
+// staged rows.
+template <int W, int VEC, int BT>
+__global__ void __launch_bounds__(32 * kGroupAngles, 3)
     fp_kernel(OpArgs A, const float *__restrict__ x, float *__restrict__ q) {
-    constexpr int NA = kGroupAngles, NWARP = NA * NSC, NG = BT + 2;
-    __shared__ float4 list[NA][NSC * 32];
-    __shared__ int cnt[NWARP][NG];
-    __shared__ int base[NA][NG + 1];
-    __shared__ int lrange[NA][2];
-    __shared__ double red[NWARP];
+    constexpr int NA = kGroupAngles, NG = BT + 2, SPAN = 32 * VEC, US = kFpStage;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    float *stg = reinterpret_cast<float *>(smem_raw);            // [2][US][SPAN]
+    float4 *list = reinterpret_cast<float4 *>(stg + 2 * US * SPAN);  // [NA][32]
+    int *base = reinterpret_cast<int *>(list + NA * 32);             // [NA][NG+1]
+    int *lrange = base + NA * (NG + 1);                               // [NA][2]
+    int *crange = lrange + NA * 2;                                    // [NA][2] next line
+    int *uinfo = crange + NA * 2;                                     // [2][2] (ulo, n) per buffer
+    int *pad = uinfo + 4;
+    (void)pad;
+    double *red = reinterpret_cast<double *>(smem_raw + fp_smem_bytes<VEC>() - sizeof(double) * NA);
     if (A.skip && *A.skip) return;
-    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int ai = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int ntile = (A.nx + BT - 1) / BT;
-    const int grp = blockIdx.x / ntile, b0 = (blockIdx.x % ntile) * BT;
+    (void)ntile;
+    // consecutive blocks take consecutive angle groups of the same bin tile: their
+    // strips overlap almost entirely, so concurrently running blocks share x in L2
+    const int grp = blockIdx.x % A.ngroups, b0 = (blockIdx.x / A.ngroups) * BT;
     const int4 G = A.groups[grp];
     const int orient = G.z;
     const float r = A.r_hi + A.r_lo;
-    // The strip: centre bins iqx in [b0-1, b0+BT], i.e. xb in
-    // [b0-1.5, b0+BT+0.5], with a margin; in offsets from the centre:
     const float T1 = (float)b0 - 1.5f - 0.02f - r;
     const float T2 = (float)(b0 + BT) + 0.5f + 0.02f - r;
     const float R = r + 1.5f;
-
-    if (threadIdx.x < NA) {
+    const int yb = blockIdx.y * SPAN;
+    const size_t ys = (size_t)A.ys;
+    const bool angle_ok = ai < G.y;
+    AngleParams ap;
+    float ca = 1.f, cl = 0.f;
+    if (angle_ok) {
+        ap = A.ang[G.x + ai];
+        ca = orient ? ap.s : ap.c;
+        cl = orient ? ap.c : ap.s;
+    }
+    if (lane == 0) {
         int lo = INT_MAX, hi = INT_MIN;
-        if ((int)threadIdx.x < G.y) {
-            const AngleParams ap = A.ang[G.x + threadIdx.x];
-            const float ca = orient ? ap.s : ap.c, cl = orient ? ap.c : ap.s;
-            float lmin, lmax;
-            if (strip_line_extent(ca, cl, T1, T2, R, lmin, lmax)) {
-                lo = max(0, (int)floorf(lmin + r) - 1);
-                hi = min(A.nx - 1, (int)ceilf(lmax + r) + 1);
-            }
+        float lmin, lmax;
+        if (angle_ok && strip_line_extent(ca, cl, T1, T2, R, lmin, lmax)) {
+            lo = max(0, (int)floorf(lmin + r) - 1);
+            hi = min(A.nx - 1, (int)ceilf(lmax + r) + 1);
         }
-        lrange[threadIdx.x][0] = lo;
-        lrange[threadIdx.x][1] = hi;
+        lrange[2 * ai] = lo;
+        lrange[2 * ai + 1] = hi;
     }
     __syncthreads();
     int L0 = INT_MAX, L1 = INT_MIN;
 #pragma unroll
     for (int i = 0; i < NA; i++) {
-        L0 = min(L0, lrange[i][0]);
-        L1 = max(L1, lrange[i][1]);
+        L0 = min(L0, lrange[2 * i]);
+        L1 = max(L1, lrange[2 * i + 1]);
     }
-
-    const int ai = warp % NA, sc = warp / NA;
-    const bool angle_ok = ai < G.y;
-    const int y0 = (blockIdx.y * NSC + sc) * 32 * VEC + lane * VEC;
-    const bool yok = y0 < A.ys;
-    AngleParams ap;
-    float ca = 1.f, cl = 0.f;
-    int my_lo = 0, my_hi = -1;
-    if (angle_ok) {
-        ap = A.ang[G.x + ai];
-        ca = orient ? ap.s : ap.c;
-        cl = orient ? ap.c : ap.s;
-        my_lo = lrange[ai][0];
-        my_hi = lrange[ai][1];
-    }
+    const int my_lo = lrange[2 * ai], my_hi = lrange[2 * ai + 1];
 
     float acc[BT][VEC];
 #pragma unroll
@@ -263,84 +497,97 @@ __global__ void __launch_bounds__(32 * kGroupAngles * NSC)
 #pragma unroll
         for (int v = 0; v < VEC; v++) acc[j][v] = 0.f;
 
-    for (int lb = L0; lb <= L1; lb += NSC) {
-        // Phase A: warp (ai, sc) enumerates line lb+sc for angle ai; lane = candidate.
-        const int li = lb + sc;
+    // each warp: its angle's candidate range on line li -> crange
+    auto ranges = [&](int li) {
+        int clo = INT_MAX, chi = INT_MIN;
+        if (angle_ok && li >= my_lo && li <= my_hi)
+            line_candidates(A, orient, ca, cl, T1, T2, r, li, clo, chi);
+        if (lane == 0) {
+            crange[2 * ai] = clo;
+            crange[2 * ai + 1] = chi;
+        }
+    };
+    // all threads: union of crange -> uinfo[buf]; issue the row copies
+    auto stage = [&](int li, int buf) {
+        int ulo = INT_MAX, uhi = INT_MIN;
+#pragma unroll
+        for (int i = 0; i < NA; i++) {
+            if (crange[2 * i] <= crange[2 * i + 1]) {
+                ulo = min(ulo, crange[2 * i]);
+                uhi = max(uhi, crange[2 * i + 1]);
+            }
+        }
+        int n = uhi >= ulo ? uhi - ulo + 1 : 0;
+        if (n > US) {
+            if (threadIdx.x == 0) atomicOr(A.err, 1);
+            n = US;
+        }
+        if (threadIdx.x == 0) {
+            uinfo[2 * buf] = ulo;
+            uinfo[2 * buf + 1] = n;
+        }
+        float *dst = stg + (size_t)buf * US * SPAN;
+        constexpr int PIECES = SPAN / 4;
+        for (int c = threadIdx.x; c < n * PIECES; c += 32 * NA) {
+            const int row = c / PIECES, col = (c % PIECES) * 4;
+            const int k = line_pixel_ray(A, orient, li, ulo + row);
+            const bool ok = yb + col < A.ys;
+            cp_async16(dst + row * SPAN + col, x + (size_t)k * ys + (ok ? yb + col : 0), ok);
+        }
+    };
+
+    if (L0 <= L1) {
+        ranges(L0);
+        __syncthreads();
+        stage(L0, 0);
+        cp_async_commit();
+    }
+    for (int li = L0; li <= L1; li++) {
+        const int buf = (li - L0) & 1;
+        __syncthreads();  // uinfo[buf] written by stage(li)
+        const int ulo = uinfo[2 * buf], un = uinfo[2 * buf + 1];
+        // Phase A: lanes = union pixels, in increasing centre-bin order for this angle.
         bool valid = false;
         int gk = 0;
         float4 ent = make_float4(0.f, 0.f, 0.f, 0.f);
-        if (angle_ok && li >= my_lo && li <= my_hi) {
-            const float Lv = (float)li - r;
-            int plo, phi;
-            if (orient == 0) {
-                const RowInfo ri = A.rows[li];
-                plo = ri.lo;
-                phi = ri.hi;
-            } else {
-                const ColInfo ci = A.cols[li];
-                plo = ci.lo;
-                phi = ci.hi;
-            }
-            float pa = (T1 - Lv * cl) / ca, pb = (T2 - Lv * cl) / ca;
-            if (pa > pb) {
-                float t = pa;
-                pa = pb;
-                pb = t;
-            }
-            const int clo = max(plo, (int)floorf(pa + r) - 1);
-            const int chi = min(phi, (int)ceilf(pb + r) + 1);
-            const int n = chi - clo + 1;
-            if (n > 32 && lane == 0) atomicOr(A.err, 1);
-            if (lane < n) {
-                const int pi = ca > 0.f ? clo + lane : chi - lane;
-                int kk;
-                if (orient == 0) {
-                    const RowInfo ri = A.rows[li];
-                    kk = ri.start + pi - ri.lo;
-                } else {
-                    const RowInfo ri = A.rows[pi];
-                    kk = ri.start + li - ri.lo;
-                }
-                const Taps t = ray_taps<W>(A.ray[kk], ap, A.r_hi, A.r_lo);
-                gk = t.iqx - b0 + 1;
-                valid = gk >= 0 && gk <= BT + 1;
-                ent = make_float4(__int_as_float(kk), t.w0, t.w1, t.w2);
-            }
+        if (angle_ok && lane < un && li >= my_lo && li <= my_hi) {
+            const int row = ca > 0.f ? lane : un - 1 - lane;
+            const int k = line_pixel_ray(A, orient, li, ulo + row);
+            const Taps t = ray_taps<W>(A.ray[k], ap, A.r_hi, A.r_lo);
+            gk = t.iqx - b0 + 1;
+            valid = gk >= 0 && gk <= BT + 1;
+            ent = make_float4(__int_as_float(row), t.w0, t.w1, t.w2);
         }
-        // Phase B: stable counting sort by bucket (line order, then lane order).
+        // Phase B (warp-local): stable counting sort by bucket.
         const unsigned key = valid ? (unsigned)gk : 64u + lane;
         const unsigned peers = __match_any_sync(0xffffffffu, key);
         const int rank = __popc(peers & ((1u << lane) - 1u));
-        if (lane < NG) cnt[warp][lane] = 0;
-        __syncwarp();
-        if (valid && rank == 0) cnt[warp][gk] = __popc(peers);
-        __syncthreads();
-        if (threadIdx.x < NA) {
-            int run = 0;
-            for (int gg = 0; gg < NG; gg++) {
-                base[threadIdx.x][gg] = run;
+        int mybase = 0;
 #pragma unroll
-                for (int s2 = 0; s2 < NSC; s2++) run += cnt[s2 * NA + threadIdx.x][gg];
-            }
-            base[threadIdx.x][NG] = run;
+        for (int gg = 0; gg <= NG; gg++) {
+            const int c = __popc(__ballot_sync(0xffffffffu, valid && gk < gg));
+            if (lane == gg) base[ai * (NG + 1) + gg] = c;
+            if (valid && gg == gk) mybase = c;
         }
+        if (valid) list[ai * 32 + mybase + rank] = ent;
+        // next line's ranges, then its staging one line ahead
+        if (li + 1 <= L1) ranges(li + 1);
         __syncthreads();
-        if (valid) {
-            int pos = base[ai][gk] + rank;
-            for (int w2 = ai; w2 < warp; w2 += NA) pos += cnt[w2][gk];
-            list[ai][pos] = ent;
-        }
+        if (li + 1 <= L1) stage(li + 1, buf ^ 1);
+        cp_async_commit();
+        cp_async_wait<1>();
         __syncthreads();
-        // Phase C: accumulate, bucket index known at compile time.
-        if (angle_ok && yok) {
-            const float *xb = x + y0;
+        // Phase C: accumulate with the bucket index known at compile time.
+        if (angle_ok) {
+            const float *S = stg + (size_t)buf * US * SPAN;
+            const int *bb = base + ai * (NG + 1);
 #pragma unroll
             for (int gg = 0; gg < NG; gg++) {
-                const int e1 = base[ai][gg + 1];
-                for (int i = base[ai][gg]; i < e1; i++) {
-                    const float4 e = list[ai][i];
+                const int e1 = bb[gg + 1];
+                for (int i = bb[gg]; i < e1; i++) {
+                    const float4 e = list[ai * 32 + i];
                     float v[VEC];
-                    ldv<VEC>(xb + (size_t)__float_as_int(e.x) * A.ys, v);
+                    lds_lane<VEC>(S + __float_as_int(e.x) * SPAN, lane, v);
                     if (gg >= 2) {
 #pragma unroll
                         for (int c = 0; c < VEC; c++) acc[gg >= 2 ? gg - 2 : 0][c] =
@@ -359,23 +606,23 @@ __global__ void __launch_bounds__(32 * kGroupAngles * NSC)
                 }
             }
         }
-        __syncthreads();
     }
+    cp_async_wait<0>();
 
     double s2 = 0.0;
-    if (angle_ok && yok) {
+    if (angle_ok) {
         const int a = G.x + ai;
-        float *qa = q + (size_t)a * A.nx * A.ys + y0;
+        float *qa = q + (size_t)a * A.nx * ys + yb;
 #pragma unroll
         for (int j = 0; j < BT; j++) {
             if (b0 + j < A.nx) {
-                stv<VEC>(qa + (size_t)(b0 + j) * A.ys, acc[j]);
+                stg_lane<VEC>(qa + (size_t)(b0 + j) * ys, lane, acc[j], A.ys - yb);
 #pragma unroll
                 for (int c = 0; c < VEC; c++) s2 += (double)__fmul_rn(acc[j][c], acc[j][c]);
             }
         }
     }
-    block_sum_to<NWARP>(s2, red, A.partials + (size_t)blockIdx.y * gridDim.x + blockIdx.x);
+    block_sum_to<NA>(s2, red, A.partials + (size_t)blockIdx.y * gridDim.x + blockIdx.x);
 }
 
 // ---------------------------------------------------------------------------
@@ -416,25 +663,54 @@ __global__ void __launch_bounds__(256) fp_lin_kernel(OpArgs A, const float *__re
 namespace arecgb {
 
 // Launch helpers, instantiated once per weighting in arec_project_{lin,kb,sq}.cu.
+template <int W, int V, int N>
+int launch_bp_one(const OpArgs &A, dim3 grid, const float *s, float *g, cudaStream_t st) {
+    if constexpr (W == ARECGB_LIN) {
+        bp_lin_kernel<V, N><<<grid, 128 * N, 0, st>>>(A, s, g);
+    } else {
+        constexpr size_t smem = bp_smem_bytes<V, N>();
+        static bool configured = false;  // per instantiation, once per process
+        if (!configured) {
+            if (cudaFuncSetAttribute(bp_kernel<W, V, N>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     (int)smem) != cudaSuccess)
+                return -2;
+            configured = true;
+        }
+        bp_kernel<W, V, N><<<grid, 128 * N, smem, st>>>(A, s, g);
+    }
+    return 0;
+}
+
 template <int W>
 int launch_bp(const OpArgs &A, int vec, int nsc, dim3 grid, const float *s, float *g,
               cudaStream_t st) {
-#define ARECGB_BP(V, N)                                                        \
-    if (vec == V && nsc == N) {                                                \
-        bp_kernel<W, V, N><<<grid, 128 * N, 0, st>>>(A, s, g);                 \
-        return 0;                                                              \
-    }
+#define ARECGB_BP(V, N) \
+    if (vec == V && nsc == N) return launch_bp_one<W, V, N>(A, grid, s, g, st);
     ARECGB_BP(1, 1) ARECGB_BP(2, 1) ARECGB_BP(4, 1) ARECGB_BP(8, 1)
     ARECGB_BP(1, 2) ARECGB_BP(2, 2) ARECGB_BP(4, 2) ARECGB_BP(8, 2)
 #undef ARECGB_BP
     return -1;
 }
 
+template <int W, int V, int BT>
+int launch_fp_one(const OpArgs &A, dim3 grid, const float *x, float *q, cudaStream_t st) {
+    constexpr size_t smem = fp_smem_bytes<V>();
+    static bool configured = false;  // per instantiation, once per process
+    if (!configured) {
+        if (cudaFuncSetAttribute(fp_kernel<W, V, BT>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 (int)smem) != cudaSuccess)
+            return -2;
+        configured = true;
+    }
+    fp_kernel<W, V, BT><<<grid, 32 * kGroupAngles, smem, st>>>(A, x, q);
+    return 0;
+}
+
 template <int W, int BT>
 int launch_fp(const OpArgs &A, int vec, int nsc, dim3 grid, const float *x, float *q,
               cudaStream_t st) {
+    (void)nsc;
     if constexpr (W == ARECGB_LIN) {
-        (void)nsc;
         (void)grid;
         const long long n = (long long)A.nrays * (A.ys / vec);
         const unsigned blocks = (unsigned)((n + 255) / 256);
@@ -444,15 +720,10 @@ int launch_fp(const OpArgs &A, int vec, int nsc, dim3 grid, const float *x, floa
         else fp_lin_kernel<8><<<blocks, 256, 0, st>>>(A, x, q);
         return 0;
     } else {
-#define ARECGB_FP(V, N)                                                                   \
-    if (vec == V && nsc == N) {                                                           \
-        fp_kernel<W, V, N, BT><<<grid, 32 * kGroupAngles * N, 0, st>>>(A, x, q);          \
-        return 0;                                                                         \
-    }
-        ARECGB_FP(1, 1) ARECGB_FP(2, 1) ARECGB_FP(4, 1) ARECGB_FP(8, 1)
-        ARECGB_FP(1, 2) ARECGB_FP(2, 2) ARECGB_FP(4, 2) ARECGB_FP(8, 2)
-#undef ARECGB_FP
-        return -1;
+        if (vec == 1) return launch_fp_one<W, 1, BT>(A, grid, x, q, st);
+        if (vec == 2) return launch_fp_one<W, 2, BT>(A, grid, x, q, st);
+        if (vec == 4) return launch_fp_one<W, 4, BT>(A, grid, x, q, st);
+        return launch_fp_one<W, 8, BT>(A, grid, x, q, st);
     }
 }
 

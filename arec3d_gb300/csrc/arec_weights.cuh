@@ -53,18 +53,19 @@ __device__ __forceinline__ void ray_position(const float4 ray, const AngleParams
     lo = l;
 }
 
-// rint(u + lo) with ties to even, and f = (u + lo) - rint(u + lo) as (d, lo).
+// rint(u + lo) with ties to even, and d with (u + lo) - rint(u + lo) = d + lo.
+// n = rintf(u) leaves d = u - n exact with |d| <= 0.5; since |lo| is below half
+// an ulp of u, only d = +-0.5 (u on a half-integer, where rintf chose the even
+// neighbour) can round the other way, and then the sign of lo decides.
 __device__ __forceinline__ int round_centre(float u, float lo, float &d) {
     float n = rintf(u);
-    d = __fsub_rn(u, n);  // exact: |u - n| <= 0.5 and n is u rounded
-    float f = __fadd_rn(d, lo);
-    int odd = ((int)n) & 1;
-    if (f > 0.5f || (f == 0.5f && odd)) {
+    d = __fsub_rn(u, n);
+    if (d == 0.5f && lo > 0.0f) {
         n = __fadd_rn(n, 1.0f);
-        d = __fsub_rn(d, 1.0f);
-    } else if (f < -0.5f || (f == -0.5f && odd)) {
+        d = -0.5f;
+    } else if (d == -0.5f && lo < 0.0f) {
         n = __fsub_rn(n, 1.0f);
-        d = __fadd_rn(d, 1.0f);
+        d = 0.5f;
     }
     return (int)n;
 }

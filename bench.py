@@ -181,6 +181,31 @@ def run_reference(args, rank, world):
     print(json.dumps(out))
 
 
+def kernels_only(args):
+    """Forward and back projector of the benchmark geometry on `--slices`
+    slices, `--launches` times each (a short command for ncu)."""
+    import torch
+
+    import arec3d_gb300 as gb
+    from arec3d_gb300 import synthetic as syn
+
+    gb.build()
+    angles = syn.uniform_angles(args.angles)
+    plan = gb.Plan(gb.SQ, 0.5 * (NX - 1), args.slices, angles)
+    g = torch.Generator(device="cuda")
+    g.manual_seed(0)
+    x = torch.rand(plan.nrays, plan.ys, device="cuda", generator=g)
+    x[:, args.slices:] = 0
+    q = torch.zeros(plan.nangles, plan.nx, plan.ys, device="cuda")
+    n2 = torch.zeros(1, dtype=torch.float64, device="cuda")
+    for _ in range(args.launches):
+        plan.project(x, q, norm2=n2)
+        plan.backproject(q, x, norm2=n2)
+    torch.cuda.synchronize()
+    print(json.dumps({"kernels_only": True, "slices": args.slices, "launches": args.launches,
+                      "norm2": float(n2.item())}))
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -192,8 +217,16 @@ def main():
     ap.add_argument("--ref-slices", type=int, default=16)
     ap.add_argument("--ref-iters", type=int, default=60,
                     help="iterations to extrapolate the reference arm to")
+    ap.add_argument("--kernels-only", action="store_true",
+                    help="run only the forward and back projectors (for profiling)")
+    ap.add_argument("--slices", type=int, default=NY, help="slices for --kernels-only")
+    ap.add_argument("--launches", type=int, default=3, help="launches for --kernels-only")
+    ap.add_argument("--angles", type=int, default=NA, help="angles for --kernels-only")
     args = ap.parse_args()
     rank, local, world = dist_env()
+    if args.kernels_only:
+        kernels_only(args)
+        return
 
     if args.impl == "reference":
         run_reference(args, rank, world)

@@ -64,6 +64,11 @@ int arecgb_plan_destroy(arecgb_plan *plan);
 /* nx = detector width = round(2r+1), nrays = pixels in the disk, ys = slice stride. */
 int arecgb_plan_info(const arecgb_plan *plan, int *nx, int *nrays, int *ys);
 
+/* Device-side consistency flag of the plan's kernels since the last check
+ * (0 = none; nonzero means a geometric bound the kernels rely on was violated),
+ * cleared by the call.  Synchronises the device. */
+int arecgb_plan_check(arecgb_plan *plan);
+
 /* q = A x (replaces arecProject2D[_KB|_SQ], arecproject.cpp:19,351,540).
  * d_norm2 (device, optional) receives sum(q*q) accumulated in double. */
 int arecgb_project(arecgb_plan *plan, const float *d_x, float *d_q, double *d_norm2,

@@ -25,6 +25,7 @@ MAX_TRACE = 4096
 
 _f32p = np.ctypeslib.ndpointer(np.float32, flags="C_CONTIGUOUS")
 _i32p = np.ctypeslib.ndpointer(np.int32, flags="C_CONTIGUOUS")
+_f64p = np.ctypeslib.ndpointer(np.float64, flags="C_CONTIGUOUS")
 
 
 class Trace(C.Structure):
@@ -61,6 +62,13 @@ def lib():
                               C.c_float, _f32p, C.c_int, C.c_int, C.POINTER(Trace)]
         L.oc_cgls.argtypes = [C.c_int, C.c_int, C.c_int, C.c_int, _f32p, _f32p, C.c_int, C.c_float,
                               _f32p, C.c_int, C.c_double, C.c_int, C.c_int, C.POINTER(Trace)]
+        L.oc_project64.argtypes = [C.c_int, C.c_double, C.c_int, _f64p, _f32p, C.c_int, _f64p]
+        L.oc_backproject64.argtypes = [C.c_int, C.c_double, C.c_int, _f64p, _f32p, C.c_int, _f64p]
+        L.oc_sirt64.argtypes = [C.c_int, C.c_int, C.c_int, C.c_int, _f64p, _f32p, C.c_float,
+                                C.c_int, C.c_float, _f64p, C.c_int, C.c_int, C.POINTER(Trace)]
+        L.oc_cgls64.argtypes = [C.c_int, C.c_int, C.c_int, C.c_int, _f64p, _f32p, C.c_int,
+                                C.c_float, _f64p, C.c_int, C.c_double, C.c_int, C.c_int,
+                                C.POINTER(Trace)]
         L.oc_ccorr2d.argtypes = [C.c_int, C.c_int, _f32p, _f32p, _f32p]
         L.oc_quad2dfit.argtypes = [_f32p, C.POINTER(C.c_float), C.POINTER(C.c_float),
                                    C.POINTER(C.c_float)]
@@ -129,6 +137,51 @@ def cgls(weighting, b, angles, maxit=10, tol=1e-3, x0=None, rnorm_ref=0.0, nthre
     tr = Trace()
     lib().oc_cgls(weighting, nx, ny, na, b, f32(angles), maxit, tol, x, int(x0 is not None),
                   float(rnorm_ref), nthreads, int(verbose), C.byref(tr))
+    return x, tr
+
+
+# --- FP64 oracle: the reference's weights, every sum and update in double ---------------------
+def f64(a):
+    return np.ascontiguousarray(a, dtype=np.float64)
+
+
+def project64(weighting, radius, x, angles):
+    x = f64(x)
+    nx, nr, _ = cyl(radius)
+    angles = f32(angles)
+    q = np.zeros((len(angles), x.shape[1], nx), np.float64)
+    lib().oc_project64(weighting, radius, x.shape[1], x, angles, len(angles), q)
+    return q
+
+
+def backproject64(weighting, radius, q, angles):
+    q = f64(q)
+    nx, nr, _ = cyl(radius)
+    angles = f32(angles)
+    g = np.zeros((nr, q.shape[1]), np.float64)
+    lib().oc_backproject64(weighting, radius, q.shape[1], q, angles, len(angles), g)
+    return g
+
+
+def sirt64(weighting, b, angles, lam=5e-6, maxit=10, tol=1e-3, nthreads=1):
+    b = f64(b)
+    na, ny, nx = b.shape
+    _, nr, _ = cyl(0.5 * (nx - 1))
+    x = np.zeros((nr, ny), np.float64)
+    tr = Trace()
+    lib().oc_sirt64(weighting, nx, ny, na, b, f32(angles), lam, maxit, tol, x, nthreads, 0,
+                    C.byref(tr))
+    return x, tr
+
+
+def cgls64(weighting, b, angles, maxit=10, tol=1e-3, x0=None, rnorm_ref=0.0, nthreads=1):
+    b = f64(b)
+    na, ny, nx = b.shape
+    _, nr, _ = cyl(0.5 * (nx - 1))
+    x = np.zeros((nr, ny), np.float64) if x0 is None else f64(x0).copy()
+    tr = Trace()
+    lib().oc_cgls64(weighting, nx, ny, na, b, f32(angles), maxit, tol, x, int(x0 is not None),
+                    float(rnorm_ref), nthreads, 0, C.byref(tr))
     return x, tr
 
 

@@ -134,67 +134,6 @@ static int geom_init(geom *g, double radius) {
 
 static void geom_free(geom *g) { free(g->cord); }
 
-/* arecProject2D_SQ (arecproject.cpp:540-648) */
-static void fp_sq(const geom *g, int ny, const float *x, const float *angles, int na, float *q) {
-    const int nx = g->nx;
-    const double xcent = g->radius, zcent = g->radius;
-    memset(q, 0, sizeof(float) * (size_t)nx * ny * na);
-    for (int ia = 0; ia < na; ia++) {
-        double c = (double)cosf(angles[ia]), s = (double)sinf(angles[ia]);
-        sq_par p = sq_points((double)angles[ia]);
-        float *qa = q + (size_t)ia * nx * ny;
-        for (int i = 0; i < g->nrays; i++) {
-            double xc = g->cord[2 * i] - xcent;
-            double zc = g->cord[2 * i + 1] - zcent;
-            double xb = xc * c + zc * s + xcent;
-            int iqx = (int)rint(xb);
-            double xv = iqx - xb;
-            double v0 = sq_cdf(xv - 1.5, p), v1 = sq_cdf(xv - 0.5, p);
-            double v2 = sq_cdf(xv + 0.5, p), v3 = sq_cdf(xv + 1.5, p);
-            double w[3] = {v1 - v0, v2 - v1, v3 - v2};
-            const float *xr = x + (size_t)i * ny;
-            for (int iy = 0; iy < ny; iy++) {
-                float ct = xr[iy];
-                float *row = qa + (size_t)iy * nx;
-                for (int j = 0; j < 3; j++) {
-                    int b = iqx - 1 + j;
-                    if (b >= 0 && b < nx) row[b] = (float)((double)row[b] + w[j] * (double)ct);
-                }
-            }
-        }
-    }
-}
-
-/* arecBackProject2D_SQ (arecproject.cpp:650-765) */
-static void bp_sq(const geom *g, int ny, const float *q, const float *angles, int na, float *out) {
-    const int nx = g->nx;
-    const double xcent = g->radius, zcent = g->radius;
-    memset(out, 0, sizeof(float) * (size_t)g->nrays * ny);
-    for (int ia = 0; ia < na; ia++) {
-        double c = (double)cosf(angles[ia]), s = (double)sinf(angles[ia]);
-        sq_par p = sq_points((double)angles[ia]);
-        const float *qa = q + (size_t)ia * nx * ny;
-        for (int i = 0; i < g->nrays; i++) {
-            double xc = g->cord[2 * i] - xcent;
-            double zc = g->cord[2 * i + 1] - zcent;
-            double xb = xc * c + zc * s + xcent;
-            int iqx = (int)rint(xb);
-            double xv = iqx - xb;
-            double v0 = sq_cdf(xv - 1.5, p), v1 = sq_cdf(xv - 0.5, p);
-            double v2 = sq_cdf(xv + 0.5, p), v3 = sq_cdf(xv + 1.5, p);
-            double w[3] = {v1 - v0, v2 - v1, v3 - v2};
-            float *o = out + (size_t)i * ny;
-            for (int iy = 0; iy < ny; iy++) {
-                const float *row = qa + (size_t)iy * nx;
-                for (int j = 0; j < 3; j++) {
-                    int b = iqx - 1 + j;
-                    if (b >= 0 && b < nx) o[iy] = (float)((double)o[iy] + w[j] * (double)row[b]);
-                }
-            }
-        }
-    }
-}
-
 /* arecProject2D_KB (arecproject.cpp:351-437): weights are the float table
  * interpolant evaluated at float(xb - bin). */
 static void kb_weights(double xb, int *iqx_out, double w[3]) {
@@ -203,60 +142,6 @@ static void kb_weights(double xb, int *iqx_out, double w[3]) {
     w[1] = (double)kb_interp((float)(xb - iqx));
     w[2] = (double)kb_interp((float)(xb - (iqx + 1)));
     *iqx_out = iqx;
-}
-
-static void fp_kb(const geom *g, int ny, const float *x, const float *angles, int na, float *q) {
-    const int nx = g->nx;
-    const double xcent = g->radius, zcent = g->radius;
-    memset(q, 0, sizeof(float) * (size_t)nx * ny * na);
-    for (int ia = 0; ia < na; ia++) {
-        double c = (double)cosf(angles[ia]), s = (double)sinf(angles[ia]);
-        float *qa = q + (size_t)ia * nx * ny;
-        for (int i = 0; i < g->nrays; i++) {
-            double xc = g->cord[2 * i] - xcent;
-            double zc = g->cord[2 * i + 1] - zcent;
-            double xb = xc * c + zc * s + xcent;
-            int iqx;
-            double w[3];
-            kb_weights(xb, &iqx, w);
-            const float *xr = x + (size_t)i * ny;
-            for (int iy = 0; iy < ny; iy++) {
-                float ct = xr[iy];
-                float *row = qa + (size_t)iy * nx;
-                for (int j = 0; j < 3; j++) {
-                    int b = iqx - 1 + j;
-                    if (b >= 0 && b < nx) row[b] = (float)((double)row[b] + w[j] * (double)ct);
-                }
-            }
-        }
-    }
-}
-
-/* arecBackProject2D_KB (arecproject.cpp:447-535) */
-static void bp_kb(const geom *g, int ny, const float *q, const float *angles, int na, float *out) {
-    const int nx = g->nx;
-    const double xcent = g->radius, zcent = g->radius;
-    memset(out, 0, sizeof(float) * (size_t)g->nrays * ny);
-    for (int ia = 0; ia < na; ia++) {
-        double c = (double)cosf(angles[ia]), s = (double)sinf(angles[ia]);
-        const float *qa = q + (size_t)ia * nx * ny;
-        for (int i = 0; i < g->nrays; i++) {
-            double xc = g->cord[2 * i] - xcent;
-            double zc = g->cord[2 * i + 1] - zcent;
-            double xb = xc * c + zc * s + xcent;
-            int iqx;
-            double w[3];
-            kb_weights(xb, &iqx, w);
-            float *o = out + (size_t)i * ny;
-            for (int iy = 0; iy < ny; iy++) {
-                const float *row = qa + (size_t)iy * nx;
-                for (int j = 0; j < 3; j++) {
-                    int b = iqx - 1 + j;
-                    if (b >= 0 && b < nx) o[iy] = (float)((double)o[iy] + w[j] * (double)row[b]);
-                }
-            }
-        }
-    }
 }
 
 /* arecProject2D (arecproject.cpp:19-99), pmethod=1.  The loop runs i = 1..nrays
@@ -276,87 +161,6 @@ static void lin_weights(const geom *g, int k, double c, double s, int *b0, float
     *w0 = (float)(1.0 - (double)d);
     *w1 = d;
     *b0 = iqx - 1;
-}
-
-static void fp_lin(const geom *g, int ny, const float *x, const float *angles, int na, float *q) {
-    const int nx = g->nx;
-    memset(q, 0, sizeof(float) * (size_t)nx * ny * na);
-    for (int ia = 0; ia < na; ia++) {
-        double c = (double)cosf(angles[ia]), s = (double)sinf(angles[ia]);
-        float *qa = q + (size_t)ia * nx * ny;
-        for (int k = 0; k < g->nrays; k++) {
-            int b0;
-            float w0, w1;
-            lin_weights(g, k, c, s, &b0, &w0, &w1);
-            const float *xr = x + (size_t)k * ny;
-            for (int iy = 0; iy < ny; iy++) {
-                float ct = xr[iy];
-                float *row = qa + (size_t)iy * nx;
-                if (b0 >= 0 && b0 < nx) row[b0] += w0 * ct;
-                if (b0 + 1 >= 0 && b0 + 1 < nx) row[b0 + 1] += w1 * ct;
-            }
-        }
-    }
-}
-
-/* arecBackProject2D (arecproject.cpp:109-183): the two taps are applied as two
- * passes over the slices, in float. */
-static void bp_lin(const geom *g, int ny, const float *q, const float *angles, int na,
-                   float *out) {
-    const int nx = g->nx;
-    memset(out, 0, sizeof(float) * (size_t)g->nrays * ny);
-    for (int ia = 0; ia < na; ia++) {
-        double c = (double)cosf(angles[ia]), s = (double)sinf(angles[ia]);
-        const float *qa = q + (size_t)ia * nx * ny;
-        for (int k = 0; k < g->nrays; k++) {
-            int b0;
-            float w0, w1;
-            lin_weights(g, k, c, s, &b0, &w0, &w1);
-            float *o = out + (size_t)k * ny;
-            if (b0 >= 0 && b0 < nx)
-                for (int iy = 0; iy < ny; iy++) o[iy] += w0 * qa[(size_t)iy * nx + b0];
-            if (b0 + 1 >= 0 && b0 + 1 < nx)
-                for (int iy = 0; iy < ny; iy++) o[iy] += w1 * qa[(size_t)iy * nx + b0 + 1];
-        }
-    }
-}
-
-static void geom_fp(int weighting, const geom *g, int ny, const float *x, const float *angles,
-                    int na, float *q) {
-    if (weighting == 1)
-        fp_lin(g, ny, x, angles, na, q);
-    else if (weighting == 2)
-        fp_kb(g, ny, x, angles, na, q);
-    else
-        fp_sq(g, ny, x, angles, na, q);
-}
-
-static void geom_bp(int weighting, const geom *g, int ny, const float *q, const float *angles,
-                    int na, float *out) {
-    if (weighting == 1)
-        bp_lin(g, ny, q, angles, na, out);
-    else if (weighting == 2)
-        bp_kb(g, ny, q, angles, na, out);
-    else
-        bp_sq(g, ny, q, angles, na, out);
-}
-
-int oc_project(int weighting, double radius, int ny, const float *x, const float *angles,
-               int nangles, float *q) {
-    geom g;
-    if (geom_init(&g, radius)) return -1;
-    geom_fp(weighting, &g, ny, x, angles, nangles, q);
-    geom_free(&g);
-    return 0;
-}
-
-int oc_backproject(int weighting, double radius, int ny, const float *q, const float *angles,
-                   int nangles, float *out) {
-    geom g;
-    if (geom_init(&g, radius)) return -1;
-    geom_bp(weighting, &g, ny, q, angles, nangles, out);
-    geom_free(&g);
-    return 0;
 }
 
 /* ----------------------------------------------------------------------------
@@ -394,276 +198,18 @@ static void slab_range(int ny, int nranks, int rank, int *y0, int *nyl) {
     }
 }
 
-typedef struct {
-    int method; /* 0 = SIRT, 1 = CGLS */
-    int weighting, nx, ny, na;
-    const float *b, *angles;
-    float lam, tol;
-    int maxit, warm, verbose;
-    double rnorm_ref;
-    float *x;
-    oc_trace *tr;
-    comm_t *cm;
-    int rank;
-    int status;
-} solve_arg;
-
-/* cyl_sirt_SQ (AREC3D/AREC3D/arecsirt.cpp:193-373) on one slab.  The
- * squared norm of A^T b is accumulated into a variable that is never reset, so
- * after each restart the denominator grows (arecsirt.cpp:273,285-290). */
-static int sirt_slab(solve_arg *a, const geom *g, int nyl, const float *bl, float *xl) {
-    const int nx = g->nx, na = a->na, rank = a->rank;
-    size_t nnz = (size_t)g->nrays * nyl, nsin = (size_t)nx * nyl * na;
-    float *proj = (float *)calloc(nsin ? nsin : 1, sizeof(float));
-    float *bvol = (float *)calloc(nnz ? nnz : 1, sizeof(float));
-    float *pvol = (float *)calloc(nnz ? nnz : 1, sizeof(float));
-    float *grad = (float *)calloc(nnz ? nnz : 1, sizeof(float));
-    float lam = a->lam;
-    double relnrm0 = 1.00001, bnorm2 = 0.0, bnorm = 0.0;
-    int restarts = 0, iter = 1, count = 0;
-    memset(xl, 0, sizeof(float) * nnz);
-    while (iter <= a->maxit) {
-        double relnrm;
-        if (iter == 1) {
-            if (restarts == 0) geom_bp(a->weighting, g, nyl, bl, a->angles, na, bvol);
-            for (size_t j = 0; j < nnz; j++) {
-                bnorm2 += (double)(bvol[j] * bvol[j]);
-                grad[j] = bvol[j];
-            }
-            bnorm = sqrt(allreduce_sum(a->cm, rank, bnorm2));
-        } else {
-            geom_fp(a->weighting, g, nyl, xl, a->angles, na, proj);
-            geom_bp(a->weighting, g, nyl, proj, a->angles, na, pvol);
-            for (size_t j = 0; j < nnz; j++) {
-                grad[j] = bvol[j];
-                grad[j] -= pvol[j];
-            }
-        }
-        double rn2 = 0.0;
-        for (size_t j = 0; j < nnz; j++) rn2 += grad[j] * (double)grad[j];
-        double rnorm = sqrt(allreduce_sum(a->cm, rank, rn2));
-        relnrm = rnorm / bnorm;
-        if (rank == 0 && a->tr) {
-            if (count < OC_MAX_TRACE) {
-                a->tr->rel[count] = relnrm;
-                a->tr->rnorm[count] = rnorm;
-            }
-            if (count == 0) a->tr->rnorm0 = rnorm;
-        }
-        count++;
-        if (rank == 0 && a->verbose)
-            printf("iter = %3d, rnorm / bnorm = %11.3e, rnorm = %11.3e\n", iter, relnrm, rnorm);
-        if (relnrm > relnrm0) {
-            if (restarts > 20) {
-                if (rank == 0 && a->verbose)
-                    printf("Failure to converge, even with lam = %11.3e\n", lam);
-                break;
-            }
-            ++restarts;
-            iter = 1;
-            lam /= 2.0;
-            relnrm0 = 1.0001;
-            memset(xl, 0, sizeof(float) * nnz);
-            memset(pvol, 0, sizeof(float) * nnz);
-            if (rank == 0 && a->verbose) printf("reducing lam to %11.3e, restarting\n", lam);
-            continue;
-        }
-        if (relnrm < a->tol || relnrm > relnrm0) break;
-        relnrm0 = relnrm;
-        for (size_t j = 0; j < nnz; j++) {
-            xl[j] += lam * grad[j];
-            pvol[j] = 0.0f;
-        }
-        ++iter;
-    }
-    if (rank == 0 && a->tr) {
-        a->tr->iterations = count;
-        a->tr->restarts = restarts;
-        a->tr->lam_final = lam;
-    }
-    free(proj);
-    free(bvol);
-    free(pvol);
-    free(grad);
-    return 0;
-}
-
-/* cyl_cgls_SQ (AREC3D/AREC3D/areccgls.cpp:245-478) on one slab.  Scalars are
- * double; vector updates evaluate in double and store float; norms sum float
- * products in double; the best iterate (smallest normal-equation residual) is
- * restored unless it is the iterate maxit-1 (areccgls.cpp:459-463). */
-static int cgls_slab(solve_arg *a, const geom *g, int nyl, const float *bl, float *xl) {
-    const int nx = g->nx, na = a->na, rank = a->rank;
-    size_t nnz = (size_t)g->nrays * nyl, nsin = (size_t)nx * nyl * na;
-    float *proj = (float *)calloc(nsin ? nsin : 1, sizeof(float));
-    float *sres = (float *)calloc(nsin ? nsin : 1, sizeof(float));
-    float *gvol = (float *)calloc(nnz ? nnz : 1, sizeof(float));
-    float *pvol = (float *)calloc(nnz ? nnz : 1, sizeof(float));
-    float *xsave = (float *)calloc(nnz ? nnz : 1, sizeof(float));
-    int iterbest = a->maxit - 1, iter = 1, count = 0;
-    double gamma, gamma0 = 0.0, rnorm, rnorm0, relnrm, rnorm_min;
-    if (a->warm)
-        geom_fp(a->weighting, g, nyl, xl, a->angles, na, proj);
-    else
-        memset(xl, 0, sizeof(float) * nnz);
-    for (size_t i = 0; i < nsin; i++) sres[i] = bl[i] - proj[i];
-    geom_bp(a->weighting, g, nyl, sres, a->angles, na, gvol);
-    double rn2 = 0.0;
-    for (size_t j = 0; j < nnz; j++) rn2 += (double)(gvol[j] * gvol[j]);
-    gamma = allreduce_sum(a->cm, rank, rn2);
-    rnorm0 = sqrt(gamma);
-    double denom = a->rnorm_ref > 0 ? a->rnorm_ref : rnorm0;
-    if (rank == 0 && a->verbose) printf("CG iter = 0, resnrm = %11.3e\n", rnorm0);
-    if (rank == 0 && a->tr) a->tr->rnorm0 = rnorm0;
-    rnorm_min = rnorm0;
-    while (iter <= a->maxit) {
-        if (iter == 1) {
-            memcpy(pvol, gvol, sizeof(float) * nnz);
-        } else {
-            double beta = gamma / gamma0;
-            for (size_t j = 0; j < nnz; j++) pvol[j] = (float)((double)gvol[j] + beta * (double)pvol[j]);
-        }
-        geom_fp(a->weighting, g, nyl, pvol, a->angles, na, proj);
-        double pn2 = 0.0;
-        for (size_t j = 0; j < nsin; j++) pn2 += (double)(proj[j] * proj[j]);
-        double alpha = gamma / allreduce_sum(a->cm, rank, pn2);
-        for (size_t j = 0; j < nnz; j++) xl[j] = (float)((double)xl[j] + alpha * (double)pvol[j]);
-        for (size_t j = 0; j < nsin; j++)
-            sres[j] = (float)((double)sres[j] - alpha * (double)proj[j]);
-        geom_bp(a->weighting, g, nyl, sres, a->angles, na, gvol);
-        rn2 = 0.0;
-        for (size_t j = 0; j < nnz; j++) rn2 += (double)(gvol[j] * gvol[j]);
-        gamma0 = gamma;
-        gamma = allreduce_sum(a->cm, rank, rn2);
-        rnorm = sqrt(gamma);
-        relnrm = rnorm / denom;
-        if (rnorm < rnorm_min) {
-            rnorm_min = rnorm;
-            iterbest = iter;
-            memcpy(xsave, xl, sizeof(float) * nnz);
-        }
-        if (rank == 0 && a->tr && count < OC_MAX_TRACE) {
-            a->tr->rel[count] = relnrm;
-            a->tr->rnorm[count] = rnorm;
-        }
-        count++;
-        if (rank == 0 && a->verbose)
-            printf("CG iter = %3d, rnorm / bnorm = %11.3e, rnorm = %11.3e\n", iter, relnrm, rnorm);
-        if (relnrm < a->tol) break;
-        ++iter;
-    }
-    if (iterbest < a->maxit - 1) memcpy(xl, xsave, sizeof(float) * nnz);
-    if (rank == 0 && a->tr) {
-        a->tr->iterations = count;
-        a->tr->iterbest = iterbest;
-    }
-    free(proj);
-    free(sres);
-    free(gvol);
-    free(pvol);
-    free(xsave);
-    return 0;
-}
-
-static void *solve_thread(void *p) {
-    solve_arg *a = (solve_arg *)p;
-    geom g;
-    if (geom_init(&g, 0.5 * (a->nx - 1))) {
-        a->status = -1;
-        return NULL;
-    }
-    int y0 = 0, nyl = 0;
-    slab_range(a->ny, a->cm->nranks, a->rank, &y0, &nyl);
-    const int nx = a->nx, na = a->na;
-    /* gather this slab's slices of b ([na][ny][nx]) and of x ([nrays][ny]) */
-    float *bl = (float *)malloc(sizeof(float) * ((size_t)nx * nyl * na + 1));
-    float *xl = (float *)malloc(sizeof(float) * ((size_t)g.nrays * nyl + 1));
-    for (int ia = 0; ia < na; ia++)
-        memcpy(bl + (size_t)ia * nyl * nx, a->b + ((size_t)ia * a->ny + y0) * nx,
-               sizeof(float) * (size_t)nyl * nx);
-    for (int k = 0; k < g.nrays; k++)
-        memcpy(xl + (size_t)k * nyl, a->x + (size_t)k * a->ny + y0, sizeof(float) * nyl);
-    a->status = a->method == 0 ? sirt_slab(a, &g, nyl, bl, xl) : cgls_slab(a, &g, nyl, bl, xl);
-    for (int k = 0; k < g.nrays; k++)
-        memcpy(a->x + (size_t)k * a->ny + y0, xl + (size_t)k * nyl, sizeof(float) * nyl);
-    free(bl);
-    free(xl);
-    geom_free(&g);
-    return NULL;
-}
-
-static int run_solver(solve_arg *proto, int nthreads) {
-    if (nthreads < 1) nthreads = 1;
-    if (nthreads > proto->ny) nthreads = proto->ny;
-    comm_t cm;
-    cm.nranks = nthreads;
-    cm.slot = (double *)calloc((size_t)nthreads, sizeof(double));
-    if (nthreads > 1) pthread_barrier_init(&cm.bar, NULL, (unsigned)nthreads);
-    solve_arg *args = (solve_arg *)calloc((size_t)nthreads, sizeof(solve_arg));
-    pthread_t *th = (pthread_t *)calloc((size_t)nthreads, sizeof(pthread_t));
-    for (int r = 0; r < nthreads; r++) {
-        args[r] = *proto;
-        args[r].cm = &cm;
-        args[r].rank = r;
-        if (r > 0) args[r].tr = NULL;
-    }
-    if (nthreads == 1) {
-        solve_thread(&args[0]);
-    } else {
-        for (int r = 0; r < nthreads; r++) pthread_create(&th[r], NULL, solve_thread, &args[r]);
-        for (int r = 0; r < nthreads; r++) pthread_join(th[r], NULL);
-        pthread_barrier_destroy(&cm.bar);
-    }
-    int st = 0;
-    for (int r = 0; r < nthreads; r++)
-        if (args[r].status) st = args[r].status;
-    free(args);
-    free(th);
-    free(cm.slot);
-    return st;
-}
-
-int oc_sirt(int weighting, int nx, int ny, int nangles, const float *b, const float *angles,
-            float lam, int maxit, float tol, float *x, int nthreads, int verbose, oc_trace *tr) {
-    solve_arg a;
-    memset(&a, 0, sizeof(a));
-    a.method = 0;
-    a.weighting = weighting;
-    a.nx = nx;
-    a.ny = ny;
-    a.na = nangles;
-    a.b = b;
-    a.angles = angles;
-    a.lam = lam;
-    a.tol = tol;
-    a.maxit = maxit;
-    a.verbose = verbose;
-    a.x = x;
-    a.tr = tr;
-    return run_solver(&a, nthreads);
-}
-
-int oc_cgls(int weighting, int nx, int ny, int nangles, const float *b, const float *angles,
-            int maxit, float tol, float *x, int warm, double rnorm_ref, int nthreads, int verbose,
-            oc_trace *tr) {
-    solve_arg a;
-    memset(&a, 0, sizeof(a));
-    a.method = 1;
-    a.weighting = weighting;
-    a.nx = nx;
-    a.ny = ny;
-    a.na = nangles;
-    a.b = b;
-    a.angles = angles;
-    a.tol = tol;
-    a.maxit = maxit;
-    a.warm = warm;
-    a.rnorm_ref = rnorm_ref;
-    a.verbose = verbose;
-    a.x = x;
-    a.tr = tr;
-    return run_solver(&a, nthreads);
-}
+#define CAT2(a, b) a##b
+#define CAT(a, b) CAT2(a, b)
+#define REAL float
+#define FN(n) n
+#include "oracle_ops.inc"
+#undef REAL
+#undef FN
+#define REAL double
+#define FN(n) CAT(n, 64)
+#include "oracle_ops.inc"
+#undef REAL
+#undef FN
 
 /* ----------------------------------------------------------------------------
  * Cross-correlation shift search.

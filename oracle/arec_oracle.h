@@ -59,6 +59,18 @@ int oc_cgls(int weighting, int nx, int ny, int nangles, const float *b, const fl
             int maxit, float tol, float *x, int warm, double rnorm_ref, int nthreads, int verbose,
             oc_trace *tr);
 
+/* FP64 oracle: the same operators (the reference's weights) applied with
+ * every sum, update and vector in double; arrays are double. */
+int oc_project64(int weighting, double radius, int ny, const double *x, const float *angles,
+                 int nangles, double *q);
+int oc_backproject64(int weighting, double radius, int ny, const double *q, const float *angles,
+                     int nangles, double *g);
+int oc_sirt64(int weighting, int nx, int ny, int nangles, const double *b, const float *angles,
+              float lam, int maxit, float tol, double *x, int nthreads, int verbose, oc_trace *tr);
+int oc_cgls64(int weighting, int nx, int ny, int nangles, const double *b, const float *angles,
+              int maxit, float tol, double *x, int warm, double rnorm_ref, int nthreads,
+              int verbose, oc_trace *tr);
+
 /* ccorr2d / speak / quad2dfit / arecCCImages
  * (AREC3D/AREC3D/align2dstack.cpp:480-521, 1059-1166; arecImage.cpp:384-434).
  * Images are [ny][nx] row-major; the FFT is oracle/fft64.c in double. */

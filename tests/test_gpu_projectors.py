@@ -45,6 +45,7 @@ def test_fp_bp_parity(gb, oc, w, gi):
     if w == 1:
         g, g_ref = g[:-2], g_ref[:-2]
     assert rel_l2(g, g_ref) < TOL
+    assert plan.check() == 0
 
 
 @pytest.mark.parametrize("w", [1, 2, 3])
