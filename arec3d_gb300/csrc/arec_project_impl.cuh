@@ -387,9 +387,9 @@ constexpr int kFpStage = 32;  // staged pixels per line: the union of the group'
 
 template <int VEC>
 constexpr size_t fp_smem_bytes() {
-    return sizeof(float) * 2 * kFpStage * (32 * VEC) + sizeof(float4) * kGroupAngles * 32 +
-           sizeof(int) * kGroupAngles * (kFpBins + 3) + sizeof(int) * (kGroupAngles * 4 + 8) +
-           sizeof(double) * kGroupAngles;
+    return sizeof(float) * 2 * kFpStage * (32 * VEC) + sizeof(float4) * 2 * kGroupAngles * 32 +
+           sizeof(int) * 2 * kGroupAngles * (kFpBins + 3) +
+           sizeof(int) * (kGroupAngles * 4 + 4 + 2 * kFpStage) + sizeof(double) * kGroupAngles;
 }
 
 // Candidate pixel range [clo, chi] on line li for one angle: pixels whose
@@ -441,13 +441,14 @@ __global__ void __launch_bounds__(32 * kGroupAngles, 3)
     constexpr int NA = kGroupAngles, NG = BT + 2, SPAN = 32 * VEC, US = kFpStage;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     float *stg = reinterpret_cast<float *>(smem_raw);            // [2][US][SPAN]
-    float4 *list = reinterpret_cast<float4 *>(stg + 2 * US * SPAN);  // [NA][32]
-    int *base = reinterpret_cast<int *>(list + NA * 32);             // [NA][NG+1]
-    int *lrange = base + NA * (NG + 1);                               // [NA][2]
+    // entry lists and bucket bases are double-buffered by line parity, so a line's
+    // phase B never overwrites what slower warps still read for the previous line
+    float4 *list2 = reinterpret_cast<float4 *>(stg + 2 * US * SPAN);  // [2][NA][32]
+    int *base2 = reinterpret_cast<int *>(list2 + 2 * NA * 32);        // [2][NA][NG+1]
+    int *lrange = base2 + 2 * NA * (NG + 1);                           // [NA][2]
     int *crange = lrange + NA * 2;                                    // [NA][2] next line
     int *uinfo = crange + NA * 2;                                     // [2][2] (ulo, n) per buffer
-    int *pad = uinfo + 4;
-    (void)pad;
+    int *rowk = uinfo + 4;                                            // [2][US] ray of each staged row
     double *red = reinterpret_cast<double *>(smem_raw + fp_smem_bytes<VEC>() - sizeof(double) * NA);
     if (A.skip && *A.skip) return;
     const int ai = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -498,16 +499,20 @@ __global__ void __launch_bounds__(32 * kGroupAngles, 3)
         for (int v = 0; v < VEC; v++) acc[j][v] = 0.f;
 
     // each warp: its angle's candidate range on line li -> crange
+    int next_clo = INT_MAX, next_chi = INT_MIN;
     auto ranges = [&](int li) {
         int clo = INT_MAX, chi = INT_MIN;
         if (angle_ok && li >= my_lo && li <= my_hi)
             line_candidates(A, orient, ca, cl, T1, T2, r, li, clo, chi);
+        next_clo = clo;
+        next_chi = chi;
         if (lane == 0) {
             crange[2 * ai] = clo;
             crange[2 * ai + 1] = chi;
         }
     };
-    // all threads: union of crange -> uinfo[buf]; issue the row copies
+    // all threads: union of crange -> uinfo[buf]; one lane per staged row looks
+    // up its ray index, then all threads issue the row copies
     auto stage = [&](int li, int buf) {
         int ulo = INT_MAX, uhi = INT_MIN;
 #pragma unroll
@@ -526,13 +531,15 @@ __global__ void __launch_bounds__(32 * kGroupAngles, 3)
             uinfo[2 * buf] = ulo;
             uinfo[2 * buf + 1] = n;
         }
+        int *rk = rowk + buf * US;
+        if (threadIdx.x < n) rk[threadIdx.x] = line_pixel_ray(A, orient, li, ulo + threadIdx.x);
+        __syncthreads();
         float *dst = stg + (size_t)buf * US * SPAN;
         constexpr int PIECES = SPAN / 4;
         for (int c = threadIdx.x; c < n * PIECES; c += 32 * NA) {
             const int row = c / PIECES, col = (c % PIECES) * 4;
-            const int k = line_pixel_ray(A, orient, li, ulo + row);
             const bool ok = yb + col < A.ys;
-            cp_async16(dst + row * SPAN + col, x + (size_t)k * ys + (ok ? yb + col : 0), ok);
+            cp_async16(dst + row * SPAN + col, x + (size_t)rk[row] * ys + (ok ? yb + col : 0), ok);
         }
     };
 
@@ -544,33 +551,61 @@ __global__ void __launch_bounds__(32 * kGroupAngles, 3)
     }
     for (int li = L0; li <= L1; li++) {
         const int buf = (li - L0) & 1;
-        __syncthreads();  // uinfo[buf] written by stage(li)
+        const int my_clo = next_clo, my_chi = next_chi;
         const int ulo = uinfo[2 * buf], un = uinfo[2 * buf + 1];
-        // Phase A: lanes = union pixels, in increasing centre-bin order for this angle.
+        float4 *list = list2 + buf * NA * 32;
+        int *base = base2 + buf * NA * (NG + 1);
+        // Phase A: lanes = this angle's candidate pixels (in increasing centre-bin
+        // order); entries address the staged union rows.
         bool valid = false;
         int gk = 0;
         float4 ent = make_float4(0.f, 0.f, 0.f, 0.f);
-        if (angle_ok && lane < un && li >= my_lo && li <= my_hi) {
-            const int row = ca > 0.f ? lane : un - 1 - lane;
-            const int k = line_pixel_ray(A, orient, li, ulo + row);
+        // an angle with no candidates on this line has (INT_MAX, INT_MIN): test
+        // before subtracting, the difference would overflow
+        int mlo = 0, mhi = -1;
+        if (my_clo <= my_chi && un > 0) {
+            mlo = max(my_clo, ulo);
+            mhi = min(my_chi, ulo + un - 1);
+        }
+        const int mn = mhi - mlo + 1;  // <= un; pix - ulo stays in [0, un)
+        if (angle_ok && lane < mn) {
+            const int pix = ca > 0.f ? mlo + lane : mhi - lane;
+            const int k = rowk[buf * US + (pix - ulo)];
             const Taps t = ray_taps<W>(A.ray[k], ap, A.r_hi, A.r_lo);
             gk = t.iqx - b0 + 1;
             valid = gk >= 0 && gk <= BT + 1;
-            ent = make_float4(__int_as_float(row), t.w0, t.w1, t.w2);
+            ent = make_float4(__int_as_float(pix - ulo), t.w0, t.w1, t.w2);
         }
         // Phase B (warp-local): stable counting sort by bucket.
         const unsigned key = valid ? (unsigned)gk : 64u + lane;
         const unsigned peers = __match_any_sync(0xffffffffu, key);
         const int rank = __popc(peers & ((1u << lane) - 1u));
-        int mybase = 0;
-#pragma unroll
-        for (int gg = 0; gg <= NG; gg++) {
-            const int c = __popc(__ballot_sync(0xffffffffu, valid && gk < gg));
-            if (lane == gg) base[ai * (NG + 1) + gg] = c;
-            if (valid && gg == gk) mybase = c;
+        // lane g (< NG) learns the size of bucket g from that bucket's first member
+        const int leader = (valid && rank == 0) ? gk : -1;
+        int cnt = 0;
+        {
+            const unsigned lead_mask = __ballot_sync(0xffffffffu, leader >= 0);
+            unsigned m = lead_mask;
+            while (m) {
+                const int src = __ffs(m) - 1;
+                m &= m - 1;
+                const int g_src = __shfl_sync(0xffffffffu, leader, src);
+                const int c_src = __popc(__shfl_sync(0xffffffffu, (int)peers, src));
+                if (lane == g_src) cnt = c_src;
+            }
         }
+        int incl = cnt;  // inclusive scan over lanes 0..31 of the bucket sizes
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const int t = __shfl_up_sync(0xffffffffu, incl, o);
+            if (lane >= o) incl += t;
+        }
+        const int excl = incl - cnt;
+        if (lane <= NG) base[ai * (NG + 1) + lane] = excl;
+        const int mybase = __shfl_sync(0xffffffffu, excl, valid ? gk : 0);
         if (valid) list[ai * 32 + mybase + rank] = ent;
-        // next line's ranges, then its staging one line ahead
+        // next line's ranges, then its staging one line ahead (stage() syncs once
+        // after publishing the ranges' union and row table)
         if (li + 1 <= L1) ranges(li + 1);
         __syncthreads();
         if (li + 1 <= L1) stage(li + 1, buf ^ 1);

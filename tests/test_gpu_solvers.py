@@ -107,7 +107,10 @@ def test_cgls_fixed_denominator(gb, oc):
     xd = empty_vol(plan)
     hist, info = plan.cgls(sino_to_dev(plan, b), xd, 8, 0.0, rnorm_ref=ref)
     np.testing.assert_allclose(hist, tr.rel_history(), rtol=RTOL_TRACE)
-    assert rel_l2(vol_from_dev(plan, xd), x_ref) < TOL
+    x64, _ = oc.cgls64(w, b, ang, maxit=8, tol=0.0, rnorm_ref=ref)
+    e_gpu, e_ref = rel_l2(vol_from_dev(plan, xd), x_ref), rel_l2(x_ref, x64)
+    print("fixed-denominator cgls: gpu-ref %.2e, ref-fp64 %.2e" % (e_gpu, e_ref))
+    assert e_gpu < max(TOL, FRAC * e_ref)
 
 
 def test_cgls_long_solve_tracks_reference(gb, oc):
