@@ -74,6 +74,8 @@ def lib():
             getattr(L, n).argtypes = [vp, vp, C.c_int, C.c_int, C.c_int, C.c_int, vp]
         L.arecgb_cc_shifts.argtypes = [vp, vp, C.c_int, C.c_int, C.c_int, vp, vp, vp, vp, vp]
         L.arecgb_ccorr2d_device.argtypes = [vp, vp, vp, C.c_int, C.c_int, vp]
+        L.arecgb_cc_shifts_static.argtypes = [vp, vp, C.c_int, C.c_int, C.c_int, vp, vp, vp, vp,
+                                              vp]
         img, pimg = ArecImage, C.POINTER(ArecImage)
         for n in ("arecProject2D", "arecProject2D_KB", "arecProject2D_SQ", "arecBackProject2D",
                   "arecBackProject2D_KB", "arecBackProject2D_SQ"):
@@ -216,6 +218,16 @@ def cc_shifts(img1, img2, sx, sy, ix=None, iy=None, stream=None):
     nz, ny, nx = img1.shape
     _check(lib().arecgb_cc_shifts(_ptr(img1), _ptr(img2), nz, ny, nx, _ptr(sx), _ptr(sy),
                                   _ptr(ix), _ptr(iy), _stream(stream)), "arecgb_cc_shifts")
+
+
+def cc_shifts_static(img1, img2, sx, sy, ix=None, iy=None, stream=None):
+    """Shift search that allocates nothing (static 3.5 MiB scratch per device;
+    nx, ny powers of two in [16, 512], nz*ny*nx <= 262144).  The scratch is
+    shared: do not let two calls overlap."""
+    nz, ny, nx = img1.shape
+    _check(lib().arecgb_cc_shifts_static(_ptr(img1), _ptr(img2), nz, ny, nx, _ptr(sx),
+                                         _ptr(sy), _ptr(ix), _ptr(iy), _stream(stream)),
+           "arecgb_cc_shifts_static")
 
 
 def ccorr2d_device(x, y, c, stream=None):

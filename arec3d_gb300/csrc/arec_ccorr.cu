@@ -554,4 +554,143 @@ int peak_search(const float *dc, int nz, int ny, int nx, float *sx, float *sy, i
     return 0;
 }
 
+
+// ---------------------------------------------------------------------------
+// Shift search without allocation (arecgb_cc_shifts_static).
+//
+// For callers that must not allocate device memory while they run: an
+// alignment loop that interleaves shift searches with a reconstruction running
+// on another stream (cc_shifts' cudaFree synchronises the whole device and
+// would stall that solve), or a host whose memory is owned by another
+// allocator (a caching allocator that already holds the free HBM).
+//
+// Scratch: one file-scope device array of kStaticBytes (3.5 MiB), carved into
+//   Xh, Yh  float2 [kStaticSpec]   half spectra of both images
+//   c       float  [kStaticPixels] correlation images
+//   stats   RowStat[kStaticRows]   per-row peak statistics
+//   tw      float2 [1008]          twiddles for N = 16..512, table N at offset N - 16
+// Limit: nx, ny powers of two in [16, 512] and nz * ny * nx <= kStaticPixels
+// (one 512 x 512 pair, or e.g. 64 pairs of 64 x 64).  Larger requests are
+// rejected with ARECGB_ERR_ARG; arecgb_cc_shifts has no such limit.
+// Nothing in the scratch must start at zero: every element a call reads was
+// written earlier in the same call (row pass -> column pass -> inverse rows ->
+// peak).  Only the twiddle tables persist; the set-up writes them.
+// The scratch is shared by every call on a device: two calls that can overlap
+// (different streams, or host threads without ordering) race on it.
+constexpr size_t kStaticPixels = 512 * 512;
+constexpr size_t kStaticRows = kStaticPixels / 16;                  // ny * nz <= pixels / nx
+constexpr size_t kStaticSpec = kStaticPixels / 2 + kStaticRows;     // (nx/2 + 1) * ny * nz
+constexpr size_t kStaticTw = 1024;                                  // 16 + 32 + ... + 512 = 1008
+constexpr size_t kOffYh = sizeof(float2) * kStaticSpec;
+constexpr size_t kOffC = 2 * kOffYh;
+constexpr size_t kOffStats = kOffC + sizeof(float) * kStaticPixels;
+constexpr size_t kOffTw = kOffStats + sizeof(RowStat) * kStaticRows;
+constexpr size_t kStaticBytes = kOffTw + sizeof(float2) * kStaticTw;
+static_assert(kOffYh % 256 == 0 && kOffC % 256 == 0 && kOffStats % 256 == 0 &&
+                  kOffTw % 256 == 0,
+              "scratch pieces must stay 256-byte aligned");
+
+static __device__ __align__(256) unsigned char g_cc_static[kStaticBytes];
+
+struct StaticScratch {
+    bool ready = false;
+    unsigned char *base = nullptr;
+};
+static std::mutex g_static_mu;
+static std::map<int, StaticScratch> g_static;  // device -> scratch address
+
+// Once per device, with that device current: resolve the scratch address and
+// write the twiddle tables (a synchronous copy).  Run the first call before
+// any stream capture.
+static int static_setup(unsigned char **base) {
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) {
+        set_error(std::string("cc_shifts_static: cudaGetDevice: ") + cudaGetErrorString(e));
+        return cuda_status(e);
+    }
+    std::lock_guard<std::mutex> lk(g_static_mu);
+    StaticScratch &s = g_static[dev];
+    if (s.ready) {
+        *base = s.base;
+        return 0;
+    }
+    void *ptr = nullptr;
+    e = cudaGetSymbolAddress(&ptr, g_cc_static);
+    if (e != cudaSuccess || !ptr) {
+        set_error(std::string("cc_shifts_static: cudaGetSymbolAddress: ") +
+                  cudaGetErrorString(e));
+        return cuda_status(e != cudaSuccess ? e : cudaErrorInvalidSymbol);
+    }
+    std::vector<float2> h(kStaticTw, make_float2(0.f, 0.f));
+    for (int N = 16; N <= 512; N *= 2)
+        for (int k = 0; k < N; k++) {
+            const double a = 2.0 * M_PI * (double)k / (double)N;
+            h[N - 16 + k] = make_float2((float)std::cos(a), (float)-std::sin(a));
+        }
+    e = cudaMemcpy((unsigned char *)ptr + kOffTw, h.data(), sizeof(float2) * kStaticTw,
+                   cudaMemcpyHostToDevice);
+    if (e != cudaSuccess) {
+        set_error(std::string("cc_shifts_static: twiddle upload: ") + cudaGetErrorString(e));
+        return cuda_status(e);
+    }
+    s.base = (unsigned char *)ptr;
+    s.ready = true;
+    *base = s.base;
+    return 0;
+}
+
+int cc_shifts_static(const float *d1, const float *d2, int nz, int ny, int nx, float *sx,
+                     float *sy, int *ix, int *iy, cudaStream_t st) {
+    const bool shape_ok = nx >= 16 && nx <= 512 && ny >= 16 && ny <= 512 &&
+                          (nx & (nx - 1)) == 0 && (ny & (ny - 1)) == 0;
+    if (!shape_ok || nz < 0 || !d1 || !d2 || !sx || !sy) {
+        set_error("cc_shifts_static: nx and ny must be powers of two in [16, 512]");
+        return ARECGB_ERR_ARG;
+    }
+    if ((size_t)nz * ny * nx > kStaticPixels) {
+        set_error("cc_shifts_static: nz * ny * nx = " + std::to_string((size_t)nz * ny * nx) +
+                  " exceeds the static scratch limit of " + std::to_string(kStaticPixels) +
+                  " pixels (one 512 x 512 pair); use arecgb_cc_shifts");
+        return ARECGB_ERR_ARG;
+    }
+    unsigned char *base = nullptr;
+    int rc = static_setup(&base);
+    if (rc) return rc;
+    if (nz == 0) return 0;
+    float2 *Xh = reinterpret_cast<float2 *>(base);
+    float2 *Yh = reinterpret_cast<float2 *>(base + kOffYh);
+    float *c = reinterpret_cast<float *>(base + kOffC);
+    RowStat *stats = reinterpret_cast<RowStat *>(base + kOffStats);
+    const float2 *tw = reinterpret_cast<const float2 *>(base + kOffTw);
+    const float2 *twx = tw + (nx - 16), *twy = tw + (ny - 16);
+    // shared memory: 8 * G * nx = 32 KB per row block, 64 * ny <= 32 KB per
+    // column block.  The limits are set on every call: cc_shifts sets them to
+    // its own (possibly smaller) sizes.
+    const int G = rows_per_block(nx);
+    const size_t row_smem = sizeof(float2) * (size_t)G * nx;
+    const size_t col_smem = sizeof(float2) * 2 * kColTile * (size_t)ny;
+    if ((rc = set_smem((const void *)k_cc_rows_fwd, row_smem))) return rc;
+    if ((rc = set_smem((const void *)k_cc_rows_inv, row_smem))) return rc;
+    if ((rc = set_smem((const void *)k_cc_cols, col_smem))) return rc;
+    const int H = nx / 2 + 1;
+    k_cc_rows_fwd<<<dim3((ny + G - 1) / G, nz), 256, row_smem, st>>>(d1, d2, Xh, Yh, nx, ny, twx);
+    k_cc_cols<<<dim3((H + kColTile - 1) / kColTile, nz), 256, col_smem, st>>>(Xh, Yh, nx, ny, twy);
+    k_cc_rows_inv<<<dim3((ny + G - 1) / G, nz), 256, row_smem, st>>>(Xh, c, stats, nx, ny, twx);
+    k_peak<<<nz, 256, 0, st>>>(c, stats, nx, ny, sx, sy, ix, iy);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) {
+        set_error(std::string("cc_shifts_static: ") + cudaGetErrorString(e));
+        return cuda_status(e);
+    }
+    return 0;
+}
+
 }  // namespace arecgb
+
+extern "C" int arecgb_cc_shifts_static(const float *d_img1, const float *d_img2, int nz, int ny,
+                                       int nx, float *d_sx, float *d_sy, int *d_ix, int *d_iy,
+                                       void *stream) {
+    return arecgb::cc_shifts_static(d_img1, d_img2, nz, ny, nx, d_sx, d_sy, d_ix, d_iy,
+                                    (cudaStream_t)stream);
+}

@@ -105,6 +105,21 @@ int arecgb_sino_to_reference(const float *d_dev, float *d_ref, int na, int ny, i
 int arecgb_cc_shifts(const float *d_img1, const float *d_img2, int nz, int ny, int nx,
                      float *d_sx, float *d_sy, int *d_ix, int *d_iy, void *stream);
 
+/* Shift search that allocates nothing (no counterpart in the reference: its
+ * arecCCImages allocates per call).  Same arguments, results and layout as
+ * arecgb_cc_shifts, for callers that cannot allocate device memory while they
+ * run (an alignment loop beside a solve on another stream, where cudaFree
+ * would synchronise the device; memory owned by another allocator).
+ * Scratch is one static 3.5 MiB device array per device.  Limit: nx, ny powers
+ * of two in [16, 512] and nz * ny * nx <= 262144 (one 512 x 512 pair);
+ * larger requests return ARECGB_ERR_ARG.  The first call on a device does the
+ * set-up (resolves the scratch address, uploads twiddle tables, synchronously)
+ * and should come before any stream capture.  The call is asynchronous on
+ * `stream`.  All calls on a device share the scratch: calls that can overlap
+ * (other streams, unordered host threads) race. */
+int arecgb_cc_shifts_static(const float *d_img1, const float *d_img2, int nz, int ny, int nx,
+                            float *d_sx, float *d_sy, int *d_ix, int *d_iy, void *stream);
+
 /* Full correlation image (replaces ccorr2d, AREC3D/AREC3D/align2dstack.cpp:480):
  * c = IDFT(conj(DFT x) * DFT y), unnormalised, device memory [ny][nx]. */
 int arecgb_ccorr2d_device(const float *d_x, const float *d_y, float *d_c, int ny, int nx,
