@@ -103,6 +103,22 @@ def lib():
         L.arecgb_soft_noneg.argtypes = [pimg]
         L.arecgb_soft_noneg.restype = None
         L.arecgb_last_trace.argtypes = [dp, C.c_int, C.POINTER(SolveInfo)]
+        L.arecgb_conv3x3_bf16.argtypes = [vp] * 4 + [C.c_int] * 7 + [vp, vp]
+        L.arecgb_unet_create.argtypes = [C.POINTER(vp), C.c_int, C.c_int, C.c_int, C.c_int,
+                                         C.c_ulonglong]
+        L.arecgb_unet_destroy.argtypes = [vp]
+        L.arecgb_unet_num_params.argtypes = [vp]
+        L.arecgb_unet_num_params.restype = C.c_longlong
+        lp = C.POINTER(C.c_longlong)
+        L.arecgb_unet_layer_offsets.argtypes = [vp, lp, lp, ip, ip]
+        L.arecgb_unet_get_params.argtypes = [vp, vp, vp]
+        L.arecgb_unet_set_params.argtypes = [vp, vp, vp]
+        L.arecgb_unet_forward.argtypes = [vp, vp, vp, C.c_int, vp]
+        L.arecgb_unet_backward.argtypes = [vp, vp, vp, vp]
+        L.arecgb_unet_train_step.argtypes = [vp, vp, vp, C.c_int, C.c_float, C.c_float, dp, vp]
+        for n in ("arecgb_unet_images_from_volume", "arecgb_unet_images_to_volume"):
+            getattr(L, n).argtypes = [vp, vp, vp, C.c_int, C.c_int, C.c_int, C.c_float, vp]
+        L.arecgb_warm_start.argtypes = [vp, vp, vp, vp, vp, vp, vp]
         _lib = L
     return _lib
 
@@ -211,6 +227,72 @@ class Plan:
         _check(lib().arecgb_sino_to_reference(_ptr(dev), _ptr(ref), self.nangles, self.ny,
                                               self.nx, self.ys, _stream(stream)),
                "arecgb_sino_to_reference")
+
+
+class UNet:
+    """Learned warm start network (BF16 4-level U-Net, 32 base channels) on
+    square images [n][size][size] (size a multiple of 8)."""
+
+    LAYERS = ("c1a", "c1b", "c2a", "c2b", "c3a", "c3b", "c4a", "c4b", "u3", "d3a", "d3b",
+              "u2", "d2a", "d2b", "u1", "d1a", "d1b", "out")
+
+    def __init__(self, size, max_batch, train=False, seed=0):
+        h = C.c_void_p()
+        _check(lib().arecgb_unet_create(C.byref(h), size, size, max_batch, int(train), seed),
+               "arecgb_unet_create")
+        self._h, self.size, self.max_batch, self.train = h, size, max_batch, train
+        self.nparams = int(lib().arecgb_unet_num_params(h))
+        n = len(self.LAYERS)
+        wo, bo = (C.c_longlong * n)(), (C.c_longlong * n)()
+        ci, co = (C.c_int * n)(), (C.c_int * n)()
+        lib().arecgb_unet_layer_offsets(h, wo, bo, ci, co)
+        self.layers = [dict(name=self.LAYERS[i], w_off=wo[i], b_off=bo[i], cin=ci[i],
+                            cout=co[i]) for i in range(n)]
+
+    def __del__(self):
+        h = getattr(self, "_h", None)
+        if h:
+            lib().arecgb_unet_destroy(h)
+            self._h = None
+
+    def get_params(self, out, stream=None):
+        _check(lib().arecgb_unet_get_params(self._h, _ptr(out), _stream(stream)),
+               "arecgb_unet_get_params")
+
+    def set_params(self, params, stream=None):
+        _check(lib().arecgb_unet_set_params(self._h, _ptr(params), _stream(stream)),
+               "arecgb_unet_set_params")
+
+    def forward(self, x, y, stream=None):
+        _check(lib().arecgb_unet_forward(self._h, _ptr(x), _ptr(y), x.shape[0], _stream(stream)),
+               "arecgb_unet_forward")
+
+    def backward(self, dout, grads=None, stream=None):
+        _check(lib().arecgb_unet_backward(self._h, _ptr(dout), _ptr(grads), _stream(stream)),
+               "arecgb_unet_backward")
+
+    def train_step(self, x, target, lr, weight_decay=0.0, stream=None):
+        loss = C.c_double()
+        _check(lib().arecgb_unet_train_step(self._h, _ptr(x), _ptr(target), x.shape[0], lr,
+                                            weight_decay, C.byref(loss), _stream(stream)),
+               "arecgb_unet_train_step")
+        return loss.value
+
+    def warm_start(self, plan, x_early, x0, img_in, img_out, stream=None):
+        _check(lib().arecgb_warm_start(plan._h, _ptr(x_early), _ptr(x0), _ptr(img_in),
+                                       _ptr(img_out), _stream(stream)), "arecgb_warm_start")
+
+
+def images_from_volume(plan, vol, img, npad, y0, count, scale=1.0, stream=None):
+    _check(lib().arecgb_unet_images_from_volume(plan._h, _ptr(vol), _ptr(img), npad, y0, count,
+                                                scale, _stream(stream)),
+           "arecgb_unet_images_from_volume")
+
+
+def images_to_volume(plan, img, vol, npad, y0, count, scale=1.0, stream=None):
+    _check(lib().arecgb_unet_images_to_volume(plan._h, _ptr(img), _ptr(vol), npad, y0, count,
+                                              scale, _stream(stream)),
+           "arecgb_unet_images_to_volume")
 
 
 def cc_shifts(img1, img2, sx, sy, ix=None, iy=None, stream=None):

@@ -509,7 +509,7 @@ int sirt(Plan *p, const float *d_b, float *d_x, float lam, int maxit, float tol,
         set_error("sirt: pinned allocation failed");
         return ARECGB_ERR_NOMEM;
     }
-    double relnrm0 = 1.00001, bnorm2 = 0.0, bnorm = 0.0;
+    double relnrm0 = 1.00001, bnorm2 = 0.0, bnorm = 0.0, atb_norm = 0.0, rel_last = 0.0;
     int restarts = 0, iter = 1, count = 0;
     const int nblk = std::min(kRedBlocks, grid_for(nv, 8));
     cudaMemsetAsync(d_x, 0, sizeof(float) * nv, st);
@@ -540,12 +540,14 @@ int sirt(Plan *p, const float *d_b, float *d_x, float lam, int maxit, float tol,
             break;
         }
         if (iter == 1) {
+            if (restarts == 0) atb_norm = std::sqrt(h_red[0]);
             bnorm2 += h_red[0];
             bnorm = std::sqrt(bnorm2);
         }
         rn2 = h_red[1];
         const double rnorm = std::sqrt(rn2);
         const double relnrm = rnorm / bnorm;
+        rel_last = relnrm;
         if (hist_host && count < maxit) hist_host[count] = relnrm;
         count++;
         if (verbose)
@@ -588,8 +590,8 @@ int sirt(Plan *p, const float *d_b, float *d_x, float lam, int maxit, float tol,
         info->restarts = restarts;
         info->status = 0;
         info->lam_final = lam;
-        info->rnorm0 = 0.0;
-        info->rel_final = 0.0;
+        info->rnorm0 = atb_norm;  // ||A^T b||: the CGLS denominator for a warm start
+        info->rel_final = rel_last;
     }
     cudaFree(red);
     cudaFreeHost(h_red);

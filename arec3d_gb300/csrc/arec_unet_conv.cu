@@ -1,0 +1,206 @@
+// 3x3 convolution (stride 1, zero padding 1) as an implicit GEMM on the
+// 5th-generation tensor cores: tcgen05.mma (BF16 x BF16 -> FP32 in TMEM).
+//
+//   Y[p][co] = act( bias[co] + sum_{tap, ci} X[p + tap][ci] * Wt[co][tap][ci] )
+//
+// X, Y: NHWC bf16 ([P = n*H*W pixels][C]); Wt: [Cout][9][Cin] bf16.
+// A block owns 128 consecutive pixels (GEMM M = 128) and all Cout output
+// channels (GEMM N = Cout in {32, 64, 128, 256}); K = 9*Cin runs in chunks of
+// 32 channels of one tap.  Per chunk, 128 threads gather the A slab (the 128
+// pixels' shifted neighbours, zeros outside the image) and the B slab (weights)
+// into shared memory in the tensor core's K-major layout; one thread issues two
+// tcgen05.mma (K = 16 each) into the TMEM accumulator and commits them to the
+// stage's mbarrier, so the next chunk's gather overlaps the MMAs (two stages).
+// The epilogue reads TMEM with tcgen05.ld (warp w: pixels 32w..32w+31), adds
+// the bias, applies ReLU and stores bf16.
+//
+// The same kernel computes the data gradient of a convolution from the
+// spatially flipped, channel-transposed weights.
+#include <cuda_bf16.h>
+#include <stdint.h>
+
+#include "arec_internal.cuh"
+#include "arec_umma.cuh"
+
+namespace arecgb {
+
+constexpr int kConvKC = 32;          // input channels per K chunk
+constexpr uint32_t kWaitLimit = 4u << 20;
+
+template <int COUT>
+struct ConvCfg {
+    static constexpr int A_BYTES = 128 * kConvKC * 2;  // 8 KB
+    static constexpr int B_BYTES = COUT * kConvKC * 2;
+    static constexpr int STAGE = A_BYTES + B_BYTES;
+    static constexpr int SMEM = 2 * STAGE;
+    static constexpr uint32_t NCOLS = COUT < 32 ? 32 : COUT;
+};
+
+// byte offset of element (row, k) (k < 32) in a K-major no-swizzle slab with
+// `rows` rows: two MMA slabs (K = 16 each) of rows/8 core-matrix groups.
+__device__ __forceinline__ int kmaj_offset(int row, int kpiece /*0..3, 8 elements*/, int rows) {
+    const int s = kpiece >> 1, j = kpiece & 1;
+    return s * (rows / 8) * 256 + (row >> 3) * 256 + j * 128 + (row & 7) * 16;
+}
+
+template <int COUT, int LBO, int SBO>
+__global__ void __launch_bounds__(128)
+    conv3x3_umma_kernel(const __nv_bfloat16 *__restrict__ X, const __nv_bfloat16 *__restrict__ Wt,
+                        const float *__restrict__ bias, __nv_bfloat16 *__restrict__ Y, int H,
+                        int Wd, int Cin, int P, int relu, int ystride, int *err) {
+    using Cfg = ConvCfg<COUT>;
+    extern __shared__ __align__(1024) unsigned char sm[];
+    __shared__ uint64_t mbar[2];
+    __shared__ uint32_t tmem_base;
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    const int p0 = blockIdx.x * 128;
+
+    if (warp == 0) {
+        umma::tmem_alloc(&tmem_base, Cfg::NCOLS);
+        umma::tmem_relinquish();
+    }
+    if (tid == 0) {
+        umma::mbar_init(&mbar[0], 1);
+        umma::mbar_init(&mbar[1], 1);
+        umma::mbar_fence_init();
+    }
+    umma::fence_before_sync();
+    __syncthreads();
+    umma::fence_after_sync();
+    const uint32_t tmem = tmem_base;
+
+    // this thread's pixel (row of A)
+    const int p = p0 + tid;
+    const bool pvalid = p < P;
+    const int hw = H * Wd;
+    const int n = p / hw, h = (p / Wd) % H, w = p % Wd;
+    const int cchunks = Cin / kConvKC;
+    const int nchunks = 9 * cchunks;
+    constexpr uint32_t idesc = umma::idesc_bf16(128, COUT);
+    bool ok = true;
+
+    for (int c = 0; c < nchunks; c++) {
+        const int st = c & 1;
+        if (c >= 2 && ok) {
+            if (!umma::mbar_wait(&mbar[st], ((c - 2) >> 1) & 1, kWaitLimit)) ok = false;
+        }
+        unsigned char *A = sm + st * Cfg::STAGE;
+        unsigned char *B = A + Cfg::A_BYTES;
+        const int tap = c / cchunks, c0 = (c % cchunks) * kConvKC;
+        const int dy = tap / 3 - 1, dx = tap % 3 - 1;
+        // A: pixel tid, its neighbour at (dy, dx), channels c0..c0+31 (4 x 16 B)
+        {
+            const int hh = h + dy, ww = w + dx;
+            const bool inside = pvalid && hh >= 0 && hh < H && ww >= 0 && ww < Wd;
+            const uint4 *src = reinterpret_cast<const uint4 *>(
+                X + ((size_t)n * hw + (size_t)(inside ? hh : 0) * Wd + (inside ? ww : 0)) * Cin + c0);
+#pragma unroll
+            for (int q = 0; q < 4; q++) {
+                uint4 v = inside ? __ldg(src + q) : make_uint4(0, 0, 0, 0);
+                *reinterpret_cast<uint4 *>(A + kmaj_offset(tid, q, 128)) = v;
+            }
+        }
+        // B: weights Wt[co][tap][c0..c0+31]
+        for (int i = tid; i < COUT * 4; i += 128) {
+            const int co = i >> 2, q = i & 3;
+            const uint4 v = __ldg(reinterpret_cast<const uint4 *>(
+                Wt + ((size_t)co * 9 + tap) * Cin + c0 + q * 8));
+            *reinterpret_cast<uint4 *>(B + kmaj_offset(co, q, COUT)) = v;
+        }
+        umma::fence_async_smem();
+        umma::fence_before_sync();
+        __syncthreads();
+        umma::fence_after_sync();
+        if (tid == 0 && ok) {
+#pragma unroll
+            for (int s = 0; s < 2; s++) {
+                const uint64_t ad = umma::smem_desc(umma::smem_addr(A + s * (128 / 8) * 256), LBO, SBO);
+                const uint64_t bd =
+                    umma::smem_desc(umma::smem_addr(B + s * (COUT / 8) * 256), LBO, SBO);
+                umma::mma_bf16(tmem, ad, bd, idesc, (c > 0 || s > 0) ? 1u : 0u);
+            }
+            umma::mma_commit(&mbar[st]);
+        }
+    }
+    // all MMAs done (the last commit covers every earlier MMA of the issuing thread)
+    if (nchunks > 0 && ok) {
+        const int last = nchunks - 1;
+        if (!umma::mbar_wait(&mbar[last & 1], (last >> 1) & 1, kWaitLimit)) ok = false;
+    }
+    if (!ok && lane == 0) atomicOr(err, 4);
+    umma::fence_after_sync();
+
+    // epilogue: warp w reads TMEM lanes 32w.. (pixels p0 + 32w + lane)
+    if (ok) {
+#pragma unroll 1
+        for (int cc = 0; cc < COUT / 32; cc++) {
+            float v[32];
+            umma::tmem_ld32(tmem + ((uint32_t)(32 * warp) << 16) + (uint32_t)(cc * 32), v);
+            if (pvalid) {
+                __align__(16) __nv_bfloat16 out[32];
+#pragma unroll
+                for (int i = 0; i < 32; i++) {
+                    float t = v[i] + (bias ? bias[cc * 32 + i] : 0.f);
+                    if (relu) t = fmaxf(t, 0.f);
+                    out[i] = __float2bfloat16(t);
+                }
+                uint4 *dst = reinterpret_cast<uint4 *>(Y + (size_t)p * ystride + cc * 32);
+#pragma unroll
+                for (int q = 0; q < 4; q++) dst[q] = reinterpret_cast<const uint4 *>(out)[q];
+            }
+        }
+    }
+    umma::fence_before_sync();
+    __syncthreads();
+    if (warp == 0) umma::tmem_dealloc(tmem, Cfg::NCOLS);
+}
+
+template <int COUT, int LBO, int SBO>
+static int launch_conv(const __nv_bfloat16 *X, const __nv_bfloat16 *Wt, const float *bias,
+                       __nv_bfloat16 *Y, int H, int Wd, int Cin, int P, int relu, int ystride,
+                       int *err, cudaStream_t st) {
+    using Cfg = ConvCfg<COUT>;
+    static bool configured = false;
+    if (!configured) {
+        ARECGB_CUDA(cudaFuncSetAttribute(conv3x3_umma_kernel<COUT, LBO, SBO>,
+                                         cudaFuncAttributeMaxDynamicSharedMemorySize, Cfg::SMEM));
+        configured = true;
+    }
+    conv3x3_umma_kernel<COUT, LBO, SBO><<<(P + 127) / 128, 128, Cfg::SMEM, st>>>(
+        X, Wt, bias, Y, H, Wd, Cin, P, relu, ystride, err);
+    ARECGB_CUDA(cudaGetLastError());
+    return 0;
+}
+
+// layout: 0 = (LBO 128, SBO 256) [K-halves 128 B apart, row groups 256 B apart],
+//         1 = the two offsets exchanged (for validating the descriptor fields).
+int conv3x3_bf16(const void *X, const void *Wt, const float *bias, void *Y, int N, int H, int Wd,
+                 int Cin, int Cout, int relu, int layout, int *err, cudaStream_t st, int ystride) {
+    if (ystride <= 0) ystride = Cout;
+    if (Cin % kConvKC || Cin < kConvKC || N < 1 || H < 1 || Wd < 1 || ystride < Cout ||
+        ystride % 8) {
+        set_error("conv3x3: Cin must be a positive multiple of 32");
+        return ARECGB_ERR_ARG;
+    }
+    const auto *x = reinterpret_cast<const __nv_bfloat16 *>(X);
+    const auto *w = reinterpret_cast<const __nv_bfloat16 *>(Wt);
+    auto *y = reinterpret_cast<__nv_bfloat16 *>(Y);
+    const int P = N * H * Wd;
+#define ARECGB_CONV(C)                                                                     \
+    if (Cout == C)                                                                         \
+        return layout ? launch_conv<C, 256, 128>(x, w, bias, y, H, Wd, Cin, P, relu, ystride, err, st) \
+                      : launch_conv<C, 128, 256>(x, w, bias, y, H, Wd, Cin, P, relu, ystride, err, st);
+    ARECGB_CONV(32) ARECGB_CONV(64) ARECGB_CONV(128) ARECGB_CONV(256)
+#undef ARECGB_CONV
+    set_error("conv3x3: Cout must be 32, 64, 128 or 256");
+    return ARECGB_ERR_ARG;
+}
+
+}  // namespace arecgb
+
+extern "C" int arecgb_conv3x3_bf16(const void *X, const void *Wt, const float *bias, void *Y, int N,
+                                   int H, int W, int Cin, int Cout, int relu, int layout, int *err,
+                                   void *stream) {
+    return arecgb::conv3x3_bf16(X, Wt, bias, Y, N, H, W, Cin, Cout, relu, layout, err,
+                                (cudaStream_t)stream, Cout);
+}

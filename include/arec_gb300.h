@@ -47,7 +47,7 @@ typedef struct {
     int restarts;   /* SIRT step-size restarts (arecsirt.cpp:318-338) */
     int status;     /* reference-style status of the solve */
     float lam_final;
-    double rnorm0;    /* initial residual norm */
+    double rnorm0;    /* initial residual norm (SIRT: ||A^T b||) */
     double rel_final; /* last relative residual */
 } arecgb_solve_info;
 
@@ -124,6 +124,61 @@ int arecgb_cc_shifts_static(const float *d_img1, const float *d_img2, int nz, in
  * c = IDFT(conj(DFT x) * DFT y), unnormalised, device memory [ny][nx]. */
 int arecgb_ccorr2d_device(const float *d_x, const float *d_y, float *d_c, int ny, int nx,
                           void *stream);
+
+/* ---- Learned warm start (no counterpart in the reference) -------------------
+ * A BF16 4-level U-Net (32 base channels, FP32 accumulation and master
+ * weights) over square images of height x width (multiples of 8), NHWC with
+ * one channel: image stacks are [n][height][width] floats, device memory.
+ * Parameters are one flat FP32 vector; per layer the weights [Cout][9][Cin]
+ * then the biases (arecgb_unet_layer_offsets gives the 18 layers' offsets and
+ * channel counts in network order: c1a c1b c2a c2b c3a c3b c4a c4b u3 d3a d3b
+ * u2 d2a d2b u1 d1a d1b out).  train != 0 allocates gradients, AdamW moments
+ * and backward scratch. */
+typedef struct arecgb_unet arecgb_unet;
+
+/* The network's tensor-core building block, exposed for testing:
+ * Y[p][co] = act(bias[co] + sum_{tap,ci} X[p+tap][ci] * Wt[co][tap][ci]),
+ * 3x3, zero padding, X [n][H][W][Cin] and Y [n][H][W][Cout] bf16 (raw 16-bit),
+ * Wt [Cout][9][Cin] bf16, bias FP32 (optional); Cin a multiple of 32, Cout in
+ * {32, 64, 128, 256}; relu != 0 applies ReLU; layout must be 0 (1 exchanges
+ * the descriptor's two byte offsets, a wrong layout kept to validate them);
+ * *d_err (device int) gets bit 4 if a tensor-core wait timed out. */
+int arecgb_conv3x3_bf16(const void *d_x, const void *d_wt, const float *d_bias, void *d_y, int n,
+                        int height, int width, int cin, int cout, int relu, int layout,
+                        int *d_err, void *stream);
+
+int arecgb_unet_create(arecgb_unet **net, int height, int width, int max_batch, int train,
+                       unsigned long long seed);
+int arecgb_unet_destroy(arecgb_unet *net);
+long long arecgb_unet_num_params(const arecgb_unet *net);
+/* fills up to 18 entries of each (any may be NULL); returns the layer count */
+int arecgb_unet_layer_offsets(const arecgb_unet *net, long long *w_off, long long *b_off,
+                              int *cin, int *cout);
+int arecgb_unet_get_params(const arecgb_unet *net, float *d_params, void *stream);
+int arecgb_unet_set_params(arecgb_unet *net, const float *d_params, void *stream);
+/* out = in + net(in); n_images <= max_batch; synchronises the stream */
+int arecgb_unet_forward(arecgb_unet *net, const float *d_in, float *d_out, int n_images,
+                        void *stream);
+/* gradient of a loss with d(loss)/d(out) = d_dout for the last forward's input
+ * (which must still be valid); d_grads (optional) receives the flat gradient */
+int arecgb_unet_backward(arecgb_unet *net, const float *d_dout, float *d_grads, void *stream);
+/* one AdamW step on the mean squared error against d_target; *loss (optional,
+ * synchronises) = that mean before the step */
+int arecgb_unet_train_step(arecgb_unet *net, const float *d_in, const float *d_target,
+                           int n_images, float lr, float weight_decay, double *loss,
+                           void *stream);
+/* cylinder volume (device layout [nrays][ys]) slices y0..y0+count <-> images
+ * [count][npad][npad] (zero outside the disk), values multiplied by scale */
+int arecgb_unet_images_from_volume(const arecgb_plan *plan, const float *d_vol, float *d_img,
+                                   int npad, int y0, int count, float scale, void *stream);
+int arecgb_unet_images_to_volume(const arecgb_plan *plan, const float *d_img, float *d_vol,
+                                 int npad, int y0, int count, float scale, void *stream);
+/* x0 = s * net(x_early / s) for every slice, s = RMS of x_early over the
+ * cylinder; img_in/img_out: scratch of max_batch * height * width floats each;
+ * the net's images must be square with height >= the cylinder's width.
+ * x0 may equal x_early.  Follow with arecgb_cgls(..., warm = 1, ...). */
+int arecgb_warm_start(const arecgb_plan *plan, arecgb_unet *net, const float *d_x_early,
+                      float *d_x0, float *d_img_in, float *d_img_out, void *stream);
 
 #ifdef __cplusplus
 }

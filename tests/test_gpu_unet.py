@@ -1,0 +1,199 @@
+"""U-Net kernels on the GPU against a plain PyTorch fp32 reference of the same
+operation (bf16 inputs, fp32 accumulation; outputs compared after the kernel's
+bf16 rounding)."""
+import ctypes as C
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+BF16_TOL = 1e-2  # relative L2: bf16 output rounding is 2^-8 ~ 4e-3 per element
+
+
+def conv_ref(x, w, b, relu):
+    import torch
+
+    # x: [N,H,W,Cin] bf16, w: [Cout,9,Cin] bf16 -> fp32 reference in NCHW
+    xf = x.float().permute(0, 3, 1, 2)
+    cout, _, cin = w.shape
+    wf = w.float().reshape(cout, 3, 3, cin).permute(0, 3, 1, 2)
+    y = torch.nn.functional.conv2d(xf, wf, b, padding=1)
+    if relu:
+        y = torch.relu(y)
+    return y.permute(0, 2, 3, 1)
+
+
+def run_conv(gb, x, w, b, relu, layout=0):
+    import torch
+
+    n, h, wd, cin = x.shape
+    cout = w.shape[0]
+    y = torch.zeros(n, h, wd, cout, dtype=torch.bfloat16, device="cuda")
+    err = torch.zeros(1, dtype=torch.int32, device="cuda")
+    L = gb.lib()
+    L.arecgb_conv3x3_bf16.argtypes = [C.c_void_p] * 4 + [C.c_int] * 7 + [C.c_void_p, C.c_void_p]
+    rc = L.arecgb_conv3x3_bf16(x.data_ptr(), w.data_ptr(), b.data_ptr() if b is not None else None,
+                               y.data_ptr(), n, h, wd, cin, cout, int(relu), layout,
+                               err.data_ptr(), None)
+    torch.cuda.synchronize()
+    assert rc == 0, gb.last_error()
+    assert int(err.item()) == 0
+    return y
+
+
+@pytest.mark.parametrize("cin,cout,shape", [(32, 32, (1, 16, 16)), (32, 64, (2, 8, 24)),
+                                            (64, 128, (1, 32, 32)), (128, 256, (1, 12, 20)),
+                                            (256, 32, (3, 9, 7))])
+def test_conv3x3_matches_torch(gb, cin, cout, shape):
+    import torch
+
+    torch.manual_seed(cin + cout)
+    n, h, wd = shape
+    x = torch.randn(n, h, wd, cin, device="cuda").bfloat16()
+    w = (torch.randn(cout, 9, cin, device="cuda") / (3 * cin ** 0.5)).bfloat16()
+    b = torch.randn(cout, device="cuda") * 0.1
+    ref = conv_ref(x, w, b, relu=True)
+    errs = {}
+    for layout in (0, 1):
+        y = run_conv(gb, x, w, b, True, layout)
+        errs[layout] = float((y.float() - ref).norm() / ref.norm())
+    print("conv %d->%d %s: rel err layout0 %.2e layout1 %.2e" % (cin, cout, shape, errs[0], errs[1]))
+    assert errs[0] < BF16_TOL
+
+
+# Whole-network forward and gradients against the CPU oracle (oracle/unet_ref.py,
+# FP64 autograd rounding activations and tensor-core weights to bf16 where the
+# GPU stores bf16).
+#
+# Exact case: sparse weights (one +-1 or +-1/2 per output channel), zero
+# biases, small-integer inputs and output gradients keep every activation and
+# gradient exactly representable in bf16 and every sum exact in FP32, so the
+# GPU must match the oracle to EXACT_TOL whatever the summation order: this
+# pins indexing, concatenation, pooling, upsampling and the flipped weights.
+#
+# Random case: He-initialised weights.  Then rounding-boundary flips (FP32 on
+# the GPU vs FP64 in the oracle) propagate through the network: the oracle
+# itself moves by 0.3-0.5% between FP32 and FP64 accumulation.
+# RAND_FWD_TOL / RAND_GRAD_TOL bound that statistical drift.
+EXACT_TOL = 1e-6   # forward: the same bf16 values
+EXACT_GRAD_TOL = 1e-5  # weight gradients: FP32 sums over all pixels, order differs
+RAND_FWD_TOL = 3e-2
+RAND_GRAD_TOL = 0.25
+
+
+def _sparse_params(layers, nparams, rng):
+    """Three nonzero weights per output channel, +-1/2 or +-1/4 (80% positive
+    so activations survive the ReLUs), zero biases, output weights +-1.  The
+    oracle gives identical results in FP32 and FP64 for these (every sum that
+    is rounded to bf16 is exact), yet every layer gets nonzero gradients."""
+    p = np.zeros(nparams)
+    for l in layers:
+        ci, co = l["cin"], l["cout"]
+        if l["name"] == "out":
+            p[l["w_off"]:l["w_off"] + ci] = rng.choice([-1.0, 1.0], size=ci)
+            continue
+        w = np.zeros((co, 9, ci))
+        for _ in range(3):
+            sign = np.where(rng.random(co) < 0.8, 1.0, -1.0)
+            w[np.arange(co), rng.integers(0, 9, co), rng.integers(0, ci, co)] += (
+                sign * rng.choice([0.5, 0.25], size=co))
+        p[l["w_off"]:l["w_off"] + co * 9 * ci] = w.reshape(-1)
+    return p
+
+
+def _random_params(layers, nparams, rng):
+    p = np.zeros(nparams)
+    for l in layers:
+        ci, co = l["cin"], l["cout"]
+        if l["name"] == "out":
+            p[l["w_off"]:l["w_off"] + ci] = 0.3 * rng.standard_normal(ci)
+        else:
+            n = co * 9 * ci
+            p[l["w_off"]:l["w_off"] + n] = rng.standard_normal(n) * np.sqrt(2.0 / (9 * ci))
+        p[l["b_off"]:l["b_off"] + co] = 0.05 * rng.standard_normal(co)
+    return p.astype(np.float32).astype(np.float64)
+
+
+def _compare(gb, size, batch, params, x, dout):
+    import torch
+
+    from oracle import unet_ref
+
+    net = gb.UNet(size, batch, train=True, seed=1)
+    assert (net.layers, net.nparams) == unet_ref.layer_table()
+    net.set_params(torch.from_numpy(params.astype(np.float32)).cuda())
+    xd = torch.from_numpy(x.astype(np.float32)).cuda()
+    yd = torch.zeros_like(xd)
+    net.forward(xd, yd)
+    grads = torch.zeros(net.nparams, device="cuda")
+    net.backward(torch.from_numpy(dout.astype(np.float32)).cuda(), grads)
+    y_ref, g_ref = unet_ref.forward_and_grads(params, net.layers, net.nparams, x, dout)
+    y, g = yd.cpu().numpy(), grads.cpu().numpy()
+    e_fwd = np.linalg.norm(y - y_ref) / max(np.linalg.norm(y_ref - x), 1e-30)
+    errs = {}
+    for l in net.layers:
+        n_w = l["cin"] if l["name"] == "out" else l["cout"] * 9 * l["cin"]
+        for what, off, cnt in (("W", l["w_off"], n_w), ("b", l["b_off"], l["cout"])):
+            a, b = g[off:off + cnt], g_ref[off:off + cnt]
+            nb = np.linalg.norm(b)
+            errs[l["name"] + "." + what] = (np.linalg.norm(a - b) / nb if nb > 0
+                                            else float(np.linalg.norm(a)))
+    return e_fwd, errs
+
+
+@pytest.mark.parametrize("size,batch", [(32, 2), (48, 1)])
+def test_unet_exact_case_matches_oracle(gb, size, batch):
+    from oracle import unet_ref
+
+    layers, n = unet_ref.layer_table()
+    rng = np.random.default_rng(size)
+    params = _sparse_params(layers, n, rng)
+    x = rng.integers(0, 4, (batch, size, size)).astype(np.float64)
+    dout = rng.integers(-1, 2, (batch, size, size)).astype(np.float64)
+    e_fwd, errs = _compare(gb, size, batch, params, x, dout)
+    worst = max(errs.items(), key=lambda kv: kv[1])
+    print("unet exact %dx%d: forward %.1e, worst gradient %s %.1e" % (size, size, e_fwd, *worst))
+    assert e_fwd <= EXACT_TOL
+    assert worst[1] <= EXACT_GRAD_TOL, errs
+
+
+@pytest.mark.parametrize("size,batch", [(32, 2), (48, 1)])
+def test_unet_random_case_near_oracle(gb, size, batch):
+    from oracle import unet_ref
+
+    layers, n = unet_ref.layer_table()
+    rng = np.random.default_rng(size + 7)
+    params = _random_params(layers, n, rng)
+    yy, xx = np.mgrid[0:size, 0:size] / size
+    x = np.stack([np.sin(6 * xx + rng.uniform(0, 6)) * np.cos(5 * yy) +
+                  0.3 * rng.standard_normal((size, size)) for _ in range(batch)])
+    x = x.astype(np.float32).astype(np.float64)
+    dout = rng.standard_normal(x.shape).astype(np.float32).astype(np.float64)
+    e_fwd, errs = _compare(gb, size, batch, params, x, dout)
+    worst = max(errs.items(), key=lambda kv: kv[1])
+    print("unet random %dx%d: forward %.2e, worst gradient %s %.2e, median %.2e" %
+          (size, size, e_fwd, *worst, float(np.median(list(errs.values())))))
+    assert e_fwd < RAND_FWD_TOL
+    assert worst[1] < RAND_GRAD_TOL, errs
+
+
+def _inputs(rng, n, size):
+    yy, xx = np.mgrid[0:size, 0:size] / size
+    x = np.stack([np.sin(6 * xx + rng.uniform(0, 6)) * np.cos(5 * yy) +
+                  0.3 * rng.standard_normal((size, size)) for _ in range(n)])
+    return x.astype(np.float32)
+
+
+def test_unet_train_step_reduces_loss(gb):
+    import torch
+
+    size, batch = 64, 4
+    net = gb.UNet(size, batch, train=True, seed=5)
+    rng = np.random.default_rng(5)
+    x = _inputs(rng, batch, size)
+    target = x + 0.5 * np.roll(x, 1, axis=2)  # a fixed linear map the net can learn
+    xd, td = torch.from_numpy(x).cuda(), torch.from_numpy(target.astype(np.float32)).cuda()
+    losses = [net.train_step(xd, td, 2e-3) for _ in range(60)]
+    print("unet training loss %.4e -> %.4e" % (losses[0], losses[-1]))
+    assert losses[-1] < 0.2 * losses[0]

@@ -167,3 +167,36 @@ print("ok")
 """ % ROOT
     r = subprocess.run([sys.executable, "-c", code], capture_output=True, text=True)
     assert r.returncode == 0 and "ok" in r.stdout, r.stderr[-2000:]
+
+
+def test_unet_oracle_gradients_finite_differences():
+    """The U-Net oracle's autograd gradients (FP64, no bf16 rounding) against
+    central differences on a few parameters of every layer."""
+    pytest.importorskip("torch")
+    from oracle import unet_ref
+
+    layers, n = unet_ref.layer_table()
+    rng = np.random.default_rng(0)
+    p = np.zeros(n)
+    for l in layers:
+        nw = l["cin"] if l["name"] == "out" else l["cout"] * 9 * l["cin"]
+        p[l["w_off"]:l["w_off"] + nw] = rng.standard_normal(nw) * np.sqrt(2.0 / (9 * l["cin"]))
+        p[l["b_off"]:l["b_off"] + l["cout"]] = 0.1 * rng.standard_normal(l["cout"])
+    x = rng.standard_normal((1, 16, 16))
+    dout = rng.standard_normal((1, 16, 16))
+    _, g = unet_ref.forward_and_grads(p, layers, n, x, dout, bf16=False)
+
+    def f(q):
+        import torch
+
+        t = unet_ref.unpack(q, layers)
+        return float((unet_ref.forward(t, torch.as_tensor(x), bf16=False) * torch.as_tensor(dout)).sum())
+
+    h = 1e-6
+    for l in layers:
+        for off in (l["w_off"], l["w_off"] + 5, l["b_off"]):
+            q1, q2 = p.copy(), p.copy()
+            q1[off] += h
+            q2[off] -= h
+            fd = (f(q1) - f(q2)) / (2 * h)
+            assert abs(fd - g[off]) <= 1e-5 * max(1.0, abs(fd)), (l["name"], off, fd, g[off])
