@@ -177,7 +177,13 @@ int plan_create(Plan **out, int weighting, double radius, int ny, int nangles,
         groups.push_back(make_int4(a, n, o, 0));
         a += n;
     }
+    // orientation 0 first (band launches take one orientation at a time)
+    std::stable_sort(groups.begin(), groups.end(),
+                     [](const int4 &a, const int4 &b) { return a.z < b.z; });
     p->ngroups = (int)groups.size();
+    p->ngroups_o[0] = (int)std::count_if(groups.begin(), groups.end(),
+                                         [](const int4 &g) { return g.z == 0; });
+    p->ngroups_o[1] = p->ngroups - p->ngroups_o[0];
 
     // Back-projection tiles of kTileX x kTileZ pixels holding at least one ray.
     std::vector<int2> tiles;

@@ -58,8 +58,10 @@ struct Plan {
     AngleParams *d_ang = nullptr;
     RowInfo *d_rows = nullptr;    // nx rows
     ColInfo *d_cols = nullptr;    // nx columns
-    int4 *d_groups = nullptr;     // forward-projection angle groups: (first, count, orient, 0)
-    int ngroups = 0;
+    int4 *d_groups = nullptr;     // forward-projection angle groups: (first, count, orient, 0),
+    int ngroups = 0;              //   the row-sweeping (orient 0) groups first
+    int ngroups_o[2] = {0, 0};    // groups per orientation
+    int fp_band = 64;             // forward projection: lines per band launch
     int2 *d_tiles = nullptr;      // back-projection ray tiles: (ix0, iz0) of 8x4-pixel tiles
     int ntiles = 0;
     int *d_err = nullptr;         // device error flag (nonzero: a kernel saw an impossible case)

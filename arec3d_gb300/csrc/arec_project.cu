@@ -1,4 +1,6 @@
 // Projector dispatch: launch shapes, weighting selection and the FP64 norm.
+#include <algorithm>
+
 #include "arec_project_impl.cuh"
 
 namespace arecgb {
@@ -6,9 +8,11 @@ namespace arecgb {
 int launch_bp_lin(const OpArgs &, int, int, dim3, const float *, float *, cudaStream_t);
 int launch_bp_kb(const OpArgs &, int, int, dim3, const float *, float *, cudaStream_t);
 int launch_bp_sq(const OpArgs &, int, int, dim3, const float *, float *, cudaStream_t);
-int launch_fp_lin(const OpArgs &, int, int, dim3, const float *, float *, cudaStream_t);
-int launch_fp_kb(const OpArgs &, int, int, dim3, const float *, float *, cudaStream_t);
-int launch_fp_sq(const OpArgs &, int, int, dim3, const float *, float *, cudaStream_t);
+int launch_fp_lin(const OpArgs &, int, const float *, float *, cudaStream_t);
+int launch_fpb_kb(const OpArgs &, int, dim3, const float *, float *, int, int, int, int,
+                  cudaStream_t);
+int launch_fpb_sq(const OpArgs &, int, dim3, const float *, float *, int, int, int, int,
+                  cudaStream_t);
 int sumsq_partials(const float *d_v, size_t n, double *d_partials, int nblocks, cudaStream_t st);
 
 static OpArgs make_args(const Plan *p, const int *skip) {
@@ -40,40 +44,56 @@ static int slice_blocks(const Plan *p) {
     return (p->ys + span - 1) / span;
 }
 
+constexpr int kNormBlocks = 1024;
+
 static int fp_slice_blocks(const Plan *p) { return (p->ys + 32 * p->vec - 1) / (32 * p->vec); }
 
-int fp_grid_blocks(const Plan *p) {
-    if (p->weighting == ARECGB_LIN) return 1024;  // sum-of-squares pass over q
-    const int ntile = (p->nx + kFpBins - 1) / kFpBins;
-    return p->ngroups * ntile * fp_slice_blocks(p);
-}
+// The forward projector's FP64 norm is a separate pass over q (1024 partials).
+int fp_grid_blocks(const Plan *) { return kNormBlocks; }
 
 int bp_grid_blocks(const Plan *p) { return p->ntiles * slice_blocks(p); }
+
+// q = 0 unless the solve has finished (then the call leaves q alone).
+__global__ void __launch_bounds__(256) k_zero_unless(float4 *q, size_t n4, const int *skip) {
+    if (skip && *skip) return;
+    for (size_t i = (size_t)blockIdx.x * 256 + threadIdx.x; i < n4; i += (size_t)gridDim.x * 256)
+        q[i] = make_float4(0.f, 0.f, 0.f, 0.f);
+}
 
 int forward_project(const Plan *p, const float *d_x, float *d_q, double *d_norm2,
                     const int *d_skip, cudaStream_t st) {
     const OpArgs A = make_args(p, d_skip);
-    const int nsc = slice_chunks(p);
+    const size_t nq = sin_floats(p);
     int rc;
     if (p->weighting == ARECGB_LIN) {
-        ARECGB_CUDA(cudaMemsetAsync(d_q, 0, sizeof(float) * sin_floats(p), st));
-        rc = launch_fp_lin(A, p->vec, nsc, dim3(1), d_x, d_q, st);
-        ARECGB_CUDA(cudaGetLastError());
-        if (rc) return ARECGB_ERR_ARG;
-        if (d_norm2) {
-            rc = sumsq_partials(d_q, sin_floats(p), p->d_partials, 1024, st);
-            if (rc) return rc;
-            return reduce_partials(p->d_partials, 1024, d_norm2, st);
+        ARECGB_CUDA(cudaMemsetAsync(d_q, 0, sizeof(float) * nq, st));
+        rc = launch_fp_lin(A, p->vec, d_x, d_q, st);
+    } else {
+        // zero q, then each (orientation, line band) launch adds its part
+        k_zero_unless<<<(unsigned)std::min<size_t>(152 * 8, (nq / 4 + 255) / 256), 256, 0, st>>>(
+            reinterpret_cast<float4 *>(d_q), nq / 4, d_skip);
+        const int ntile = (p->nx + kFpBins - 1) / kFpBins;
+        rc = 0;
+        for (int o = 0; o < 2 && !rc; o++) {
+            const int ngo = p->ngroups_o[o];
+            if (!ngo) continue;
+            const int g0 = o ? p->ngroups_o[0] : 0;
+            const dim3 grid(ngo * ntile, fp_slice_blocks(p));
+            for (int lo = 0; lo < p->nx && !rc; lo += p->fp_band) {
+                const int hi = std::min(p->nx, lo + p->fp_band);
+                rc = p->weighting == ARECGB_KB
+                         ? launch_fpb_kb(A, p->vec, grid, d_x, d_q, g0, ngo, lo, hi, st)
+                         : launch_fpb_sq(A, p->vec, grid, d_x, d_q, g0, ngo, lo, hi, st);
+            }
         }
-        return ARECGB_OK;
     }
-    const int ntile = (p->nx + kFpBins - 1) / kFpBins;
-    dim3 grid(p->ngroups * ntile, fp_slice_blocks(p));
-    rc = p->weighting == ARECGB_KB ? launch_fp_kb(A, p->vec, nsc, grid, d_x, d_q, st)
-                                   : launch_fp_sq(A, p->vec, nsc, grid, d_x, d_q, st);
     ARECGB_CUDA(cudaGetLastError());
     if (rc) return ARECGB_ERR_ARG;
-    if (d_norm2) return reduce_partials(p->d_partials, grid.x * grid.y, d_norm2, st);
+    if (d_norm2) {
+        rc = sumsq_partials(d_q, nq, p->d_partials, kNormBlocks, st);
+        if (rc) return rc;
+        return reduce_partials(p->d_partials, kNormBlocks, d_norm2, st);
+    }
     return ARECGB_OK;
 }
 

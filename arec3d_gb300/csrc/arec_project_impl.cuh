@@ -12,24 +12,26 @@
 //
 // Forward projection  q[a][b][y] = sum_{k,j: iqx(k,a)-1+j = b} w_j(k,a) x[k][y]
 //   reference: arecProject2D[_KB|_SQ] (arecproject.cpp:19,351,540), which
-//   scatters.  Here each output is owned by one block (no atomics): a block owns
-//   a group of up to 4 consecutive angles, a tile of BT detector bins and
-//   256/512 slices, and gathers the rays of the strip of the cylinder that
+//   scatters.  Here each output is owned by one block per launch (no atomics): a
+//   block owns a group of up to 4 consecutive angles, a tile of BT detector bins
+//   and 256 slices, and gathers the rays of the strip of the cylinder that
 //   projects into the tile.  The strip is swept line by line (rows when
 //   |cos| >= |sin|, columns otherwise, so consecutive pixels move <= 1 bin and a
-//   line holds <= 32 candidates); candidates are bucketed by centre bin with a
-//   stable counting sort in shared memory, so the accumulation loop runs over a
-//   compile-time bucket index and each loaded pixel feeds up to 3 register
-//   accumulators.  The four angle warps of a block read nearly the same pixels,
-//   which then come from L1.
+//   line holds <= 32 candidates), and the sweep is split into bands of lines,
+//   one launch per (orientation, band) adding into q, so that the concurrently
+//   running blocks read one band of x from L2.  Candidates arrive in centre-bin
+//   order, so the accumulation loop runs over a compile-time bucket index and
+//   each loaded pixel feeds up to 3 register accumulators.
 //
 // Both kernels evaluate the identical ray_taps<W>() so A and A^T are exact
-// transposes of each other.  Both fuse the FP64 sum of squares of their output
-// (one partial per block, reduced in a fixed order afterwards).
+// transposes of each other.  The back projector fuses the FP64 sum of squares
+// of its output (one partial per block, reduced in a fixed order afterwards);
+// the forward projector's is a separate pass over q.
 #pragma once
 
 #include <climits>
 
+#include "arec_umma.cuh"
 #include "arec_weights.cuh"
 
 namespace arecgb {
@@ -120,6 +122,37 @@ __device__ __forceinline__ void stg_lane(float *base, int lane, const float (&v)
         if (lane * 2 < limit) *reinterpret_cast<float2 *>(base + lane * 2) = make_float2(v[0], v[1]);
     } else {
         if (lane < limit) base[lane] = v[0];
+    }
+}
+
+constexpr uint32_t kFpWait = 1u << 20;  // mbarrier polls before a wait gives up (a row lands in ~1 us)
+
+template <int VEC>
+__device__ __forceinline__ void add_lane(float *base, int lane, const float (&v)[VEC], int limit) {
+    if constexpr (VEC >= 4) {
+#pragma unroll
+        for (int c = 0; c < VEC / 4; c++) {
+            const int o = lane_piece<VEC>(lane, c);
+            if (o < limit) {
+                float4 *d = reinterpret_cast<float4 *>(base + o);
+                float4 t = *d;
+                t.x += v[4 * c];
+                t.y += v[4 * c + 1];
+                t.z += v[4 * c + 2];
+                t.w += v[4 * c + 3];
+                *d = t;
+            }
+        }
+    } else if constexpr (VEC == 2) {
+        if (lane * 2 < limit) {
+            float2 *d = reinterpret_cast<float2 *>(base + lane * 2);
+            float2 t = *d;
+            t.x += v[0];
+            t.y += v[1];
+            *d = t;
+        }
+    } else {
+        if (lane < limit) base[lane] += v[0];
     }
 }
 
@@ -385,13 +418,6 @@ __device__ __forceinline__ bool strip_line_extent(float ca, float cl, float T1, 
 
 constexpr int kFpStage = 32;  // staged pixels per line: the union of the group's candidates
 
-template <int VEC>
-constexpr size_t fp_smem_bytes() {
-    return sizeof(float) * 2 * kFpStage * (32 * VEC) + sizeof(float4) * 2 * kGroupAngles * 32 +
-           sizeof(int) * 2 * kGroupAngles * (kFpBins + 3) +
-           sizeof(int) * (kGroupAngles * 4 + 4 + 2 * kFpStage) + sizeof(double) * kGroupAngles;
-}
-
 // Candidate pixel range [clo, chi] on line li for one angle: pixels whose
 // centre bin may fall in [b0-1, b0+BT] (a margin of one pixel each side; the
 // exact test is the centre bin itself).
@@ -428,35 +454,48 @@ __device__ __forceinline__ int line_pixel_ray(const OpArgs &A, int orient, int l
     return ri.start + li - ri.lo;
 }
 
-// Square-pixel and Kaiser-Bessel weightings.  Block = one angle group (<= 4
-// angles, one warp each) x BT bins x 32*VEC slices.  Per line of the strip, the
-// x rows of the union of the angles' candidate pixels are staged in shared
-// memory (double-buffered cp.async, one line ahead); each warp computes its
-// angle's weights for those pixels (lanes = pixels), buckets them by centre bin
-// with warp votes, and accumulates BT bins x VEC slices in registers from the
-// staged rows.
+// ---------------------------------------------------------------------------
+// Banded forward projection (square-pixel and Kaiser-Bessel weightings).
+//
+// The same gather as fp_kernel, split by line bands: one launch takes the
+// angle groups of one sweep orientation and the lines [band_lo, band_hi) of
+// their strips (rows for orientation 0, columns for 1), and ADDS its partial
+// sums to q, which is zeroed first.  All blocks of a launch then read x from one
+// band of the cylinder (band lines x nx pixels x the block's slices: 64 MB for
+// 64 lines of 1024 pixels and 256 slices), which stays in L2, instead of
+// every angle group streaming the whole volume from DRAM.  Launches run in a
+// fixed order on one stream, so the result does not depend on timing.
+//
+// Per line, warp 0 stages the union of the group's candidate rows with one
+// bulk copy per row (cp.async.bulk, completing on the buffer's mbarrier), one
+// line ahead; every warp computes its angle's weights for the staged rows
+// (lanes = rows, ordered by increasing centre bin), compacts the rows whose
+// centre bin falls in the tile (a contiguous run: the centre bin is monotonic
+// along a line; a counting sort covers any exception) and accumulates them
+// with the bucket index known at compile time.  One block barrier per line.
+template <int VEC>
+constexpr size_t fpb_smem_bytes() {
+    return sizeof(float) * 2 * kFpStage * (32 * VEC) + sizeof(float4) * kGroupAngles * 32 +
+           sizeof(int) * 2 * kFpStage + sizeof(int) * (2 * kGroupAngles + 4) +
+           sizeof(int) * kGroupAngles * (kFpBins + 3);
+}
+
 template <int W, int VEC, int BT>
 __global__ void __launch_bounds__(32 * kGroupAngles, 3)
-    fp_kernel(OpArgs A, const float *__restrict__ x, float *__restrict__ q) {
+    fp_band_kernel(OpArgs A, const float *__restrict__ x, float *__restrict__ q, int g0, int ngo,
+                   int band_lo, int band_hi) {
     constexpr int NA = kGroupAngles, NG = BT + 2, SPAN = 32 * VEC, US = kFpStage;
-    extern __shared__ __align__(16) unsigned char smem_raw[];
-    float *stg = reinterpret_cast<float *>(smem_raw);            // [2][US][SPAN]
-    // entry lists and bucket bases are double-buffered by line parity, so a line's
-    // phase B never overwrites what slower warps still read for the previous line
-    float4 *list2 = reinterpret_cast<float4 *>(stg + 2 * US * SPAN);  // [2][NA][32]
-    int *base2 = reinterpret_cast<int *>(list2 + 2 * NA * 32);        // [2][NA][NG+1]
-    int *lrange = base2 + 2 * NA * (NG + 1);                           // [NA][2]
-    int *crange = lrange + NA * 2;                                    // [NA][2] next line
-    int *uinfo = crange + NA * 2;                                     // [2][2] (ulo, n) per buffer
-    int *rowk = uinfo + 4;                                            // [2][US] ray of each staged row
-    double *red = reinterpret_cast<double *>(smem_raw + fp_smem_bytes<VEC>() - sizeof(double) * NA);
+    extern __shared__ __align__(128) unsigned char smem_raw[];
+    __shared__ __align__(8) uint64_t full[2];
+    float *stg = reinterpret_cast<float *>(smem_raw);                // [2][US][SPAN]
+    float4 *list = reinterpret_cast<float4 *>(stg + 2 * US * SPAN);  // [NA][32]
+    int *rowk = reinterpret_cast<int *>(list + NA * 32);             // [2][US] ray of each row
+    int *lrange = rowk + 2 * US;                                     // [NA][2]
+    int *uinfo = lrange + 2 * NA;                                    // [2][2] (first pixel, rows)
+    int *base = uinfo + 4;                                           // [NA][NG+1] fallback sort
     if (A.skip && *A.skip) return;
     const int ai = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const int ntile = (A.nx + BT - 1) / BT;
-    (void)ntile;
-    // consecutive blocks take consecutive angle groups of the same bin tile: their
-    // strips overlap almost entirely, so concurrently running blocks share x in L2
-    const int grp = blockIdx.x % A.ngroups, b0 = (blockIdx.x / A.ngroups) * BT;
+    const int grp = g0 + blockIdx.x % ngo, b0 = (blockIdx.x / ngo) * BT;
     const int4 G = A.groups[grp];
     const int orient = G.z;
     const float r = A.r_hi + A.r_lo;
@@ -465,6 +504,7 @@ __global__ void __launch_bounds__(32 * kGroupAngles, 3)
     const float R = r + 1.5f;
     const int yb = blockIdx.y * SPAN;
     const size_t ys = (size_t)A.ys;
+    const uint32_t row_bytes = (uint32_t)min(SPAN, A.ys - yb) * 4u;
     const bool angle_ok = ai < G.y;
     AngleParams ap;
     float ca = 1.f, cl = 0.f;
@@ -477,11 +517,16 @@ __global__ void __launch_bounds__(32 * kGroupAngles, 3)
         int lo = INT_MAX, hi = INT_MIN;
         float lmin, lmax;
         if (angle_ok && strip_line_extent(ca, cl, T1, T2, R, lmin, lmax)) {
-            lo = max(0, (int)floorf(lmin + r) - 1);
-            hi = min(A.nx - 1, (int)ceilf(lmax + r) + 1);
+            lo = max(band_lo, max(0, (int)floorf(lmin + r) - 1));
+            hi = min(band_hi - 1, min(A.nx - 1, (int)ceilf(lmax + r) + 1));
         }
         lrange[2 * ai] = lo;
         lrange[2 * ai + 1] = hi;
+    }
+    if (threadIdx.x == 0) {
+        umma::mbar_init(&full[0], 1);
+        umma::mbar_init(&full[1], 1);
+        umma::mbar_fence_init();
     }
     __syncthreads();
     int L0 = INT_MAX, L1 = INT_MIN;
@@ -490,7 +535,55 @@ __global__ void __launch_bounds__(32 * kGroupAngles, 3)
         L0 = min(L0, lrange[2 * i]);
         L1 = max(L1, lrange[2 * i + 1]);
     }
+    if (L0 > L1) return;  // the strip misses this band (uniform over the block)
     const int my_lo = lrange[2 * ai], my_hi = lrange[2 * ai + 1];
+
+    // warp 0, lanes < NA: the angles' sweep cosines for the candidate ranges
+    float cq = 1.f, lq = 0.f;
+    int q_lo = INT_MAX, q_hi = INT_MIN;
+    if (ai == 0 && lane < G.y) {
+        const AngleParams aq = A.ang[G.x + lane];
+        cq = orient ? aq.s : aq.c;
+        lq = orient ? aq.c : aq.s;
+        q_lo = lrange[2 * lane];
+        q_hi = lrange[2 * lane + 1];
+    }
+    // warp 0: stage the union of the group's candidate pixels on line li
+    auto stage = [&](int li, int buf) {
+        int clo = INT_MAX, chi = INT_MIN;
+        if (lane < NA && li >= q_lo && li <= q_hi) {
+            line_candidates(A, orient, cq, lq, T1, T2, r, li, clo, chi);
+            if (clo > chi) {
+                clo = INT_MAX;
+                chi = INT_MIN;
+            }
+        }
+#pragma unroll
+        for (int o = 1; o < NA; o <<= 1) {
+            clo = min(clo, __shfl_xor_sync(0xffffffffu, clo, o));
+            chi = max(chi, __shfl_xor_sync(0xffffffffu, chi, o));
+        }
+        const int ulo = __shfl_sync(0xffffffffu, clo, 0), uhi = __shfl_sync(0xffffffffu, chi, 0);
+        int n = uhi >= ulo ? uhi - ulo + 1 : 0;
+        if (n > US) {
+            if (lane == 0) atomicOr(A.err, 1);
+            n = US;
+        }
+        int k = 0;
+        if (lane < n) {
+            k = line_pixel_ray(A, orient, li, ulo + lane);
+            rowk[buf * US + lane] = k;
+        }
+        if (lane == 0) {
+            uinfo[2 * buf] = ulo;
+            uinfo[2 * buf + 1] = n;
+            umma::mbar_arrive_expect_tx(&full[buf], (uint32_t)n * row_bytes);
+        }
+        __syncwarp();
+        if (lane < n)
+            umma::bulk_g2s(stg + ((size_t)buf * US + lane) * SPAN, x + (size_t)k * ys + yb,
+                           row_bytes, &full[buf]);
+    };
 
     float acc[BT][VEC];
 #pragma unroll
@@ -498,131 +591,64 @@ __global__ void __launch_bounds__(32 * kGroupAngles, 3)
 #pragma unroll
         for (int v = 0; v < VEC; v++) acc[j][v] = 0.f;
 
-    // each warp: its angle's candidate range on line li -> crange
-    int next_clo = INT_MAX, next_chi = INT_MIN;
-    auto ranges = [&](int li) {
-        int clo = INT_MAX, chi = INT_MIN;
-        if (angle_ok && li >= my_lo && li <= my_hi)
-            line_candidates(A, orient, ca, cl, T1, T2, r, li, clo, chi);
-        next_clo = clo;
-        next_chi = chi;
-        if (lane == 0) {
-            crange[2 * ai] = clo;
-            crange[2 * ai + 1] = chi;
-        }
-    };
-    // all threads: union of crange -> uinfo[buf]; one lane per staged row looks
-    // up its ray index, then all threads issue the row copies
-    auto stage = [&](int li, int buf) {
-        int ulo = INT_MAX, uhi = INT_MIN;
-#pragma unroll
-        for (int i = 0; i < NA; i++) {
-            if (crange[2 * i] <= crange[2 * i + 1]) {
-                ulo = min(ulo, crange[2 * i]);
-                uhi = max(uhi, crange[2 * i + 1]);
-            }
-        }
-        int n = uhi >= ulo ? uhi - ulo + 1 : 0;
-        if (n > US) {
-            if (threadIdx.x == 0) atomicOr(A.err, 1);
-            n = US;
-        }
-        if (threadIdx.x == 0) {
-            uinfo[2 * buf] = ulo;
-            uinfo[2 * buf + 1] = n;
-        }
-        int *rk = rowk + buf * US;
-        if (threadIdx.x < n) rk[threadIdx.x] = line_pixel_ray(A, orient, li, ulo + threadIdx.x);
-        __syncthreads();
-        float *dst = stg + (size_t)buf * US * SPAN;
-        constexpr int PIECES = SPAN / 4;
-        for (int c = threadIdx.x; c < n * PIECES; c += 32 * NA) {
-            const int row = c / PIECES, col = (c % PIECES) * 4;
-            const bool ok = yb + col < A.ys;
-            cp_async16(dst + row * SPAN + col, x + (size_t)rk[row] * ys + (ok ? yb + col : 0), ok);
-        }
-    };
-
-    if (L0 <= L1) {
-        ranges(L0);
-        __syncthreads();
-        stage(L0, 0);
-        cp_async_commit();
-    }
+    if (ai == 0) stage(L0, 0);
+    __syncthreads();
+    bool ok = true;
     for (int li = L0; li <= L1; li++) {
-        const int buf = (li - L0) & 1;
-        const int my_clo = next_clo, my_chi = next_chi;
-        const int ulo = uinfo[2 * buf], un = uinfo[2 * buf + 1];
-        float4 *list = list2 + buf * NA * 32;
-        int *base = base2 + buf * NA * (NG + 1);
-        // Phase A: lanes = this angle's candidate pixels (in increasing centre-bin
-        // order); entries address the staged union rows.
+        const int it = li - L0, buf = it & 1;
+        if (ai == 0 && li + 1 <= L1) stage(li + 1, buf ^ 1);
+        const int un = uinfo[2 * buf + 1];
+        if (ok && !umma::mbar_wait(&full[buf], (uint32_t)(it >> 1) & 1u, kFpWait)) {
+            ok = false;
+            atomicOr(A.err, 16);
+        }
+        // Phase A: lanes = staged rows in increasing centre-bin order for this angle.
         bool valid = false;
         int gk = 0;
         float4 ent = make_float4(0.f, 0.f, 0.f, 0.f);
-        // an angle with no candidates on this line has (INT_MAX, INT_MIN): test
-        // before subtracting, the difference would overflow
-        int mlo = 0, mhi = -1;
-        if (my_clo <= my_chi && un > 0) {
-            mlo = max(my_clo, ulo);
-            mhi = min(my_chi, ulo + un - 1);
-        }
-        const int mn = mhi - mlo + 1;  // <= un; pix - ulo stays in [0, un)
-        if (angle_ok && lane < mn) {
-            const int pix = ca > 0.f ? mlo + lane : mhi - lane;
-            const int k = rowk[buf * US + (pix - ulo)];
+        if (ok && angle_ok && lane < un && li >= my_lo && li <= my_hi) {
+            const int row = ca > 0.f ? lane : un - 1 - lane;
+            const int k = rowk[buf * US + row];
             const Taps t = ray_taps<W>(A.ray[k], ap, A.r_hi, A.r_lo);
             gk = t.iqx - b0 + 1;
             valid = gk >= 0 && gk <= BT + 1;
-            ent = make_float4(__int_as_float(pix - ulo), t.w0, t.w1, t.w2);
+            ent = make_float4(__int_as_float(row | (gk << 8)), t.w0, t.w1, t.w2);
         }
-        // Phase B (warp-local): stable counting sort by bucket.
-        const unsigned key = valid ? (unsigned)gk : 64u + lane;
-        const unsigned peers = __match_any_sync(0xffffffffu, key);
-        const int rank = __popc(peers & ((1u << lane) - 1u));
-        // lane g (< NG) learns the size of bucket g from that bucket's first member
-        const int leader = (valid && rank == 0) ? gk : -1;
-        int cnt = 0;
-        {
-            const unsigned lead_mask = __ballot_sync(0xffffffffu, leader >= 0);
-            unsigned m = lead_mask;
-            while (m) {
-                const int src = __ffs(m) - 1;
-                m &= m - 1;
-                const int g_src = __shfl_sync(0xffffffffu, leader, src);
-                const int c_src = __popc(__shfl_sync(0xffffffffu, (int)peers, src));
-                if (lane == g_src) cnt = c_src;
-            }
-        }
-        int incl = cnt;  // inclusive scan over lanes 0..31 of the bucket sizes
+        // Phase B: compaction.  Expected: the valid lanes are one run with
+        // non-decreasing centre bins; otherwise a stable counting sort.
+        const unsigned vm = __ballot_sync(0xffffffffu, valid);
+        const int cnt = __popc(vm);
+        const int f = vm ? __ffs(vm) - 1 : 0;
+        const int gprev = __shfl_up_sync(0xffffffffu, gk, 1);
+        const bool run = vm == 0 || (vm >> f) == (cnt == 32 ? 0xffffffffu : (1u << cnt) - 1u);
+        const bool sorted = run && !__any_sync(0xffffffffu, valid && lane > f && gk < gprev);
+        if (sorted) {
+            if (valid) list[ai * 32 + lane - f] = ent;
+        } else {
+            const unsigned key = valid ? (unsigned)gk : 64u + lane;
+            const unsigned peers = __match_any_sync(0xffffffffu, key);
+            const int rank = __popc(peers & ((1u << lane) - 1u));
+            int mybase = 0;
 #pragma unroll
-        for (int o = 1; o < 32; o <<= 1) {
-            const int t = __shfl_up_sync(0xffffffffu, incl, o);
-            if (lane >= o) incl += t;
+            for (int gg = 0; gg <= NG; gg++) {
+                const int c = __popc(__ballot_sync(0xffffffffu, valid && gk < gg));
+                if (valid && gg == gk) mybase = c;
+            }
+            if (valid) list[ai * 32 + mybase + rank] = ent;
         }
-        const int excl = incl - cnt;
-        if (lane <= NG) base[ai * (NG + 1) + lane] = excl;
-        const int mybase = __shfl_sync(0xffffffffu, excl, valid ? gk : 0);
-        if (valid) list[ai * 32 + mybase + rank] = ent;
-        // next line's ranges, then its staging one line ahead (stage() syncs once
-        // after publishing the ranges' union and row table)
-        if (li + 1 <= L1) ranges(li + 1);
-        __syncthreads();
-        if (li + 1 <= L1) stage(li + 1, buf ^ 1);
-        cp_async_commit();
-        cp_async_wait<1>();
-        __syncthreads();
-        // Phase C: accumulate with the bucket index known at compile time.
-        if (angle_ok) {
+        __syncwarp();
+        // Phase C: entries in bucket order; the bucket index is a compile-time constant.
+        if (cnt) {
             const float *S = stg + (size_t)buf * US * SPAN;
-            const int *bb = base + ai * (NG + 1);
+            int i = 0;
 #pragma unroll
             for (int gg = 0; gg < NG; gg++) {
-                const int e1 = bb[gg + 1];
-                for (int i = bb[gg]; i < e1; i++) {
+                while (i < cnt) {
                     const float4 e = list[ai * 32 + i];
+                    const int key = __float_as_int(e.x);
+                    if ((key >> 8) != gg) break;
                     float v[VEC];
-                    lds_lane<VEC>(S + __float_as_int(e.x) * SPAN, lane, v);
+                    lds_lane<VEC>(S + (key & 255) * SPAN, lane, v);
                     if (gg >= 2) {
 #pragma unroll
                         for (int c = 0; c < VEC; c++) acc[gg >= 2 ? gg - 2 : 0][c] =
@@ -638,26 +664,24 @@ __global__ void __launch_bounds__(32 * kGroupAngles, 3)
                         for (int c = 0; c < VEC; c++) acc[gg <= BT - 1 ? gg : 0][c] =
                             fmaf(e.w, v[c], acc[gg <= BT - 1 ? gg : 0][c]);
                     }
+                    i++;
                 }
             }
         }
+        __syncthreads();  // buffer, row table and lists free for the next lines
     }
-    cp_async_wait<0>();
-
-    double s2 = 0.0;
+    if (!ok) {
+        // a wait gave up: let the copies still in flight land before the block exits
+        for (int it = max(0, L1 - L0 - 1); it <= L1 - L0; it++)
+            umma::mbar_wait(&full[it & 1], (uint32_t)(it >> 1) & 1u, kFpWait);
+        return;
+    }
     if (angle_ok) {
-        const int a = G.x + ai;
-        float *qa = q + (size_t)a * A.nx * ys + yb;
+        float *qa = q + (size_t)(G.x + ai) * A.nx * ys + yb;
 #pragma unroll
-        for (int j = 0; j < BT; j++) {
-            if (b0 + j < A.nx) {
-                stg_lane<VEC>(qa + (size_t)(b0 + j) * ys, lane, acc[j], A.ys - yb);
-#pragma unroll
-                for (int c = 0; c < VEC; c++) s2 += (double)__fmul_rn(acc[j][c], acc[j][c]);
-            }
-        }
+        for (int j = 0; j < BT; j++)
+            if (b0 + j < A.nx) add_lane<VEC>(qa + (size_t)(b0 + j) * ys, lane, acc[j], A.ys - yb);
     }
-    block_sum_to<NA>(s2, red, A.partials + (size_t)blockIdx.y * gridDim.x + blockIdx.x);
 }
 
 // ---------------------------------------------------------------------------
@@ -728,38 +752,40 @@ int launch_bp(const OpArgs &A, int vec, int nsc, dim3 grid, const float *s, floa
 }
 
 template <int W, int V, int BT>
-int launch_fp_one(const OpArgs &A, dim3 grid, const float *x, float *q, cudaStream_t st) {
-    constexpr size_t smem = fp_smem_bytes<V>();
+int launch_fpb_one(const OpArgs &A, dim3 grid, const float *x, float *q, int g0, int ngo, int lo,
+                   int hi, cudaStream_t st) {
+    constexpr size_t smem = fpb_smem_bytes<V>();
     static bool configured = false;  // per instantiation, once per process
     if (!configured) {
-        if (cudaFuncSetAttribute(fp_kernel<W, V, BT>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                 (int)smem) != cudaSuccess)
+        if (cudaFuncSetAttribute(fp_band_kernel<W, V, BT>,
+                                 cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
             return -2;
         configured = true;
     }
-    fp_kernel<W, V, BT><<<grid, 32 * kGroupAngles, smem, st>>>(A, x, q);
+    fp_band_kernel<W, V, BT><<<grid, 32 * kGroupAngles, smem, st>>>(A, x, q, g0, ngo, lo, hi);
     return 0;
 }
 
 template <int W, int BT>
-int launch_fp(const OpArgs &A, int vec, int nsc, dim3 grid, const float *x, float *q,
-              cudaStream_t st) {
-    (void)nsc;
-    if constexpr (W == ARECGB_LIN) {
-        (void)grid;
-        const long long n = (long long)A.nrays * (A.ys / vec);
-        const unsigned blocks = (unsigned)((n + 255) / 256);
-        if (vec == 1) fp_lin_kernel<1><<<blocks, 256, 0, st>>>(A, x, q);
-        else if (vec == 2) fp_lin_kernel<2><<<blocks, 256, 0, st>>>(A, x, q);
-        else if (vec == 4) fp_lin_kernel<4><<<blocks, 256, 0, st>>>(A, x, q);
-        else fp_lin_kernel<8><<<blocks, 256, 0, st>>>(A, x, q);
-        return 0;
-    } else {
-        if (vec == 1) return launch_fp_one<W, 1, BT>(A, grid, x, q, st);
-        if (vec == 2) return launch_fp_one<W, 2, BT>(A, grid, x, q, st);
-        if (vec == 4) return launch_fp_one<W, 4, BT>(A, grid, x, q, st);
-        return launch_fp_one<W, 8, BT>(A, grid, x, q, st);
-    }
+int launch_fpb(const OpArgs &A, int vec, dim3 grid, const float *x, float *q, int g0, int ngo,
+               int lo, int hi, cudaStream_t st) {
+    if (vec == 1) return launch_fpb_one<W, 1, BT>(A, grid, x, q, g0, ngo, lo, hi, st);
+    if (vec == 2) return launch_fpb_one<W, 2, BT>(A, grid, x, q, g0, ngo, lo, hi, st);
+    if (vec == 4) return launch_fpb_one<W, 4, BT>(A, grid, x, q, g0, ngo, lo, hi, st);
+    return launch_fpb_one<W, 8, BT>(A, grid, x, q, g0, ngo, lo, hi, st);
+}
+
+// Linear weighting (scatter).
+template <int W>
+int launch_fp(const OpArgs &A, int vec, const float *x, float *q, cudaStream_t st) {
+    static_assert(W == ARECGB_LIN, "the other weightings use the banded kernel");
+    const long long n = (long long)A.nrays * (A.ys / vec);
+    const unsigned blocks = (unsigned)((n + 255) / 256);
+    if (vec == 1) fp_lin_kernel<1><<<blocks, 256, 0, st>>>(A, x, q);
+    else if (vec == 2) fp_lin_kernel<2><<<blocks, 256, 0, st>>>(A, x, q);
+    else if (vec == 4) fp_lin_kernel<4><<<blocks, 256, 0, st>>>(A, x, q);
+    else fp_lin_kernel<8><<<blocks, 256, 0, st>>>(A, x, q);
+    return 0;
 }
 
 }  // namespace arecgb

@@ -8,9 +8,9 @@ int launch_bp_kb(const OpArgs &A, int vec, int nsc, dim3 grid, const float *s, f
     return launch_bp<ARECGB_KB>(A, vec, nsc, grid, s, g, st);
 }
 
-int launch_fp_kb(const OpArgs &A, int vec, int nsc, dim3 grid, const float *x, float *q,
-               cudaStream_t st) {
-    return launch_fp<ARECGB_KB, kFpBins>(A, vec, nsc, grid, x, q, st);
+int launch_fpb_kb(const OpArgs &A, int vec, dim3 grid, const float *x, float *q, int g0, int ngo,
+                int lo, int hi, cudaStream_t st) {
+    return launch_fpb<ARECGB_KB, kFpBins>(A, vec, grid, x, q, g0, ngo, lo, hi, st);
 }
 
 }  // namespace arecgb

@@ -8,9 +8,8 @@ int launch_bp_lin(const OpArgs &A, int vec, int nsc, dim3 grid, const float *s, 
     return launch_bp<ARECGB_LIN>(A, vec, nsc, grid, s, g, st);
 }
 
-int launch_fp_lin(const OpArgs &A, int vec, int nsc, dim3 grid, const float *x, float *q,
-               cudaStream_t st) {
-    return launch_fp<ARECGB_LIN, kFpBins>(A, vec, nsc, grid, x, q, st);
+int launch_fp_lin(const OpArgs &A, int vec, const float *x, float *q, cudaStream_t st) {
+    return launch_fp<ARECGB_LIN>(A, vec, x, q, st);
 }
 
 }  // namespace arecgb

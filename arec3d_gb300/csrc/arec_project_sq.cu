@@ -8,9 +8,9 @@ int launch_bp_sq(const OpArgs &A, int vec, int nsc, dim3 grid, const float *s, f
     return launch_bp<ARECGB_SQ>(A, vec, nsc, grid, s, g, st);
 }
 
-int launch_fp_sq(const OpArgs &A, int vec, int nsc, dim3 grid, const float *x, float *q,
-               cudaStream_t st) {
-    return launch_fp<ARECGB_SQ, kFpBins>(A, vec, nsc, grid, x, q, st);
+int launch_fpb_sq(const OpArgs &A, int vec, dim3 grid, const float *x, float *q, int g0, int ngo,
+                int lo, int hi, cudaStream_t st) {
+    return launch_fpb<ARECGB_SQ, kFpBins>(A, vec, grid, x, q, g0, ngo, lo, hi, st);
 }
 
 }  // namespace arecgb
