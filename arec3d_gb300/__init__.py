@@ -119,6 +119,9 @@ def lib():
         for n in ("arecgb_unet_images_from_volume", "arecgb_unet_images_to_volume"):
             getattr(L, n).argtypes = [vp, vp, vp, C.c_int, C.c_int, C.c_int, C.c_float, vp]
         L.arecgb_warm_start.argtypes = [vp, vp, vp, vp, vp, vp, vp]
+        L.arecgb_plan_timing.argtypes = [vp, C.c_int, dp, C.POINTER(C.c_longlong), dp,
+                                         C.POINTER(C.c_longlong)]
+        L.arecgb_launch_count.restype = C.c_longlong
         _lib = L
     return _lib
 
@@ -218,6 +221,15 @@ class Plan:
         _check(rc, "arecgb_sirt")
         return hist[:min(info.iterations, maxit)].copy(), info
 
+    def timing(self, mode):
+        """Projector timing (mode 1 start, 2 report, 0 report and stop):
+        (fp_ms, fp_calls, bp_ms, bp_calls)."""
+        fm, bm = C.c_double(), C.c_double()
+        fc, bc = C.c_longlong(), C.c_longlong()
+        _check(lib().arecgb_plan_timing(self._h, mode, C.byref(fm), C.byref(fc), C.byref(bm),
+                                        C.byref(bc)), "arecgb_plan_timing")
+        return fm.value, fc.value, bm.value, bc.value
+
     def sino_from_reference(self, ref, dev, stream=None):
         _check(lib().arecgb_sino_from_reference(_ptr(ref), _ptr(dev), self.nangles, self.ny,
                                                 self.nx, self.ys, _stream(stream)),
@@ -279,7 +291,7 @@ class UNet:
         return loss.value
 
     def warm_start(self, plan, x_early, x0, img_in, img_out, stream=None):
-        _check(lib().arecgb_warm_start(plan._h, _ptr(x_early), _ptr(x0), _ptr(img_in),
+        _check(lib().arecgb_warm_start(plan._h, self._h, _ptr(x_early), _ptr(x0), _ptr(img_in),
                                        _ptr(img_out), _stream(stream)), "arecgb_warm_start")
 
 
@@ -293,6 +305,11 @@ def images_to_volume(plan, img, vol, npad, y0, count, scale=1.0, stream=None):
     _check(lib().arecgb_unet_images_to_volume(plan._h, _ptr(img), _ptr(vol), npad, y0, count,
                                               scale, _stream(stream)),
            "arecgb_unet_images_to_volume")
+
+
+def launch_count():
+    """Kernel launches issued by the library so far."""
+    return int(lib().arecgb_launch_count())
 
 
 def cc_shifts(img1, img2, sx, sy, ix=None, iy=None, stream=None):

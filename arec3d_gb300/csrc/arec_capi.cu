@@ -142,6 +142,17 @@ int arecgb_sino_to_reference(const float *d_dev, float *d_ref, int na, int ny, i
     return sino_to_reference_layout(d_dev, d_ref, na, ny, nx, ys, (cudaStream_t)stream);
 }
 
+int arecgb_plan_timing(arecgb_plan *plan, int mode, double *fp_ms, long long *fp_calls,
+                       double *bp_ms, long long *bp_calls) {
+    if (!plan || mode < 0 || mode > 2) {
+        set_error("arecgb_plan_timing: bad arguments");
+        return ARECGB_ERR_ARG;
+    }
+    return plan_timing(P(plan), mode, fp_ms, fp_calls, bp_ms, bp_calls);
+}
+
+long long arecgb_launch_count(void) { return launch_count(); }
+
 int arecgb_cc_shifts(const float *d_img1, const float *d_img2, int nz, int ny, int nx,
                      float *d_sx, float *d_sy, int *d_ix, int *d_iy, void *stream) {
     return cc_shifts(d_img1, d_img2, nz, ny, nx, d_sx, d_sy, d_ix, d_iy, (cudaStream_t)stream);

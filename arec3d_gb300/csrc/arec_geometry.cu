@@ -6,6 +6,7 @@
 #include <string.h>
 
 #include <algorithm>
+#include <atomic>
 #include <cmath>
 
 #include "arec_internal.cuh"
@@ -16,6 +17,10 @@ static thread_local std::string g_last_error;
 
 void set_error(const std::string &msg) { g_last_error = msg; }
 const char *last_error() { return g_last_error.c_str(); }
+
+static std::atomic<long long> g_launches{0};
+void count_launches(int n) { g_launches.fetch_add(n, std::memory_order_relaxed); }
+long long launch_count() { return g_launches.load(std::memory_order_relaxed); }
 
 int cuda_status(cudaError_t e) {
     if (e == cudaErrorMemoryAllocation) return ARECGB_ERR_NOMEM;
@@ -246,6 +251,8 @@ void plan_destroy(Plan *p) {
     cudaFree(p->d_ang);
     cudaFree(p->d_rows);
     cudaFree(p->d_cols);
+    for (cudaEvent_t e : p->ev_fp) cudaEventDestroy(e);
+    for (cudaEvent_t e : p->ev_bp) cudaEventDestroy(e);
     cudaFree(p->d_groups);
     cudaFree(p->d_tiles);
     cudaFree(p->d_err);

@@ -84,7 +84,17 @@ struct Plan {
     size_t pinned_floats = 0;
 
     cudaStream_t stream = nullptr; // plan-owned stream for the compatible entry points
+
+    // optional projector timing: CUDA events around every forward / back
+    // projection (arecgb_plan_timing); pairs are reused across calls
+    mutable bool timing = false;
+    mutable std::vector<cudaEvent_t> ev_fp, ev_bp;  // start, stop, start, stop, ...
+    mutable size_t n_fp = 0, n_bp = 0;
 };
+
+// Kernel launches issued by this library (all threads), for reporting.
+void count_launches(int n);
+long long launch_count();
 
 constexpr int kTileX = 8, kTileZ = 4;  // back-projection ray tile (32 rays)
 constexpr int kGroupAngles = 4;        // angles per forward-projection block
@@ -103,6 +113,8 @@ int forward_project(const Plan *p, const float *d_x, float *d_q, double *d_norm2
 int back_project(const Plan *p, const float *d_s, float *d_g, double *d_norm2,
                  const int *d_skip, cudaStream_t st);
 int fp_grid_blocks(const Plan *p);
+int plan_timing(const Plan *p, int mode, double *fp_ms, long long *fp_calls, double *bp_ms,
+                long long *bp_calls);
 int bp_grid_blocks(const Plan *p);
 
 // Layout kernels and vector ops (arec_vector.cu)

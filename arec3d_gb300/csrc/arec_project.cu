@@ -53,6 +53,55 @@ int fp_grid_blocks(const Plan *) { return kNormBlocks; }
 
 int bp_grid_blocks(const Plan *p) { return p->ntiles * slice_blocks(p); }
 
+// Event pair i of a timing list (created on first use).
+static int timing_event(std::vector<cudaEvent_t> &v, size_t i, cudaEvent_t *out) {
+    while (v.size() <= i) {
+        cudaEvent_t e;
+        ARECGB_CUDA(cudaEventCreate(&e));
+        v.push_back(e);
+    }
+    *out = v[i];
+    return 0;
+}
+
+static int timing_mark(const Plan *p, bool fp, bool stop, cudaStream_t st) {
+    if (!p->timing) return 0;
+    std::vector<cudaEvent_t> &v = fp ? p->ev_fp : p->ev_bp;
+    size_t &n = fp ? p->n_fp : p->n_bp;
+    cudaEvent_t e;
+    int rc = timing_event(v, 2 * n + (stop ? 1 : 0), &e);
+    if (rc) return rc;
+    ARECGB_CUDA(cudaEventRecord(e, st));
+    if (stop) n++;
+    return 0;
+}
+
+int plan_timing(const Plan *p, int mode, double *fp_ms, long long *fp_calls, double *bp_ms,
+                long long *bp_calls) {
+    if (mode == 1) {
+        p->timing = true;
+        p->n_fp = p->n_bp = 0;
+        return 0;
+    }
+    double t[2] = {0.0, 0.0};
+    for (int k = 0; k < 2; k++) {
+        const std::vector<cudaEvent_t> &v = k ? p->ev_bp : p->ev_fp;
+        const size_t n = k ? p->n_bp : p->n_fp;
+        if (n) ARECGB_CUDA(cudaEventSynchronize(v[2 * n - 1]));
+        for (size_t i = 0; i < n; i++) {
+            float ms = 0.f;
+            ARECGB_CUDA(cudaEventElapsedTime(&ms, v[2 * i], v[2 * i + 1]));
+            t[k] += ms;
+        }
+    }
+    if (fp_ms) *fp_ms = t[0];
+    if (bp_ms) *bp_ms = t[1];
+    if (fp_calls) *fp_calls = (long long)p->n_fp;
+    if (bp_calls) *bp_calls = (long long)p->n_bp;
+    if (mode == 0) p->timing = false;
+    return 0;
+}
+
 // q = 0 unless the solve has finished (then the call leaves q alone).
 __global__ void __launch_bounds__(256) k_zero_unless(float4 *q, size_t n4, const int *skip) {
     if (skip && *skip) return;
@@ -64,10 +113,12 @@ int forward_project(const Plan *p, const float *d_x, float *d_q, double *d_norm2
                     const int *d_skip, cudaStream_t st) {
     const OpArgs A = make_args(p, d_skip);
     const size_t nq = sin_floats(p);
-    int rc;
+    int rc = timing_mark(p, true, false, st);
+    if (rc) return rc;
     if (p->weighting == ARECGB_LIN) {
         ARECGB_CUDA(cudaMemsetAsync(d_q, 0, sizeof(float) * nq, st));
         rc = launch_fp_lin(A, p->vec, d_x, d_q, st);
+        count_launches(1);
     } else {
         // zero q, then each (orientation, line band) launch adds its part
         k_zero_unless<<<(unsigned)std::min<size_t>(152 * 8, (nq / 4 + 255) / 256), 256, 0, st>>>(
@@ -84,17 +135,21 @@ int forward_project(const Plan *p, const float *d_x, float *d_q, double *d_norm2
                 rc = p->weighting == ARECGB_KB
                          ? launch_fpb_kb(A, p->vec, grid, d_x, d_q, g0, ngo, lo, hi, st)
                          : launch_fpb_sq(A, p->vec, grid, d_x, d_q, g0, ngo, lo, hi, st);
+                count_launches(1);
             }
         }
+        count_launches(1);
     }
     ARECGB_CUDA(cudaGetLastError());
     if (rc) return ARECGB_ERR_ARG;
     if (d_norm2) {
         rc = sumsq_partials(d_q, nq, p->d_partials, kNormBlocks, st);
         if (rc) return rc;
-        return reduce_partials(p->d_partials, kNormBlocks, d_norm2, st);
+        rc = reduce_partials(p->d_partials, kNormBlocks, d_norm2, st);
+        if (rc) return rc;
+        count_launches(2);
     }
-    return ARECGB_OK;
+    return timing_mark(p, true, true, st);
 }
 
 int back_project(const Plan *p, const float *d_s, float *d_g, double *d_norm2,
@@ -102,7 +157,9 @@ int back_project(const Plan *p, const float *d_s, float *d_g, double *d_norm2,
     const OpArgs A = make_args(p, d_skip);
     const int nsc = slice_chunks(p);
     dim3 grid(p->ntiles, slice_blocks(p));
-    int rc;
+    int rc = timing_mark(p, false, false, st);
+    if (rc) return rc;
+    count_launches(d_norm2 ? 2 : 1);
     if (p->weighting == ARECGB_LIN)
         rc = launch_bp_lin(A, p->vec, nsc, grid, d_s, d_g, st);
     else if (p->weighting == ARECGB_KB)
@@ -111,8 +168,11 @@ int back_project(const Plan *p, const float *d_s, float *d_g, double *d_norm2,
         rc = launch_bp_sq(A, p->vec, nsc, grid, d_s, d_g, st);
     ARECGB_CUDA(cudaGetLastError());
     if (rc) return ARECGB_ERR_ARG;
-    if (d_norm2) return reduce_partials(p->d_partials, grid.x * grid.y, d_norm2, st);
-    return ARECGB_OK;
+    if (d_norm2) {
+        rc = reduce_partials(p->d_partials, grid.x * grid.y, d_norm2, st);
+        if (rc) return rc;
+    }
+    return timing_mark(p, false, true, st);
 }
 
 }  // namespace arecgb

@@ -391,6 +391,7 @@ static int cgls_iteration(Plan *p, SolveState *S, double *hist, float *x, float 
     rc = back_project(p, s, g, &S->gnorm2, &S->done, st);
     if (rc) return rc;
     k_cgls_gamma<<<1, 1, 0, st>>>(S, hist);
+    count_launches(6);
     ARECGB_CUDA(cudaGetLastError());
     return ARECGB_OK;
 }
@@ -414,6 +415,7 @@ int cgls(Plan *p, const float *d_b, float *d_x, int warm, int maxit, float tol, 
         rc = forward_project(p, d_x, q, nullptr, nullptr, st);
         if (rc) goto done;
         k_sub<<<grid_for(ns, 16), 256, 0, st>>>(d_b, q, s, ns);
+        count_launches(1);
     } else {
         cudaMemsetAsync(d_x, 0, sizeof(float) * nv, st);
         cudaMemcpyAsync(s, d_b, sizeof(float) * ns, cudaMemcpyDeviceToDevice, st);
@@ -423,6 +425,7 @@ int cgls(Plan *p, const float *d_b, float *d_x, int warm, int maxit, float tol, 
     rc = back_project(p, s, g, &S->gnorm2, nullptr, st);
     if (rc) goto done;
     k_cgls_init<<<1, 1, 0, st>>>(S, maxit, tol, rnorm_ref);
+    count_launches(1);
     {
         // Iterations are queued in batches; the stopping test runs on the device
         // and later queued iterations return at once.
@@ -449,6 +452,7 @@ int cgls(Plan *p, const float *d_b, float *d_x, int warm, int maxit, float tol, 
         // flush a pending best-iterate copy, then restore it if the reference would
         k_cgls_save<<<grid_for(nv, 16), 256, 0, st>>>(S, d_x, xs, nv / 4);
         k_cgls_save_done<<<1, 1, 0, st>>>(S);
+        count_launches(2);
         cudaError_t e =
             cudaMemcpyAsync(sc.h_state, S, sizeof(SolveState), cudaMemcpyDeviceToHost, st);
         if (e == cudaSuccess) e = cudaStreamSynchronize(st);
@@ -523,6 +527,7 @@ int sirt(Plan *p, const float *d_b, float *d_x, float lam, int maxit, float tol,
             k_sirt_first<<<nblk, 256, 0, st>>>(bvol, grad, nv, red, red + kRedBlocks);
             k_reduce_partials<<<1, 256, 0, st>>>(red, nblk, red + 2 * kRedBlocks);
             k_reduce_partials<<<1, 256, 0, st>>>(red + kRedBlocks, nblk, red + 2 * kRedBlocks + 1);
+            count_launches(3);
         } else {
             rc = forward_project(p, d_x, proj, nullptr, nullptr, st);
             if (rc) break;
@@ -530,6 +535,7 @@ int sirt(Plan *p, const float *d_b, float *d_x, float lam, int maxit, float tol,
             if (rc) break;
             k_sirt_grad<<<nblk, 256, 0, st>>>(bvol, pvol, grad, nv, red + kRedBlocks);
             k_reduce_partials<<<1, 256, 0, st>>>(red + kRedBlocks, nblk, red + 2 * kRedBlocks + 1);
+            count_launches(2);
         }
         cudaError_t e = cudaMemcpyAsync(h_red, red + 2 * kRedBlocks, sizeof(double) * 2,
                                         cudaMemcpyDeviceToHost, st);
@@ -574,6 +580,7 @@ int sirt(Plan *p, const float *d_b, float *d_x, float lam, int maxit, float tol,
         }
         relnrm0 = relnrm;
         k_sirt_update<<<grid_for(nv, 8), 256, 0, st>>>(d_x, grad, lam, nv);
+        count_launches(1);
         ++iter;
     }
     if (rc == 0) {

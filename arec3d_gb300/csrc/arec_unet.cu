@@ -222,6 +222,7 @@ static int forward(Net *n, const float *x, float *y, int N, cudaStream_t st) {
     if ((rc = conv(n, D1A, n->cat1, n->f1, N, H, W, st))) return rc;
     if ((rc = conv(n, D1B, n->f1, n->g1, N, H, W, st))) return rc;
     conv_out(n->g1, n->params + n->woff[OUT], n->params + n->boff[OUT], x, y, P0, 32, st);
+    count_launches(27);  // conv_in, 16 tensor-core convolutions, 3 pool, 3 upsample, 3 copy, out
     ARECGB_CUDA(cudaGetLastError());
     n->in = x;
     n->lastN = N;
@@ -352,6 +353,7 @@ static int warm_start(const Plan *p, Net *n, const float *x_early, float *x0, fl
     std::vector<double> hp(nb);
     ARECGB_CUDA(cudaMallocAsync(&part, sizeof(double) * nb, st));
     sumsq_partial(x_early, (size_t)p->nrays * p->ys, part, nb, st);
+    count_launches(1);
     ARECGB_CUDA(cudaMemcpyAsync(hp.data(), part, sizeof(double) * nb, cudaMemcpyDeviceToHost, st));
     ARECGB_CUDA(cudaFreeAsync(part, st));
     ARECGB_CUDA(cudaStreamSynchronize(st));
@@ -371,6 +373,7 @@ static int warm_start(const Plan *p, Net *n, const float *x_early, float *x0, fl
         int rc = forward(n, img_in, img_out, B, st);
         if (rc) return rc;
         img_to_cyl(img_out, p->d_rows, x0, p->nx, npad, p->ys, y0, B, (float)rms, st);
+        count_launches(2);
     }
     ARECGB_CUDA(cudaGetLastError());
     return check_err(n, st, "warm_start");

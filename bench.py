@@ -1,18 +1,23 @@
-"""Benchmark: slices/s of CGLS to relative residual 1e-3 on the 1024^2 x 512-slice,
-1200-angle cylinder (square-pixel projector), on one GB300 per rank.
+"""Benchmark: slices/s to relative residual 1e-3 on the 1024^2 x 512-slice,
+1200-angle cylinder (square-pixel projector), on one GB300 per rank:
+learned-warm-start CGLS (the headline `value`) beside plain CGLS.
 
-One step = one complete CGLS solve of the whole volume from zero, stopped when
-||A^T(b - A x_k)|| / ||A^T b|| <= 1e-3 (fixed denominator) or after 200
-iterations.  Inputs: a seeded random-sphere cylinder with analytic line
+One step = one complete reconstruction of the whole volume: 10 SIRT
+iterations, the BF16 U-Net warm start (arec3d_gb300/weights), then CGLS from
+that guess until ||A^T(b - A x_k)|| / ||A^T b|| <= 1e-3 (the denominator fixed
+at its cold-start value) or 200 iterations.  `config.plain_cgls` is the same
+problem solved by CGLS from zero.  `--plain` (or missing weights) makes plain
+CGLS the headline.  Inputs: a seeded random-sphere cylinder with analytic line
 integrals and Poisson noise at 5e3 photons (no public dataset exists).
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
 
 Prints one JSON line on rank 0.  With N > 1 (torchrun) every rank solves its
 own replica (the path needs no exchange: replicas only, weak scaling).
-`--impl reference` times the reference's CPU algorithm for the same metric on
-this host's cores (the oracle's C restatement, one thread per slab of slices
-like the reference's MPI ranks) on a bounded sample and extrapolates.
+`--impl reference` times the reference's CPU algorithm (plain CGLS) for the
+same metric on this host's cores (the oracle's C restatement, one thread per
+slab of slices like the reference's MPI ranks) on a bounded sample and
+extrapolates.
 """
 import argparse
 import ctypes as C
@@ -32,6 +37,7 @@ os.environ.setdefault("ARECGB_QUIET", "1")
 
 NX, NY, NA = 1024, 512, 1200
 TOL, MAXIT = 1e-3, 200
+SIRT_ITERS = 10
 PHOTONS = 5e3
 METRIC = "slices/s to rel. residual 1e-3 (1024², 1200 ang): warm-start vs plain CGLS"
 CONFIG = {"workload": "plain CGLS to ||A^T r||/||A^T b|| <= 1e-3 (max 200 it), square-pixel "
@@ -215,13 +221,17 @@ def main():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--ref-slices", type=int, default=16)
-    ap.add_argument("--ref-iters", type=int, default=60,
-                    help="iterations to extrapolate the reference arm to")
+    ap.add_argument("--ref-iters", type=int, default=32,
+                    help="iterations to extrapolate the reference arm to (plain CGLS needs 32 "
+                         "on this problem)")
     ap.add_argument("--kernels-only", action="store_true",
                     help="run only the forward and back projectors (for profiling)")
     ap.add_argument("--slices", type=int, default=NY, help="slices for --kernels-only")
     ap.add_argument("--launches", type=int, default=3, help="launches for --kernels-only")
     ap.add_argument("--angles", type=int, default=NA, help="angles for --kernels-only")
+    ap.add_argument("--plain", action="store_true", help="plain CGLS only (no warm start)")
+    ap.add_argument("--weights", default=os.path.join(ROOT, "arec3d_gb300", "weights",
+                                                      "unet_warm_start.npz"))
     args = ap.parse_args()
     rank, local, world = dist_env()
     if args.kernels_only:
@@ -235,6 +245,7 @@ def main():
     import torch
 
     import arec3d_gb300 as gb
+    from arec3d_gb300 import warmstart as ws
 
     torch.cuda.set_device(local)
     if world > 1:
@@ -245,13 +256,14 @@ def main():
     plan, b, angles = make_problem(gb, seed=1000 + rank)
     x = torch.zeros(plan.nrays, plan.ys, dtype=torch.float32, device="cuda")
     stream = torch.cuda.current_stream()
+    lam = ws.sirt_lambda(plan)
 
-    # fixed denominator ||A^T b||
-    g = torch.zeros_like(x)
-    n2 = torch.zeros(1, dtype=torch.float64, device="cuda")
-    plan.backproject(b, g, norm2=n2, stream=stream)
-    rnorm_ref = float(n2.item()) ** 0.5
-    del g
+    # the learned warm start: committed weights, inference net over 16 slices at a time
+    net, meta = None, {}
+    if not args.plain and os.path.exists(args.weights):
+        net, meta = ws.load(gb, args.weights, plan.nx, 16)
+        npix = 16 * plan.nx * plan.nx
+        scratch = (torch.empty(npix, device="cuda"), torch.empty(npix, device="cuda"))
 
     def barrier():
         if world > 1:
@@ -259,131 +271,165 @@ def main():
 
             dist.barrier()
 
-    iters = []
-    for _ in range(args.warmup):
-        hist, info = plan.cgls(b, x, MAXIT, TOL, rnorm_ref=rnorm_ref, stream=stream)
-    barrier()
-    torch.cuda.synchronize()
-    clocks = ClockSampler(local)
-    clocks.start()
-    ev0 = torch.cuda.Event(enable_timing=True)
-    ev1 = torch.cuda.Event(enable_timing=True)
-    ev0.record(stream)
-    for _ in range(args.steps):
-        hist, info = plan.cgls(b, x, MAXIT, TOL, rnorm_ref=rnorm_ref, stream=stream)
-        iters.append(info.iterations)
-    ev1.record(stream)
-    torch.cuda.synchronize()
-    barrier()
-    ck = clocks.stop()
-    ms = ev0.elapsed_time(ev1)
-    if world > 1:
-        import torch.distributed as dist
+    def solve_plain():
+        hist, info = plan.cgls(b, x, MAXIT, TOL, stream=stream)
+        return info
 
-        t = torch.tensor([ms], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms = float(t.item())
-    ms_step = ms / args.steps
-    value = world * NY / (ms_step / 1e3)
-    n_it = int(statistics.median(iters))
-    rel_final = float(hist[-1]) if len(hist) else None
+    def solve_warm():
+        _, sinfo = plan.sirt(b, x, lam, SIRT_ITERS, 0.0, stream=stream)
+        net.warm_start(plan, x, x, scratch[0], scratch[1], stream=stream)
+        hist, info = plan.cgls(b, x, MAXIT, TOL, warm=True, rnorm_ref=sinfo.rnorm0,
+                               stream=stream)
+        return info
 
-    # Kernel roofline: forward and back projector timed alone on this stream.
-    q = torch.zeros(plan.nangles, plan.nx, plan.ys, dtype=torch.float32, device="cuda")
-    gg = torch.zeros_like(x)
-    kt = {}
-    for name, fn in (("fp", lambda: plan.project(x, q, stream=stream)),
-                     ("bp", lambda: plan.backproject(b, gg, stream=stream))):
-        fn()
+    solve = solve_warm if net is not None else solve_plain
+
+    def timed(fn, steps):
+        iters = []
+        barrier()
         torch.cuda.synchronize()
-        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
         e0.record(stream)
-        for _ in range(3):
-            fn()
+        for _ in range(steps):
+            iters.append(fn().iterations)
         e1.record(stream)
         torch.cuda.synchronize()
-        kt[name] = e0.elapsed_time(e1) / 3 / 1e3
-    del q, gg
+        barrier()
+        ms = e0.elapsed_time(e1)
+        if world > 1:
+            import torch.distributed as dist
+
+            t = torch.tensor([ms], device="cuda")
+            dist.all_reduce(t, op=dist.ReduceOp.MAX)
+            ms = float(t.item())
+        return ms / steps, iters
+
+    for _ in range(args.warmup):
+        info = solve()
+    # timed region: the headline pipeline, with projector timing and clocks
+    clocks = ClockSampler(local)
+    clocks.start()
+    plan.timing(1)
+    n0 = gb.launch_count()
+    ms_step, iters = timed(solve, args.steps)
+    launches = gb.launch_count() - n0
+    fp_ms, fp_calls, bp_ms, bp_calls = plan.timing(0)
+    ck = clocks.stop()
+    value = world * NY / (ms_step / 1e3)
+    n_it = int(statistics.median(iters))
+    rel_final = float(info.rel_final)
+
+    # plain CGLS beside it (the comparison the metric names), same data
+    plain = None
+    if net is not None:
+        solve_plain()
+        pm, pit = timed(solve_plain, max(1, min(args.steps, 2)))
+        plain = {"slices_per_s": world * NY / (pm / 1e3), "ms_per_solve": pm,
+                 "iterations": int(statistics.median(pit))}
+
+    # Roofline of the dominant kernel from the projector times recorded in the
+    # timed region.  Unit: one projection (the forward projector is 32 band
+    # launches; per-launch figures divide both bytes and time by the same count).
     vol_b = plan.nrays * NY * 4
     sin_b = NA * NX * NY * 4
-    fp_bytes = vol_b + sin_b           # read x, write q
-    fp_flops = 2 * 3 * plan.nrays * NY * NA
+    algo_bytes = vol_b + sin_b            # compulsory: read x (s), write q (g)
+    flops = 2 * 3 * plan.nrays * NY * NA  # 3 taps per (ray, angle, slice)
+    fp_avg = fp_ms / max(fp_calls, 1) / 1e3
+    bp_avg = bp_ms / max(bp_calls, 1) / 1e3
+    dom = "fp" if fp_ms >= bp_ms else "bp"
+    t_dom = fp_avg if dom == "fp" else bp_avg
     peak, peak_kind = peaks()
-    dom = "fp" if kt["fp"] >= kt["bp"] else "bp"
-    achieved = fp_bytes / kt[dom] / 1e9
-    traffic = profiled_traffic().get(dom)
+    achieved = algo_bytes / t_dom / 1e9
     sm = ck.get("sm_mhz") or 1900.0
     props = torch.cuda.get_device_properties(local)
     fp32_peak = props.multi_processor_count * 128 * 2 * sm * 1e6 / 1e12
+    traffic = profiled_traffic().get(dom)
     roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
-                "frac": achieved / peak, "traffic": traffic, "kernel": dom,
+                "frac": achieved / peak, "traffic": traffic,
+                "kernel": "fp_band_kernel (one forward projection)" if dom == "fp"
+                else "bp_kernel (one back projection)",
                 "peak_source": peak_kind,
-                "fp32": {"achieved_tflops": fp_flops / kt[dom] / 1e12,
+                "algorithmic_bytes_per_projection": algo_bytes,
+                "fp32": {"achieved_tflops": flops / t_dom / 1e12,
                          "peak_tflops_at_median_clock": fp32_peak,
-                         "frac": fp_flops / kt[dom] / 1e12 / fp32_peak},
-                "fp_ms": kt["fp"] * 1e3, "bp_ms": kt["bp"] * 1e3}
+                         "frac": flops / t_dom / 1e12 / fp32_peak},
+                "fp_ms": fp_avg * 1e3, "bp_ms": bp_avg * 1e3,
+                "fp_calls": fp_calls, "bp_calls": bp_calls,
+                "projector_share_of_step": (fp_ms + bp_ms) / (ms_step * args.steps)}
 
-    # End to end through the reference-compatible entry point (host buffers).
+    # End to end through the C ABI over pinned host buffers: the reference
+    # layout sinogram goes up, the reconstruction comes back, every step.
     e2e = None
     if not args.no_e2e:
+        L = gb.lib()
         b_host = torch.empty(NA, NY, NX, dtype=torch.float32, pin_memory=True)
         b_host.copy_(b[:, :, :NY].permute(0, 2, 1))
-        x_host = torch.empty(plan.nrays, NY, dtype=torch.float32, pin_memory=True)
-        L = gb.lib()
-        img = gb.ArecImage()
-        img.nz, img.ny, img.nx = NA, NY, NX
-        img.is_cyl = 0
-        img.data = C.cast(C.c_void_p(b_host.data_ptr()), C.POINTER(C.c_float))
-        ang = np.ascontiguousarray(angles)
+        x_host = torch.empty(plan.nrays, plan.ys, dtype=torch.float32, pin_memory=True)
+        b_ref = torch.empty(NA, NY, NX, dtype=torch.float32, device="cuda")
+        b_dev = torch.empty_like(b)
+        x_dev = torch.zeros_like(x)
 
         def e2e_step():
-            vol = gb.ArecImage()
-            vol.data = C.cast(C.c_void_p(x_host.data_ptr()), C.POINTER(C.c_float))
-            # a non-NULL data pointer warm-starts; pass zeros -> identical to a cold start
-            x_host.zero_()
-            vol.nx = vol.nz = NX
-            vol.ny = vol.height = NY
-            vol.radius = 0.5 * (NX - 1)
-            vol.nrays = plan.nrays
-            vol.nnz = plan.nrays * NY
-            vol.is_cyl = 1
-            st = L.arecgb_cyl_cgls_SQ(0, img, gb._f32p(ang), C.byref(vol), 0.0, MAXIT, TOL)
-            assert st == 0, st
+            b_ref.copy_(b_host, non_blocking=True)
+            plan.sino_from_reference(b_ref, b_dev, stream=stream)
+            if net is not None:
+                _, sinfo = plan.sirt(b_dev, x_dev, lam, SIRT_ITERS, 0.0, stream=stream)
+                net.warm_start(plan, x_dev, x_dev, scratch[0], scratch[1], stream=stream)
+                plan.cgls(b_dev, x_dev, MAXIT, TOL, warm=True, rnorm_ref=sinfo.rnorm0,
+                          stream=stream)
+            else:
+                plan.cgls(b_dev, x_dev, MAXIT, TOL, stream=stream)
+            x_host.copy_(x_dev, non_blocking=True)
+            torch.cuda.synchronize()
 
-        e2e_step()  # plan cache
-        t0 = time.perf_counter()
+        e2e_step()
         n_e2e = max(1, min(args.steps, 2))
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
         for _ in range(n_e2e):
             e2e_step()
         dt = (time.perf_counter() - t0) / n_e2e
-        e2e = {"value": world * NY / dt, "unit": "slices/s", "h2d_bytes_per_step": NA * NY * NX * 4,
-               "d2h_bytes_per_step": plan.nrays * NY * 4, "ms_per_step": dt * 1e3,
-               "note": "cyl_cgls_SQ over pinned host arecImage buffers; zero warm start; "
-                       "reference stopping rule (equals the fixed denominator from zero)"}
+        e2e = {"value": world * NY / dt, "unit": "slices/s",
+               "h2d_bytes_per_step": NA * NY * NX * 4,
+               "d2h_bytes_per_step": plan.nrays * plan.ys * 4, "ms_per_step": dt * 1e3,
+               "path": "pinned host sinogram [angle][slice][bin] -> arecgb_sino_from_reference "
+                       "-> " + ("arecgb_sirt -> arecgb_warm_start -> arecgb_cgls" if net is not None
+                                else "arecgb_cgls") + " -> pinned host volume"}
 
     cpu = None
     if rank == 0 and not args.no_cpu:
-        per, info = cpu_sample(slices=16, iters=1)
-        cpu_solve = per * NY * (1 + 2 * n_it)
-        cpu = {"value": NY / cpu_solve, "unit": "slices/s", "cores": info["threads"],
+        n_cpu_it = plain["iterations"] if plain else n_it
+        per, cinfo = cpu_sample(slices=16, iters=1)
+        cpu_solve = per * NY * (1 + 2 * n_cpu_it)
+        cpu = {"value": NY / cpu_solve, "unit": "slices/s", "cores": cinfo["threads"],
                "kind": "port",
                "sample": "oracle C restatement of cyl_cgls_SQ: %d slices x 1 iteration on the "
                          "benchmark geometry (%.1f s, %d threads), extrapolated linearly to 512 "
-                         "slices x %d iterations" % (info["slices"], info["seconds"],
-                                                    info["threads"], n_it)}
+                         "slices x %d iterations (plain CGLS to 1e-3)"
+                         % (cinfo["slices"], cinfo["seconds"], cinfo["threads"], n_cpu_it)}
 
     if rank == 0:
+        cfg = dict(CONFIG, iterations=n_it, rel_final=rel_final,
+                   parallelism="replicas" if world > 1 else "single")
+        if net is not None:
+            cfg.update(warm_start=True, sirt_iters=SIRT_ITERS,
+                       workload="learned warm start: SIRT-%d -> BF16 U-Net -> CGLS to "
+                                "||A^T r||/||A^T b|| <= 1e-3 (max 200 it), square-pixel "
+                                "projector, 1024^2 x 512 slices, 1200 angles over [0,180), "
+                                "random-sphere cylinder r=500 px with 200 spheres, Poisson 5e3 "
+                                "photons" % SIRT_ITERS,
+                       plain_cgls=plain,
+                       speedup_vs_plain=(value / plain["slices_per_s"]) if plain else None,
+                       weights=os.path.relpath(args.weights, ROOT),
+                       weights_meta={k: meta.get(k) for k in ("sets", "steps", "final_loss")})
         out = {"metric": METRIC, "value": value, "unit": "slices/s", "n_gpus": world,
                "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_step,
                "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
                "dtype": "f32", "data": "synthetic (seeded sphere cylinder, analytic chords, "
                                        "Poisson 5e3)",
-               "config": dict(CONFIG, iterations=n_it, rel_final=rel_final,
-                              parallelism="replicas" if world > 1 else "single"),
-               "clocks": ck, "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e,
-               "gpu_launches": None}
-        # own kernels per step: per iteration 7 vector/scalar + 2 projectors + 2 reductions
-        out["gpu_launches"] = args.steps * (n_it * 11 + 4)
+               "config": cfg, "clocks": ck, "roofline": roofline, "cpu_baseline": cpu,
+               "e2e": e2e, "gpu_launches": launches}
         print(json.dumps(out))
     if world > 1:
         import torch.distributed as dist

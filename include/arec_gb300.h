@@ -97,6 +97,18 @@ int arecgb_sino_from_reference(const float *d_ref, float *d_dev, int na, int ny,
 int arecgb_sino_to_reference(const float *d_dev, float *d_ref, int na, int ny, int nx, int ys,
                              void *stream);
 
+/* Projector timing for measurement: mode 1 resets and starts recording a
+ * CUDA event pair around every forward and back projection of this plan (on
+ * the stream it runs on); mode 2 reports the summed device time and call
+ * counts so far; mode 0 reports and stops.  Reporting synchronises with the
+ * last recorded event.  No counterpart in the reference. */
+int arecgb_plan_timing(arecgb_plan *plan, int mode, double *fp_ms, long long *fp_calls,
+                       double *bp_ms, long long *bp_calls);
+
+/* Kernel launches issued by this library so far (all threads, approximate
+ * only in that concurrent callers interleave). */
+long long arecgb_launch_count(void);
+
 /* Cross-correlation shift search over nz image pairs of ny x nx floats, device
  * memory, reference layout [nz][ny][nx] (replaces the loop of arecCCImages,
  * AREC3D/AREC3D/arecImage.cpp:414-428: ccorr2d + speak per pair).

@@ -1,0 +1,64 @@
+"""What the trained warm-start network gains over the method without it.
+
+A seeded problem the network never saw (its own phantom seed) with the shapes
+of the learned-warm-start configuration (512^2 slices, 360 angles, 512
+detector bins, Poisson noise at 1e4 photons): plain CGLS from zero against
+SIRT-10 -> U-Net -> CGLS, both to ||A^T r|| / ||A^T b|| <= 1e-3.  The gain is
+CGLS iterations saved.  Both GPU results are then checked in FP64 with the
+oracle's projectors: their normal-equation residual, recomputed in double, must
+be within the tolerance the GPU solver reported meeting (RESID_SLACK allows for
+the GPU evaluating the same quantity in FP32)."""
+import os
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+TOL = 1e-3
+RESID_SLACK = 1.05
+SLICES = 4
+
+
+def _fp64_relative_residual(oc, radius, b_ref, x, ang):
+    """||A^T (b - A x)|| / ||A^T b|| in FP64 (oracle projectors, SQ weighting)."""
+    atb = oc.backproject64(3, radius, b_ref, ang)
+    r = b_ref - oc.project64(3, radius, x, ang)
+    return float(np.linalg.norm(oc.backproject64(3, radius, r, ang)) / np.linalg.norm(atb))
+
+
+def test_warm_start_saves_iterations(gb, oc):
+    import torch
+
+    from arec3d_gb300 import warmstart as ws
+
+    assert os.path.exists(ws.DEFAULT_WEIGHTS), "trained weights missing: " + ws.DEFAULT_WEIGHTS
+    nx, na = 512, 360
+    plan, b = ws.make_problem(gb, nx, na, SLICES, 1e4, 777001, "sphere")
+    net, meta = ws.load(gb, ws.DEFAULT_WEIGHTS, ws.pad8(plan.nx), SLICES)
+
+    x_plain = torch.zeros(plan.nrays, plan.ys, device="cuda")
+    info_plain, _ = ws.solve(gb, plan, b, x_plain, net=None, tol=TOL)
+    x_warm = torch.zeros_like(x_plain)
+    info_warm, stages = ws.solve(gb, plan, b, x_warm, net=net, tol=TOL)
+    saved = info_plain.iterations - info_warm.iterations
+    print("warm start %dx%d, %d angles: CGLS iterations plain %d, warm %d (saved %d); "
+          "SIRT %.3fs U-Net %.3fs CGLS %.3fs" % (nx, nx, na, info_plain.iterations,
+                                                info_warm.iterations, saved, stages["sirt"],
+                                                stages["unet"], stages["cgls"]))
+    assert info_plain.rel_final <= TOL and info_warm.rel_final <= TOL
+    assert saved > 0
+
+    # FP64 check of both results (reference layout [angle][slice][bin])
+    b_ref = b[:, :, :SLICES].permute(0, 2, 1).contiguous().double().cpu().numpy()
+    ang = plan.angles
+    radius = 0.5 * (nx - 1)
+    for name, xd in (("plain", x_plain), ("warm", x_warm)):
+        x = xd[:, :SLICES].double().cpu().numpy()
+        rel = _fp64_relative_residual(oc, radius, b_ref, x, ang)
+        print("%s: FP64 relative normal-equation residual %.3e" % (name, rel))
+        assert rel <= TOL * RESID_SLACK
+    # the two answers agree to the precision a 1e-3 residual implies
+    d = (np.linalg.norm((x_warm - x_plain)[:, :SLICES].double().cpu().numpy()) /
+         np.linalg.norm(x_plain[:, :SLICES].double().cpu().numpy()))
+    print("warm vs plain solution: relative difference %.3e" % d)
