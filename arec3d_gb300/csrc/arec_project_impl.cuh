@@ -194,28 +194,37 @@ __device__ __forceinline__ void cp_async_wait() {
 constexpr int kBpAngles = 32;  // angles per weight chunk
 constexpr int kBpFoot = 16;    // staged footprint width in bins (an 8x4 tile spans <= 12)
 
+constexpr int kBpBuf = 3;  // footprint buffers in flight
+
 template <int VEC, int NSC>
 constexpr size_t bp_smem_bytes() {
-    return sizeof(float4) * kBpAngles * 32 + sizeof(int) * kBpAngles +
-           sizeof(float) * 2 * kBpFoot * (NSC * 32 * VEC) + sizeof(double) * 4 * NSC;
+    return sizeof(float) * kBpBuf * kBpFoot * (NSC * 32 * VEC) + sizeof(float4) * kBpAngles * 32 +
+           sizeof(int) * kBpAngles + sizeof(double) * (4 * NSC + 1);
 }
 
-// Square-pixel and Kaiser-Bessel weightings: the footprint of the tile at each
-// angle (<= 12 bins x the block's slices) is staged in shared memory with
-// double-buffered cp.async (bins outside the detector read as zero, which is
-// what skipping them gives), so the accumulation reads only shared memory.
+// Square-pixel and Kaiser-Bessel weightings.  Block = 4*NSC accumulating warps
+// (8 rays x 32*VEC slices each) + 1 staging warp.  Per chunk of 32 angles the
+// weights of the tile's 32 rays are computed once (lanes = rays) into shared
+// memory; then the staging warp copies the footprint of each angle (<= 16 bins,
+// each a contiguous row of the block's slices) with one bulk copy per bin
+// (cp.async.bulk) into one of three buffers, two angles ahead, completing on
+// the buffer's "full" mbarrier, and the accumulating warps release buffers on
+// its "empty" mbarrier: no block-wide barrier per angle.  Bins off the detector
+// are not copied and their taps are skipped, as the reference skips them.
 template <int W, int VEC, int NSC>
-__global__ void __launch_bounds__(128 * NSC)
+__global__ void __launch_bounds__(128 * NSC + 32)
     bp_kernel(OpArgs A, const float *__restrict__ s, float *__restrict__ g) {
-    constexpr int NT = 128 * NSC, NWARP = NT / 32, AC = kBpAngles, FW = kBpFoot;
+    constexpr int NCW = 4 * NSC, AC = kBpAngles, FW = kBpFoot, NB = kBpBuf;
     constexpr int SPAN = NSC * 32 * VEC;  // slices per block
-    extern __shared__ __align__(16) unsigned char smem_raw[];
-    float4 *sw = reinterpret_cast<float4 *>(smem_raw);              // [AC][32]
+    extern __shared__ __align__(128) unsigned char smem_raw[];
+    __shared__ __align__(8) uint64_t full[NB], empty[NB];
+    float *foot = reinterpret_cast<float *>(smem_raw);               // [NB][FW][SPAN]
+    float4 *sw = reinterpret_cast<float4 *>(foot + NB * FW * SPAN);  // [AC][32]
     int *fb = reinterpret_cast<int *>(sw + AC * 32);                 // [AC]
-    float *foot = reinterpret_cast<float *>(fb + AC);                // [2][FW][SPAN]
-    double *red = reinterpret_cast<double *>(foot + 2 * FW * SPAN);  // [NWARP]
+    double *red = reinterpret_cast<double *>(fb + AC);               // [NCW + 1]
     if (A.skip && *A.skip) return;
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const bool stager = warp == NCW;
     const int2 tile = A.tiles[blockIdx.x];
     const int ix = tile.x + (lane & (kTileX - 1)), iz = tile.y + lane / kTileX;
     int k = -1;
@@ -227,8 +236,17 @@ __global__ void __launch_bounds__(128 * NSC)
     const int rg = warp & 3, sc = warp >> 2;
     const int yb = blockIdx.y * SPAN;                  // first slice of the block
     const int yw = sc * 32 * VEC;                        // this warp's slices within the block
-    const bool yok = yb + yw + lane_piece<VEC>(lane, 0) < A.ys;
+    const bool yok = !stager && yb + yw + lane_piece<VEC>(lane, 0) < A.ys;
     const size_t ys = (size_t)A.ys;
+    const uint32_t row_bytes = (uint32_t)min(SPAN, A.ys - yb) * 4u;
+    if (threadIdx.x == 0) {
+#pragma unroll
+        for (int b = 0; b < NB; b++) {
+            umma::mbar_init(&full[b], 1);
+            umma::mbar_init(&empty[b], NCW);
+        }
+        umma::mbar_fence_init();
+    }
 
     float acc[8][VEC];
 #pragma unroll
@@ -236,23 +254,11 @@ __global__ void __launch_bounds__(128 * NSC)
 #pragma unroll
         for (int q = 0; q < VEC; q++) acc[r][q] = 0.f;
 
-    // stage the footprint of angle a0+ai into buffer buf
-    auto stage = [&](int a0, int ai, int buf) {
-        const int a = a0 + ai, b0 = fb[ai];
-        float *dst = foot + (size_t)buf * FW * SPAN;
-        constexpr int CHUNKS = FW * SPAN / 4;  // 16-byte pieces
-        for (int c = threadIdx.x; c < CHUNKS; c += NT) {
-            const int f = c / (SPAN / 4), col = (c % (SPAN / 4)) * 4;
-            const int bin = b0 + f, y = yb + col;
-            const bool ok = (unsigned)bin < (unsigned)A.nx && y < A.ys;
-            const float *src = s + ((size_t)a * A.nx + (ok ? bin : 0)) * ys + (ok ? y : 0);
-            cp_async16(dst + f * SPAN + col, src, ok);
-        }
-    };
-
+    bool ok = true;
+    int t0 = 0;  // angles staged before this chunk (buffer t % NB, use t / NB)
     for (int a0 = 0; a0 < A.na; a0 += AC) {
         const int nac = min(AC, A.na - a0);
-        for (int ai = warp; ai < AC; ai += NWARP) {
+        for (int ai = warp; ai < AC; ai += NCW + 1) {
             const int a = a0 + ai;
             float4 e = make_float4(__int_as_float(INT_MIN / 2), 0.f, 0.f, 0.f);
             int lo = INT_MAX, hi = INT_MIN;
@@ -271,48 +277,79 @@ __global__ void __launch_bounds__(128 * NSC)
                 fb[ai] = lo == INT_MAX ? 0 : lo;
             }
         }
-        __syncthreads();
-        stage(a0, 0, 0);
-        cp_async_commit();
-        for (int ai = 0; ai < nac; ai++) {
-            if (ai + 1 < nac) stage(a0, ai + 1, (ai + 1) & 1);
-            cp_async_commit();
-            cp_async_wait<1>();
-            __syncthreads();
-            if (yok) {
-                const float *F = foot + (size_t)(ai & 1) * FW * SPAN + yw;
-                const int fb0 = fb[ai];
+        __syncthreads();  // weights and footprint bases of this chunk (barriers initialised)
+        if (stager) {
+            for (int ai = 0; ai < nac; ai++) {
+                const int t = t0 + ai, buf = t % NB;
+                if (t >= NB && ok &&
+                    !umma::mbar_wait(&empty[buf], (uint32_t)(t / NB - 1) & 1u, kFpWait)) {
+                    ok = false;
+                    if (lane == 0) atomicOr(A.err, 16);
+                }
+                const int bin = fb[ai] + lane;
+                const bool on = ok && lane < FW && (unsigned)bin < (unsigned)A.nx;
+                const unsigned m = __ballot_sync(0xffffffffu, on);
+                if (lane == 0) umma::mbar_arrive_expect_tx(&full[buf], (uint32_t)__popc(m) * row_bytes);
+                __syncwarp();
+                if (on)
+                    umma::bulk_g2s(foot + ((size_t)buf * FW + lane) * SPAN,
+                                   s + ((size_t)(a0 + ai) * A.nx + bin) * ys + yb, row_bytes,
+                                   &full[buf]);
+            }
+        } else {
+            for (int ai = 0; ai < nac; ai++) {
+                const int t = t0 + ai, buf = t % NB;
+                if (ok && !umma::mbar_wait(&full[buf], (uint32_t)(t / NB) & 1u, kFpWait)) {
+                    ok = false;
+                    if (lane == 0) atomicOr(A.err, 16);
+                }
+                if (ok && yok) {
+                    const float *F = foot + (size_t)buf * FW * SPAN + yw;
+                    const int fb0 = fb[ai];
 #pragma unroll
-                for (int r = 0; r < 8; r++) {
-                    const float4 e = sw[ai * 32 + rg * 8 + r];
-                    const int rb = __float_as_int(e.x) - fb0;
-                    if (rb >= 0 && rb <= FW - 3) {
+                    for (int r = 0; r < 8; r++) {
+                        const float4 e = sw[ai * 32 + rg * 8 + r];
+                        const int b = __float_as_int(e.x), rb = b - fb0;
+                        if (rb >= 0 && rb <= FW - 3) {
 #pragma unroll
-                        for (int j = 0; j < 3; j++) {
-                            const float w = j == 0 ? e.y : (j == 1 ? e.z : e.w);
-                            float v[VEC];
-                            lds_lane<VEC>(F + (rb + j) * SPAN, lane, v);
+                            for (int j = 0; j < 3; j++) {
+                                if ((unsigned)(b + j) < (unsigned)A.nx) {
+                                    const float w = j == 0 ? e.y : (j == 1 ? e.z : e.w);
+                                    float v[VEC];
+                                    lds_lane<VEC>(F + (rb + j) * SPAN, lane, v);
 #pragma unroll
-                            for (int q = 0; q < VEC; q++) acc[r][q] = fmaf(w, v[q], acc[r][q]);
+                                    for (int q = 0; q < VEC; q++) acc[r][q] = fmaf(w, v[q], acc[r][q]);
+                                }
+                            }
                         }
                     }
                 }
+                __syncwarp();
+                if (lane == 0) umma::mbar_arrive(&empty[buf]);
             }
-            __syncthreads();
         }
+        t0 += nac;
+        __syncthreads();  // the chunk's weights are no longer read
+    }
+    if (!ok && !stager) {
+        // a wait gave up: let the copies still in flight land before the block exits
+        for (int t = max(0, t0 - NB); t < t0; t++)
+            umma::mbar_wait(&full[t % NB], (uint32_t)(t / NB) & 1u, kFpWait);
     }
 
     double s2 = 0.0;
+    if (!stager) {
 #pragma unroll
-    for (int r = 0; r < 8; r++) {
-        const int kr = __shfl_sync(0xffffffffu, k, rg * 8 + r);
-        if (kr >= 0 && yok) {
-            stg_lane<VEC>(g + (size_t)kr * ys + yb + yw, lane, acc[r], A.ys - (yb + yw));
+        for (int r = 0; r < 8; r++) {
+            const int kr = __shfl_sync(0xffffffffu, k, rg * 8 + r);
+            if (kr >= 0 && yok) {
+                stg_lane<VEC>(g + (size_t)kr * ys + yb + yw, lane, acc[r], A.ys - (yb + yw));
 #pragma unroll
-            for (int q = 0; q < VEC; q++) s2 += (double)__fmul_rn(acc[r][q], acc[r][q]);
+                for (int q = 0; q < VEC; q++) s2 += (double)__fmul_rn(acc[r][q], acc[r][q]);
+            }
         }
     }
-    block_sum_to<NWARP>(s2, red, A.partials + (size_t)blockIdx.y * gridDim.x + blockIdx.x);
+    block_sum_to<NCW + 1>(s2, red, A.partials + (size_t)blockIdx.y * gridDim.x + blockIdx.x);
 }
 
 // Linear weighting: its ray coordinates are the reference's shifted table
@@ -457,44 +494,50 @@ __device__ __forceinline__ int line_pixel_ray(const OpArgs &A, int orient, int l
 // ---------------------------------------------------------------------------
 // Banded forward projection (square-pixel and Kaiser-Bessel weightings).
 //
-// The same gather as fp_kernel, split by line bands: one launch takes the
-// angle groups of one sweep orientation and the lines [band_lo, band_hi) of
-// their strips (rows for orientation 0, columns for 1), and ADDS its partial
-// sums to q, which is zeroed first.  All blocks of a launch then read x from one
-// band of the cylinder (band lines x nx pixels x the block's slices: 64 MB for
-// 64 lines of 1024 pixels and 256 slices), which stays in L2, instead of
-// every angle group streaming the whole volume from DRAM.  Launches run in a
-// fixed order on one stream, so the result does not depend on timing.
+// One launch takes the angle groups of one sweep orientation and the lines
+// [band_lo, band_hi) of their strips (rows for orientation 0, columns for 1),
+// and ADDS its partial sums to q, which is zeroed first.  All blocks of a
+// launch then read x from one band of the cylinder (band lines x nx pixels x
+// the block's slices: 64 MB for 64 lines of 1024 pixels and 256 slices), which
+// stays in L2, instead of every angle group streaming the whole volume from
+// DRAM.  Launches run in a fixed order on one stream, so the result does not
+// depend on timing.
 //
-// Per line, warp 0 stages the union of the group's candidate rows with one
-// bulk copy per row (cp.async.bulk, completing on the buffer's mbarrier), one
-// line ahead; every warp computes its angle's weights for the staged rows
-// (lanes = rows, ordered by increasing centre bin), compacts the rows whose
-// centre bin falls in the tile (a contiguous run: the centre bin is monotonic
-// along a line; a counting sort covers any exception) and accumulates them
-// with the bucket index known at compile time.  One block barrier per line.
+// Block = 4 angle warps + 1 staging warp.  The staging warp runs up to two
+// lines ahead: per line it forms the union of the group's candidate pixels,
+// looks up their rays and stages their x rows with one bulk copy per row
+// (cp.async.bulk) into one of two buffers, completing on that buffer's "full"
+// mbarrier.  Each angle warp computes its weights for the staged rows (lanes =
+// rows, ordered by increasing centre bin), compacts the rows whose centre bin
+// falls in the tile (a contiguous run: the centre bin is monotonic along a
+// line; a counting sort covers any exception), accumulates them with the
+// bucket index known at compile time, and arrives on the buffer's "empty"
+// mbarrier.  No block-wide barrier inside the line loop; every wait is
+// bounded and a timeout sets an error flag.
 template <int VEC>
 constexpr size_t fpb_smem_bytes() {
     return sizeof(float) * 2 * kFpStage * (32 * VEC) + sizeof(float4) * kGroupAngles * 32 +
-           sizeof(int) * 2 * kFpStage + sizeof(int) * (2 * kGroupAngles + 4) +
-           sizeof(int) * kGroupAngles * (kFpBins + 3);
+           sizeof(int) * 2 * kFpStage + sizeof(int) * (2 * kGroupAngles + 4);
 }
 
+constexpr int kFpThreads = 32 * (kGroupAngles + 1);
+
 template <int W, int VEC, int BT>
-__global__ void __launch_bounds__(32 * kGroupAngles, 3)
+__global__ void __launch_bounds__(kFpThreads, 3)
     fp_band_kernel(OpArgs A, const float *__restrict__ x, float *__restrict__ q, int g0, int ngo,
                    int band_lo, int band_hi) {
     constexpr int NA = kGroupAngles, NG = BT + 2, SPAN = 32 * VEC, US = kFpStage;
     extern __shared__ __align__(128) unsigned char smem_raw[];
-    __shared__ __align__(8) uint64_t full[2];
+    __shared__ __align__(8) uint64_t full[2], empty[2];
     float *stg = reinterpret_cast<float *>(smem_raw);                // [2][US][SPAN]
     float4 *list = reinterpret_cast<float4 *>(stg + 2 * US * SPAN);  // [NA][32]
     int *rowk = reinterpret_cast<int *>(list + NA * 32);             // [2][US] ray of each row
     int *lrange = rowk + 2 * US;                                     // [NA][2]
     int *uinfo = lrange + 2 * NA;                                    // [2][2] (first pixel, rows)
-    int *base = uinfo + 4;                                           // [NA][NG+1] fallback sort
     if (A.skip && *A.skip) return;
-    const int ai = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const bool stager = warp == NA;
+    const int ai = stager ? 0 : warp;
     const int grp = g0 + blockIdx.x % ngo, b0 = (blockIdx.x / ngo) * BT;
     const int4 G = A.groups[grp];
     const int orient = G.z;
@@ -505,7 +548,7 @@ __global__ void __launch_bounds__(32 * kGroupAngles, 3)
     const int yb = blockIdx.y * SPAN;
     const size_t ys = (size_t)A.ys;
     const uint32_t row_bytes = (uint32_t)min(SPAN, A.ys - yb) * 4u;
-    const bool angle_ok = ai < G.y;
+    const bool angle_ok = !stager && ai < G.y;
     AngleParams ap;
     float ca = 1.f, cl = 0.f;
     if (angle_ok) {
@@ -513,7 +556,7 @@ __global__ void __launch_bounds__(32 * kGroupAngles, 3)
         ca = orient ? ap.s : ap.c;
         cl = orient ? ap.c : ap.s;
     }
-    if (lane == 0) {
+    if (!stager && lane == 0) {
         int lo = INT_MAX, hi = INT_MIN;
         float lmin, lmax;
         if (angle_ok && strip_line_extent(ca, cl, T1, T2, R, lmin, lmax)) {
@@ -526,6 +569,8 @@ __global__ void __launch_bounds__(32 * kGroupAngles, 3)
     if (threadIdx.x == 0) {
         umma::mbar_init(&full[0], 1);
         umma::mbar_init(&full[1], 1);
+        umma::mbar_init(&empty[0], NA);
+        umma::mbar_init(&empty[1], NA);
         umma::mbar_fence_init();
     }
     __syncthreads();
@@ -536,77 +581,86 @@ __global__ void __launch_bounds__(32 * kGroupAngles, 3)
         L1 = max(L1, lrange[2 * i + 1]);
     }
     if (L0 > L1) return;  // the strip misses this band (uniform over the block)
-    const int my_lo = lrange[2 * ai], my_hi = lrange[2 * ai + 1];
+    bool ok = true;
 
-    // warp 0, lanes < NA: the angles' sweep cosines for the candidate ranges
-    float cq = 1.f, lq = 0.f;
-    int q_lo = INT_MAX, q_hi = INT_MIN;
-    if (ai == 0 && lane < G.y) {
-        const AngleParams aq = A.ang[G.x + lane];
-        cq = orient ? aq.s : aq.c;
-        lq = orient ? aq.c : aq.s;
-        q_lo = lrange[2 * lane];
-        q_hi = lrange[2 * lane + 1];
-    }
-    // warp 0: stage the union of the group's candidate pixels on line li
-    auto stage = [&](int li, int buf) {
-        int clo = INT_MAX, chi = INT_MIN;
-        if (lane < NA && li >= q_lo && li <= q_hi) {
-            line_candidates(A, orient, cq, lq, T1, T2, r, li, clo, chi);
-            if (clo > chi) {
-                clo = INT_MAX;
-                chi = INT_MIN;
+    if (stager) {
+        // lanes < NA: the angles' sweep cosines for the candidate ranges
+        float cq = 1.f, lq = 0.f;
+        int q_lo = INT_MAX, q_hi = INT_MIN;
+        if (lane < G.y) {
+            const AngleParams aq = A.ang[G.x + lane];
+            cq = orient ? aq.s : aq.c;
+            lq = orient ? aq.c : aq.s;
+            q_lo = lrange[2 * lane];
+            q_hi = lrange[2 * lane + 1];
+        }
+        for (int li = L0; li <= L1; li++) {
+            const int it = li - L0, buf = it & 1;
+            if (it >= 2 && ok &&
+                !umma::mbar_wait(&empty[buf], (uint32_t)((it - 2) >> 1) & 1u, kFpWait)) {
+                ok = false;
+                if (lane == 0) atomicOr(A.err, 16);
             }
-        }
+            int clo = INT_MAX, chi = INT_MIN;
+            if (lane < NA && li >= q_lo && li <= q_hi) {
+                line_candidates(A, orient, cq, lq, T1, T2, r, li, clo, chi);
+                if (clo > chi) {
+                    clo = INT_MAX;
+                    chi = INT_MIN;
+                }
+            }
 #pragma unroll
-        for (int o = 1; o < NA; o <<= 1) {
-            clo = min(clo, __shfl_xor_sync(0xffffffffu, clo, o));
-            chi = max(chi, __shfl_xor_sync(0xffffffffu, chi, o));
+            for (int o = 1; o < NA; o <<= 1) {
+                clo = min(clo, __shfl_xor_sync(0xffffffffu, clo, o));
+                chi = max(chi, __shfl_xor_sync(0xffffffffu, chi, o));
+            }
+            const int ulo = __shfl_sync(0xffffffffu, clo, 0);
+            const int uhi = __shfl_sync(0xffffffffu, chi, 0);
+            int n = uhi >= ulo ? uhi - ulo + 1 : 0;
+            if (n > US) {
+                if (lane == 0) atomicOr(A.err, 1);
+                n = US;
+            }
+            if (!ok) n = 0;  // a wait gave up: stage nothing more
+            int k = 0;
+            if (lane < n) {
+                k = line_pixel_ray(A, orient, li, ulo + lane);
+                rowk[buf * US + lane] = k;
+            }
+            __syncwarp();
+            if (lane == 0) {
+                uinfo[2 * buf] = ulo;
+                uinfo[2 * buf + 1] = n;
+                __threadfence_block();  // row table and counts before the arrival
+                umma::mbar_arrive_expect_tx(&full[buf], (uint32_t)n * row_bytes);
+            }
+            __syncwarp();
+            if (lane < n)
+                umma::bulk_g2s(stg + ((size_t)buf * US + lane) * SPAN, x + (size_t)k * ys + yb,
+                               row_bytes, &full[buf]);
         }
-        const int ulo = __shfl_sync(0xffffffffu, clo, 0), uhi = __shfl_sync(0xffffffffu, chi, 0);
-        int n = uhi >= ulo ? uhi - ulo + 1 : 0;
-        if (n > US) {
-            if (lane == 0) atomicOr(A.err, 1);
-            n = US;
-        }
-        int k = 0;
-        if (lane < n) {
-            k = line_pixel_ray(A, orient, li, ulo + lane);
-            rowk[buf * US + lane] = k;
-        }
-        if (lane == 0) {
-            uinfo[2 * buf] = ulo;
-            uinfo[2 * buf + 1] = n;
-            umma::mbar_arrive_expect_tx(&full[buf], (uint32_t)n * row_bytes);
-        }
-        __syncwarp();
-        if (lane < n)
-            umma::bulk_g2s(stg + ((size_t)buf * US + lane) * SPAN, x + (size_t)k * ys + yb,
-                           row_bytes, &full[buf]);
-    };
+        return;
+    }
 
+    const int my_lo = lrange[2 * ai], my_hi = lrange[2 * ai + 1];
     float acc[BT][VEC];
 #pragma unroll
     for (int j = 0; j < BT; j++)
 #pragma unroll
         for (int v = 0; v < VEC; v++) acc[j][v] = 0.f;
 
-    if (ai == 0) stage(L0, 0);
-    __syncthreads();
-    bool ok = true;
     for (int li = L0; li <= L1; li++) {
         const int it = li - L0, buf = it & 1;
-        if (ai == 0 && li + 1 <= L1) stage(li + 1, buf ^ 1);
-        const int un = uinfo[2 * buf + 1];
         if (ok && !umma::mbar_wait(&full[buf], (uint32_t)(it >> 1) & 1u, kFpWait)) {
             ok = false;
-            atomicOr(A.err, 16);
+            if (lane == 0) atomicOr(A.err, 16);
         }
+        const int un = ok ? uinfo[2 * buf + 1] : 0;
         // Phase A: lanes = staged rows in increasing centre-bin order for this angle.
         bool valid = false;
         int gk = 0;
         float4 ent = make_float4(0.f, 0.f, 0.f, 0.f);
-        if (ok && angle_ok && lane < un && li >= my_lo && li <= my_hi) {
+        if (angle_ok && lane < un && li >= my_lo && li <= my_hi) {
             const int row = ca > 0.f ? lane : un - 1 - lane;
             const int k = rowk[buf * US + row];
             const Taps t = ray_taps<W>(A.ray[k], ap, A.r_hi, A.r_lo);
@@ -637,18 +691,26 @@ __global__ void __launch_bounds__(32 * kGroupAngles, 3)
             if (valid) list[ai * 32 + mybase + rank] = ent;
         }
         __syncwarp();
-        // Phase C: entries in bucket order; the bucket index is a compile-time constant.
+        // Phase C: entries in bucket order; the bucket index is a compile-time
+        // constant.  The next entry's slices are loaded before this entry's FMAs.
         if (cnt) {
             const float *S = stg + (size_t)buf * US * SPAN;
+            const float4 *E = list + ai * 32;
+            float4 e = E[0];
+            float v[VEC];
+            lds_lane<VEC>(S + (__float_as_int(e.x) & 255) * SPAN, lane, v);
             int i = 0;
 #pragma unroll
             for (int gg = 0; gg < NG; gg++) {
-                while (i < cnt) {
-                    const float4 e = list[ai * 32 + i];
-                    const int key = __float_as_int(e.x);
-                    if ((key >> 8) != gg) break;
-                    float v[VEC];
-                    lds_lane<VEC>(S + (key & 255) * SPAN, lane, v);
+                while (i < cnt && (__float_as_int(e.x) >> 8) == gg) {
+                    float4 en = e;
+                    float vn[VEC];
+#pragma unroll
+                    for (int c = 0; c < VEC; c++) vn[c] = 0.f;
+                    if (i + 1 < cnt) {
+                        en = E[i + 1];
+                        lds_lane<VEC>(S + (__float_as_int(en.x) & 255) * SPAN, lane, vn);
+                    }
                     if (gg >= 2) {
 #pragma unroll
                         for (int c = 0; c < VEC; c++) acc[gg >= 2 ? gg - 2 : 0][c] =
@@ -664,11 +726,15 @@ __global__ void __launch_bounds__(32 * kGroupAngles, 3)
                         for (int c = 0; c < VEC; c++) acc[gg <= BT - 1 ? gg : 0][c] =
                             fmaf(e.w, v[c], acc[gg <= BT - 1 ? gg : 0][c]);
                     }
+                    e = en;
+#pragma unroll
+                    for (int c = 0; c < VEC; c++) v[c] = vn[c];
                     i++;
                 }
             }
         }
-        __syncthreads();  // buffer, row table and lists free for the next lines
+        __syncwarp();  // this warp's reads of the buffer and of its list are done
+        if (lane == 0) umma::mbar_arrive(&empty[buf]);
     }
     if (!ok) {
         // a wait gave up: let the copies still in flight land before the block exits
@@ -735,7 +801,7 @@ int launch_bp_one(const OpArgs &A, dim3 grid, const float *s, float *g, cudaStre
                 return -2;
             configured = true;
         }
-        bp_kernel<W, V, N><<<grid, 128 * N, smem, st>>>(A, s, g);
+        bp_kernel<W, V, N><<<grid, 128 * N + 32, smem, st>>>(A, s, g);
     }
     return 0;
 }
@@ -762,7 +828,7 @@ int launch_fpb_one(const OpArgs &A, dim3 grid, const float *x, float *q, int g0,
             return -2;
         configured = true;
     }
-    fp_band_kernel<W, V, BT><<<grid, 32 * kGroupAngles, smem, st>>>(A, x, q, g0, ngo, lo, hi);
+    fp_band_kernel<W, V, BT><<<grid, kFpThreads, smem, st>>>(A, x, q, g0, ngo, lo, hi);
     return 0;
 }
 

@@ -120,6 +120,11 @@ __device__ __forceinline__ bool mbar_wait(uint64_t *mbar, uint32_t parity, uint3
     return false;
 }
 
+// Plain arrival (release semantics) on an mbarrier.
+__device__ __forceinline__ void mbar_arrive(uint64_t *mbar) {
+    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];\n" ::"r"(smem_addr(mbar)) : "memory");
+}
+
 // Arrive on an mbarrier and add `bytes` to the transaction count the phase
 // waits for (the bulk copies below complete it).
 __device__ __forceinline__ void mbar_arrive_expect_tx(uint64_t *mbar, uint32_t bytes) {
