@@ -74,6 +74,9 @@ def lib():
             getattr(L, n).argtypes = [vp, vp, C.c_int, C.c_int, C.c_int, C.c_int, vp]
         L.arecgb_cc_shifts.argtypes = [vp, vp, C.c_int, C.c_int, C.c_int, vp, vp, vp, vp, vp]
         L.arecgb_ccorr2d_device.argtypes = [vp, vp, vp, C.c_int, C.c_int, vp]
+        L.arecgb_fshift2d_device.argtypes = [vp, vp, C.c_int, C.c_int, C.c_int, vp, vp, vp]
+        L.arecgb_fshift2d.argtypes = [C.c_int, C.c_int, fp, fp, C.c_float, C.c_float]
+        L.arecgb_fshift2d.restype = None
         L.arecgb_cc_shifts_static.argtypes = [vp, vp, C.c_int, C.c_int, C.c_int, vp, vp, vp, vp,
                                               vp]
         img, pimg = ArecImage, C.POINTER(ArecImage)
@@ -83,7 +86,7 @@ def lib():
             f.argtypes = [img, fp, C.c_int, pimg]
             f.restype = C.c_int
         for n in ("cyl_sirt", "cyl_sirt_KB", "cyl_sirt_SQ", "cyl_cgls", "cyl_cgls_KB",
-                  "cyl_cgls_SQ"):
+                  "cyl_cgls_SQ", "cyl_cgls_stat", "cyl_cgls_KB_stat", "cyl_cgls_SQ_stat"):
             f = getattr(L, "arecgb_" + n)
             f.argtypes = [C.c_int, img, fp, pimg, C.c_float, C.c_int, C.c_float]
             f.restype = C.c_int
@@ -122,6 +125,12 @@ def lib():
         L.arecgb_plan_timing.argtypes = [vp, C.c_int, dp, C.POINTER(C.c_longlong), dp,
                                          C.POINTER(C.c_longlong)]
         L.arecgb_launch_count.restype = C.c_longlong
+        L.arecgb_plan_autotune.argtypes = [vp, vp, vp, ip, ip, vp]
+        L.arecgb_cgls_stat.argtypes = [vp, vp, vp, C.c_int, C.c_int, C.c_float, dp,
+                                       C.POINTER(SolveInfo), vp]
+        L.arecgb_cgls_batch.argtypes = [C.POINTER(vp), C.POINTER(vp), C.POINTER(vp),
+                                        C.POINTER(C.c_int), C.c_int, C.c_int, C.c_float, dp,
+                                        C.POINTER(SolveInfo), vp]
         _lib = L
     return _lib
 
@@ -212,6 +221,16 @@ class Plan:
         _check(rc, "arecgb_cgls")
         return hist[:info.iterations].copy(), info
 
+    def cgls_stat(self, b, x, maxit, tol, warm=False, stream=None):
+        """Statistically weighted CGLS (weights from b)."""
+        hist = np.zeros(max(maxit, 1), np.float64)
+        info = SolveInfo()
+        rc = lib().arecgb_cgls_stat(self._h, _ptr(b), _ptr(x), int(bool(warm)), int(maxit),
+                                    float(tol), hist.ctypes.data_as(C.POINTER(C.c_double)),
+                                    C.byref(info), _stream(stream))
+        _check(rc, "arecgb_cgls_stat")
+        return hist[:info.iterations].copy(), info
+
     def sirt(self, b, x, lam, maxit, tol, stream=None):
         hist = np.zeros(max(maxit, 1), np.float64)
         info = SolveInfo()
@@ -220,6 +239,14 @@ class Plan:
                                _stream(stream))
         _check(rc, "arecgb_sirt")
         return hist[:min(info.iterations, maxit)].copy(), info
+
+    def autotune(self, x, q, stream=None):
+        """Choose launch shapes by timing (overwrites x and q); returns
+        (forward band height, back-projection slice chunks per block)."""
+        band, nsc = C.c_int(), C.c_int()
+        _check(lib().arecgb_plan_autotune(self._h, _ptr(x), _ptr(q), C.byref(band), C.byref(nsc),
+                                          _stream(stream)), "arecgb_plan_autotune")
+        return band.value, nsc.value
 
     def timing(self, mode):
         """Projector timing (mode 1 start, 2 report, 0 report and stop):
@@ -307,6 +334,21 @@ def images_to_volume(plan, img, vol, npad, y0, count, scale=1.0, stream=None):
            "arecgb_unet_images_to_volume")
 
 
+def cgls_batch(plans, bs, xs, maxit, tol, warm=None, rnorm_ref=None, stream=None):
+    """CGLS over several problems at once (one plan each): lists of plans,
+    device sinograms and volumes.  Returns the list of SolveInfo."""
+    n = len(plans)
+    hp = (C.c_void_p * n)(*[p._h.value for p in plans])
+    hb = (C.c_void_p * n)(*[b.data_ptr() for b in bs])
+    hx = (C.c_void_p * n)(*[x.data_ptr() for x in xs])
+    w = (C.c_int * n)(*([int(bool(v)) for v in warm] if warm else [0] * n))
+    rr = (C.c_double * n)(*(rnorm_ref if rnorm_ref else [0.0] * n))
+    info = (SolveInfo * n)()
+    _check(lib().arecgb_cgls_batch(hp, hb, hx, w, n, maxit, tol, rr, info, _stream(stream)),
+           "arecgb_cgls_batch")
+    return list(info)
+
+
 def launch_count():
     """Kernel launches issued by the library so far."""
     return int(lib().arecgb_launch_count())
@@ -327,6 +369,21 @@ def cc_shifts_static(img1, img2, sx, sy, ix=None, iy=None, stream=None):
     _check(lib().arecgb_cc_shifts_static(_ptr(img1), _ptr(img2), nz, ny, nx, _ptr(sx),
                                          _ptr(sy), _ptr(ix), _ptr(iy), _stream(stream)),
            "arecgb_cc_shifts_static")
+
+
+def fshift2d_device(images, out, sx, sy, stream=None):
+    """Fourier shift of device image stacks [nz][ny][nx] by per-image (sx, sy)."""
+    nz, ny, nx = images.shape
+    _check(lib().arecgb_fshift2d_device(_ptr(images), _ptr(out), nz, ny, nx, _ptr(sx), _ptr(sy),
+                                        _stream(stream)), "arecgb_fshift2d_device")
+
+
+def fshift2d(image, sx, sy):
+    """The reference's fshift2d on one host image [ny][nx]."""
+    a = np.ascontiguousarray(image, dtype=np.float32)
+    out = np.zeros_like(a)
+    lib().arecgb_fshift2d(a.shape[1], a.shape[0], _f32p(a), _f32p(out), float(sx), float(sy))
+    return out
 
 
 def ccorr2d_device(x, y, c, stream=None):
@@ -434,7 +491,7 @@ def _solve(name, b, angles, lam, maxit, tol, x0=None):
         vol.data = C.POINTER(C.c_float)()
     else:
         nx = b.shape[2]
-        radius = (nx // 2) if name == "cyl_cgls_KB" else 0.5 * (nx - 1)
+        radius = (nx // 2) if name == "cyl_cgls_KB" or name.endswith("_stat") else 0.5 * (nx - 1)
         vol = arecAllocateCylImage(radius, b.shape[1])
         cyl_data(vol)[:] = np.asarray(x0, np.float32)
     st = getattr(lib(), "arecgb_" + name)(0, img, _f32p(angles), C.byref(vol), float(lam),
@@ -476,6 +533,19 @@ def cyl_cgls_KB(b, angles, maxit=10, tol=1e-3, x0=None):
 
 def cyl_cgls_SQ(b, angles, maxit=10, tol=1e-3, x0=None):
     return _solve("cyl_cgls_SQ", b, angles, 0.0, maxit, tol, x0)
+
+
+def cyl_cgls_SQ_stat(b, angles, maxit=10, tol=1e-3, x0=None):
+    """Statistically weighted CGLS (the reference's integer radius nx/2: odd nx)."""
+    return _solve("cyl_cgls_SQ_stat", b, angles, 0.0, maxit, tol, x0)
+
+
+def cyl_cgls_KB_stat(b, angles, maxit=10, tol=1e-3, x0=None):
+    return _solve("cyl_cgls_KB_stat", b, angles, 0.0, maxit, tol, x0)
+
+
+def cyl_cgls_stat(b, angles, maxit=10, tol=1e-3, x0=None):
+    return _solve("cyl_cgls_stat", b, angles, 0.0, maxit, tol, x0)
 
 
 def arecCCImages(images1, images2):

@@ -19,6 +19,11 @@
 
 namespace arecgb {
 const char *last_error();
+int cgls_batch(Plan *const *plans, const float *const *d_b, float *const *d_x, const int *warm,
+               int n, int maxit, float tol, const double *rnorm_ref, double *const *hist_host,
+               arecgb_solve_info *info, cudaStream_t st, const float *const *d_w);
+int cgls_stat(Plan *p, const float *d_b, float *d_x, int warm, int maxit, float tol,
+              double *hist_host, arecgb_solve_info *info, cudaStream_t st);
 int cgls(Plan *p, const float *d_b, float *d_x, int warm, int maxit, float tol, double rnorm_ref,
          double *hist_host, arecgb_solve_info *info, cudaStream_t st);
 int sirt(Plan *p, const float *d_b, float *d_x, float lam, int maxit, float tol,
@@ -26,6 +31,8 @@ int sirt(Plan *p, const float *d_b, float *d_x, float lam, int maxit, float tol,
 int cc_shifts(const float *d1, const float *d2, int nz, int ny, int nx, float *sx, float *sy,
               int *ix, int *iy, cudaStream_t st);
 int ccorr_image(const float *dx, const float *dy, float *dc, int ny, int nx, cudaStream_t st);
+int fshift_stack(const float *d_in, float *d_out, int nz, int ny, int nx, const float *d_sx,
+                 const float *d_sy, cudaStream_t st);
 int peak_search(const float *dc, int nz, int ny, int nx, float *sx, float *sy, int *ix, int *iy,
                 cudaStream_t st);
 }  // namespace arecgb
@@ -142,6 +149,26 @@ int arecgb_sino_to_reference(const float *d_dev, float *d_ref, int na, int ny, i
     return sino_to_reference_layout(d_dev, d_ref, na, ny, nx, ys, (cudaStream_t)stream);
 }
 
+int arecgb_cgls_batch(arecgb_plan *const *plans, const float *const *d_b, float *const *d_x,
+                      const int *warm, int n, int maxit, float tol, const double *rnorm_ref,
+                      arecgb_solve_info *info, void *stream) {
+    if (n < 1 || !plans) {
+        set_error("arecgb_cgls_batch: bad arguments");
+        return ARECGB_ERR_ARG;
+    }
+    return cgls_batch(reinterpret_cast<Plan *const *>(plans), d_b, d_x, warm, n, maxit, tol,
+                      rnorm_ref, nullptr, info, (cudaStream_t)stream, nullptr);
+}
+
+int arecgb_cgls_stat(arecgb_plan *plan, const float *d_b, float *d_x, int warm, int maxit,
+                     float tol, double *rel_history, arecgb_solve_info *info, void *stream) {
+    if (!plan || !d_b || !d_x) {
+        set_error("arecgb_cgls_stat: null argument");
+        return ARECGB_ERR_ARG;
+    }
+    return cgls_stat(P(plan), d_b, d_x, warm, maxit, tol, rel_history, info, (cudaStream_t)stream);
+}
+
 int arecgb_plan_timing(arecgb_plan *plan, int mode, double *fp_ms, long long *fp_calls,
                        double *bp_ms, long long *bp_calls) {
     if (!plan || mode < 0 || mode > 2) {
@@ -153,6 +180,18 @@ int arecgb_plan_timing(arecgb_plan *plan, int mode, double *fp_ms, long long *fp
 
 long long arecgb_launch_count(void) { return launch_count(); }
 
+int arecgb_plan_autotune(arecgb_plan *plan, float *d_x, float *d_q, int *fp_band, int *bp_nsc,
+                         void *stream) {
+    if (!plan || !d_x || !d_q) {
+        set_error("arecgb_plan_autotune: null argument");
+        return ARECGB_ERR_ARG;
+    }
+    int rc = plan_autotune(P(plan), d_x, d_q, (cudaStream_t)stream);
+    if (fp_band) *fp_band = P(plan)->fp_band;
+    if (bp_nsc) *bp_nsc = P(plan)->bp_nsc;
+    return rc;
+}
+
 int arecgb_cc_shifts(const float *d_img1, const float *d_img2, int nz, int ny, int nx,
                      float *d_sx, float *d_sy, int *d_ix, int *d_iy, void *stream) {
     return cc_shifts(d_img1, d_img2, nz, ny, nx, d_sx, d_sy, d_ix, d_iy, (cudaStream_t)stream);
@@ -161,6 +200,11 @@ int arecgb_cc_shifts(const float *d_img1, const float *d_img2, int nz, int ny, i
 int arecgb_ccorr2d_device(const float *d_x, const float *d_y, float *d_c, int ny, int nx,
                           void *stream) {
     return ccorr_image(d_x, d_y, d_c, ny, nx, (cudaStream_t)stream);
+}
+
+int arecgb_fshift2d_device(const float *d_in, float *d_out, int nz, int ny, int nx,
+                           const float *d_sx, const float *d_sy, void *stream) {
+    return fshift_stack(d_in, d_out, nz, ny, nx, d_sx, d_sy, (cudaStream_t)stream);
 }
 
 }  // extern "C"
@@ -402,12 +446,35 @@ int compat_backproject(int w, const arecImage &img, const float *angles, int nan
 }
 
 // cyl_cgls[_KB|_SQ] and cyl_sirt[_KB|_SQ].
+// Weight range line of init_weights (areccgls_stat.cpp:36-44), from the host images.
+static void print_stat_weight_range(const arecImage &im) {
+    const int nx = im.nx;
+    std::vector<double> hx(nx);
+    const double alpha = 0.5, pi = std::atan(1.0) * 4.0, A = 2.0 * pi / alpha;
+    const double xa = 0.5 * alpha * (nx - 1), xb = (1.0 - 0.5 * alpha) * (nx - 1);
+    for (int x = 0; x < nx; x++) {
+        const double va = 0.5 * (1.0 + std::cos(A * (1.0 * x / (nx - 1) - alpha / 2)));
+        const double vb = 0.5 * (1.0 + std::cos(A * (1.0 * x / (nx - 1) - 1.0 + alpha / 2)));
+        hx[x] = x < xa ? va : (x > xb ? vb : 1.0);
+    }
+    float mn = 1e6f, mx = -1e6f;
+    const size_t n = (size_t)im.nx * im.ny * im.nz;
+    for (size_t i = 0; i < n; i++) {
+        const float w = (float)((double)expf(-im.data[i]) * hx[i % nx]);
+        mn = std::min(mn, w);
+        mx = std::max(mx, w);
+    }
+    printf("Statweight min: %f max: %f \n", mn, mx);
+}
+
 int compat_solve(bool is_cgls, int w, const arecImage &images, const float *angles,
-                 arecImage *xvol, float lam, int maxit, float tol) {
+                 arecImage *xvol, float lam, int maxit, float tol, bool stat = false) {
     const int nx = images.nx, ny = images.ny, nz = images.nz;
-    // radius = 0.5*(nx-1) (areccgls.cpp:49, arecsirt.cpp:37); the KB CGLS uses
-    // the integer nx/2 (areccgls_KB.cpp:37), which fails for even nx.
-    const bool kb_int_radius = is_cgls && w == ARECGB_KB;
+    // radius = 0.5*(nx-1) (areccgls.cpp:49, arecsirt.cpp:37); the KB CGLS and
+    // the weighted CGLS use the integer nx/2 (areccgls_KB.cpp:37,
+    // areccgls_stat.cpp:73), which fails for even nx.
+    const bool kb_int_radius = is_cgls && (w == ARECGB_KB || stat);
+    if (stat && !quiet()) print_stat_weight_range(images);
     const double radius = kb_int_radius ? (double)(nx / 2) : 0.5 * (nx - 1);
     const bool v = !quiet();
     const bool warm = xvol->data != NULL;
@@ -440,8 +507,8 @@ int compat_solve(bool is_cgls, int w, const arecImage &images, const float *angl
     if ((rc = upload_sino(p, images.data, p->d_sin[2]))) return rc;
     if (is_cgls && warm && (rc = upload_volume(p, xvol->data, p->d_vol[3]))) return rc;
     if (v) {
-        printf("%snrays = %d, nnz = %d\n", is_cgls && w == ARECGB_SQ ? "cyl: " : "", xvol->nrays,
-               xvol->nnz);
+        printf("%snrays = %d, nnz = %d\n", is_cgls && (w == ARECGB_SQ || stat) ? "cyl: " : "",
+               xvol->nrays, xvol->nnz);
         if (kb_int_radius)
             printf("nx = %d, ny = %d, radius = %d, height = %d\n", nx, ny, (int)radius, ny);
         else
@@ -450,7 +517,10 @@ int compat_solve(bool is_cgls, int w, const arecImage &images, const float *angl
     std::vector<double> hist((size_t)std::max(maxit, 1), 0.0);
     arecgb_solve_info info;
     memset(&info, 0, sizeof(info));
-    if (is_cgls)
+    if (is_cgls && stat)
+        rc = cgls_stat(p, p->d_sin[2], p->d_vol[3], warm ? 1 : 0, maxit, tol, hist.data(), &info,
+                       p->stream);
+    else if (is_cgls)
         rc = cgls(p, p->d_sin[2], p->d_vol[3], warm ? 1 : 0, maxit, tol, 0.0, hist.data(), &info,
                   p->stream);
     else
@@ -603,6 +673,45 @@ int arecgb_cyl_cgls_SQ(MPI_Comm, arecImage im, float *a, arecImage *x, float lam
                        float tol) {
     return compat_solve(true, ARECGB_SQ, im, a, x, lam, maxit, tol);
 }
+int arecgb_cyl_cgls_stat(MPI_Comm, arecImage im, float *a, arecImage *x, float lam, int maxit,
+                         float tol) {
+    return compat_solve(true, ARECGB_LIN, im, a, x, lam, maxit, tol, true);
+}
+int arecgb_cyl_cgls_KB_stat(MPI_Comm, arecImage im, float *a, arecImage *x, float lam, int maxit,
+                            float tol) {
+    return compat_solve(true, ARECGB_KB, im, a, x, lam, maxit, tol, true);
+}
+int arecgb_cyl_cgls_SQ_stat(MPI_Comm, arecImage im, float *a, arecImage *x, float lam, int maxit,
+                            float tol) {
+    return compat_solve(true, ARECGB_SQ, im, a, x, lam, maxit, tol, true);
+}
+
+// init_weights (areccgls_stat.cpp:12-46): w = expf(-p) times the Tukey window
+// along x, in a newly allocated cube image.
+int arecgb_init_weights(MPI_Comm, arecImage pr, arecImage *weights) {
+    const int nx = pr.nx;
+    if (arecgb_arecAllocateCBImage(weights, pr.nx, pr.ny, pr.nz) != 0) return 1;
+    std::vector<double> hx(nx);
+    const double alpha = 0.5, pi = std::atan(1.0) * 4.0, A = 2.0 * pi / alpha;
+    const double xa = 0.5 * alpha * (nx - 1), xb = (1.0 - 0.5 * alpha) * (nx - 1);
+    for (int x = 0; x < nx; x++) {
+        const double va = 0.5 * (1.0 + std::cos(A * (1.0 * x / (nx - 1) - alpha / 2)));
+        const double vb = 0.5 * (1.0 + std::cos(A * (1.0 * x / (nx - 1) - 1.0 + alpha / 2)));
+        hx[x] = x < xa ? va : (x > xb ? vb : 1.0);
+    }
+    const size_t n = (size_t)pr.nx * pr.ny * pr.nz;
+    for (size_t i = 0; i < n; i++)
+        weights->data[i] = (float)((double)expf(-pr.data[i]) * hx[i % nx]);
+    if (!quiet()) {
+        float mn = 1e6f, mx = -1e6f;
+        for (size_t i = 0; i < n; i++) {
+            mn = std::min(mn, weights->data[i]);
+            mx = std::max(mx, weights->data[i]);
+        }
+        printf("Statweight min: %f max: %f \n", mn, mx);
+    }
+    return 0;
+}
 
 // arecCCImages (AREC3D/AREC3D/arecImage.cpp:384-434): shifts of each image of
 // images2 against the same-index image of images1.
@@ -663,6 +772,23 @@ void arecgb_ccorr2d(int nx, int ny, float *x, float *y, float *c) {
     cudaFree(d);
 }
 
+// fshift2d (AREC3D/AREC3D/align2dstack.cpp:566-630) on host buffers.
+void arecgb_fshift2d(int nx, int ny, float *in, float *out, float sx, float sy) {
+    std::lock_guard<std::mutex> lk(g_mu);
+    const size_t n = (size_t)nx * ny;
+    float *d = nullptr;
+    if (cudaMalloc(&d, sizeof(float) * (2 * n + 2)) != cudaSuccess) {
+        set_error("fshift2d: device allocation failed");
+        return;
+    }
+    const float s2[2] = {sx, sy};
+    cudaMemcpy(d, in, sizeof(float) * n, cudaMemcpyHostToDevice);
+    cudaMemcpy(d + 2 * n, s2, sizeof(float) * 2, cudaMemcpyHostToDevice);
+    if (fshift_stack(d, d + n, 1, ny, nx, d + 2 * n, d + 2 * n + 1, 0) == 0)
+        cudaMemcpy(out, d + n, sizeof(float) * n, cudaMemcpyDeviceToHost);
+    cudaFree(d);
+}
+
 // speak (AREC3D/AREC3D/align2dstack.cpp:1059-1105).
 void arecgb_speak(int nx, int ny, float *data, float *xt, float *yt) {
     std::lock_guard<std::mutex> lk(g_mu);
@@ -704,6 +830,11 @@ int cyl_sirt_SQ(MPI_Comm m, arecImage i, float *a, arecImage *x, float l, int it
 int cyl_cgls(MPI_Comm m, arecImage i, float *a, arecImage *x, float l, int it, float t) { return arecgb_cyl_cgls(m, i, a, x, l, it, t); }
 int cyl_cgls_KB(MPI_Comm m, arecImage i, float *a, arecImage *x, float l, int it, float t) { return arecgb_cyl_cgls_KB(m, i, a, x, l, it, t); }
 int cyl_cgls_SQ(MPI_Comm m, arecImage i, float *a, arecImage *x, float l, int it, float t) { return arecgb_cyl_cgls_SQ(m, i, a, x, l, it, t); }
+int cyl_cgls_stat(MPI_Comm m, arecImage i, float *a, arecImage *x, float l, int it, float t) { return arecgb_cyl_cgls_stat(m, i, a, x, l, it, t); }
+int cyl_cgls_KB_stat(MPI_Comm m, arecImage i, float *a, arecImage *x, float l, int it, float t) { return arecgb_cyl_cgls_KB_stat(m, i, a, x, l, it, t); }
+int cyl_cgls_SQ_stat(MPI_Comm m, arecImage i, float *a, arecImage *x, float l, int it, float t) { return arecgb_cyl_cgls_SQ_stat(m, i, a, x, l, it, t); }
+int init_weights(MPI_Comm m, arecImage p, arecImage *w) { return arecgb_init_weights(m, p, w); }
 int arecCCImages(MPI_Comm m, arecImage a, arecImage b, float *sx, float *sy) { return arecgb_arecCCImages(m, a, b, sx, sy); }
 void ccorr2d(int nx, int ny, float *x, float *y, float *c) { arecgb_ccorr2d(nx, ny, x, y, c); }
 void speak(int nx, int ny, float *d, float *xt, float *yt) { arecgb_speak(nx, ny, d, xt, yt); }
+void fshift2d(int nx, int ny, float *in, float *out, float sx, float sy) { arecgb_fshift2d(nx, ny, in, out, sx, sy); }

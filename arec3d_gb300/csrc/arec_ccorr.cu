@@ -411,6 +411,106 @@ __global__ void __launch_bounds__(256) k_peak(const float *__restrict__ c,
 }
 
 // ---------------------------------------------------------------------------
+// Fourier shift (fshift2d, align2dstack.cpp:566-630) of a stack of images:
+//   out = Re(IDFT2(DFT2(in) * exp(i * phase))) / (nx * ny),
+//   phase = -2 pi (sx kx + sy ky) in the reference's precisions: the frequencies
+//   and sx*kx + sy*ky in float, the product with 2 pi in double rounded to a
+//   float, then the float cosine and sine (cos/sin of a float resolve to the
+//   float overloads) and a float complex product.  Full complex transforms, as
+//   the reference's: at the Nyquist frequencies the factor is not conjugate
+//   symmetric and only the real part is kept.
+
+// Pass 1: real rows -> complex spectra of the rows.
+__global__ void __launch_bounds__(256) k_fs_rows(const float *__restrict__ in,
+                                                 float2 *__restrict__ C, int nx, int ny,
+                                                 const float2 *__restrict__ tw) {
+    extern __shared__ float2 sm[];
+    const int G = 4096 / nx < 256 / (nx / 16) ? 4096 / nx : 256 / (nx / 16);
+    const int row0 = blockIdx.x * G;
+    const size_t img = (size_t)blockIdx.y * nx * ny;
+    for (int i = threadIdx.x; i < G * nx; i += blockDim.x) {
+        const int l = i / nx, c = i % nx, row = row0 + l;
+        sm[l * nx + c] = make_float2(row < ny ? in[img + (size_t)row * nx + c] : 0.f, 0.f);
+    }
+    __syncthreads();
+    fft_lines(sm, nx, nx, G, tw);
+    for (int i = threadIdx.x; i < G * nx; i += blockDim.x) {
+        const int l = i / nx, c = i % nx, row = row0 + l;
+        if (row < ny) C[img + (size_t)row * nx + c] = sm[l * nx + c];
+    }
+}
+
+__device__ __forceinline__ float fs_freq(int i, int n) {
+    const int h = (n + 1) / 2;  // ceil(n / 2)
+    return i < h ? (float)i / (float)n : (float)(i - n) / (float)n;
+}
+
+// Pass 2: column transforms, the phase factor, inverse column transforms.
+__global__ void __launch_bounds__(256) k_fs_cols(float2 *__restrict__ C, int nx, int ny,
+                                                 const float *__restrict__ sxs,
+                                                 const float *__restrict__ sys,
+                                                 const float2 *__restrict__ tw) {
+    extern __shared__ float2 sm[];
+    const int c0 = blockIdx.x * kColTile;
+    const size_t img = (size_t)blockIdx.y * nx * ny;
+    const float sx = sxs[blockIdx.y], sy = sys[blockIdx.y];
+    const double two_pi = 2.0 * 3.14159265358979323846;
+    for (int i = threadIdx.x; i < kColTile * ny; i += blockDim.x) {
+        const int row = i / kColTile, c = i % kColTile;
+        sm[c * ny + row] = C[img + (size_t)row * nx + c0 + c];
+    }
+    __syncthreads();
+    const int G = max(1, 256 / (ny / 16));
+    for (int l0 = 0; l0 < kColTile; l0 += G)
+        fft_lines(sm + (size_t)l0 * ny, ny, ny, min(G, kColTile - l0), tw);
+    for (int i = threadIdx.x; i < kColTile * ny; i += blockDim.x) {
+        const int c = i / ny, row = i % ny;
+        const float t = __fadd_rn(__fmul_rn(sx, fs_freq(c0 + c, nx)), __fmul_rn(sy, fs_freq(row, ny)));
+        const float ph = (float)(-two_pi * (double)t);
+        float sn, cs;
+        sincosf(ph, &sn, &cs);
+        const float2 f = sm[i];
+        const float re = __fsub_rn(__fmul_rn(f.x, cs), __fmul_rn(f.y, sn));
+        const float im = __fadd_rn(__fmul_rn(f.x, sn), __fmul_rn(f.y, cs));
+        sm[i] = make_float2(re, -im);  // conjugated: IDFT = conj(DFT(conj))
+    }
+    __syncthreads();
+    for (int l0 = 0; l0 < kColTile; l0 += G)
+        fft_lines(sm + (size_t)l0 * ny, ny, ny, min(G, kColTile - l0), tw);
+    for (int i = threadIdx.x; i < kColTile * ny; i += blockDim.x) {
+        const int row = i / kColTile, c = i % kColTile;
+        const float2 w = sm[c * ny + row];
+        C[img + (size_t)row * nx + c0 + c] = make_float2(w.x, -w.y);
+    }
+}
+
+// Pass 3: inverse row transforms, real part, divided by nx*ny.
+__global__ void __launch_bounds__(256) k_fs_rows_inv(const float2 *__restrict__ C,
+                                                     float *__restrict__ out, int nx, int ny,
+                                                     const float2 *__restrict__ tw) {
+    extern __shared__ float2 sm[];
+    const int G = 4096 / nx < 256 / (nx / 16) ? 4096 / nx : 256 / (nx / 16);
+    const int row0 = blockIdx.x * G;
+    const size_t img = (size_t)blockIdx.y * nx * ny;
+    for (int i = threadIdx.x; i < G * nx; i += blockDim.x) {
+        const int l = i / nx, c = i % nx, row = row0 + l;
+        float2 z = make_float2(0.f, 0.f);
+        if (row < ny) {
+            z = C[img + (size_t)row * nx + c];
+            z.y = -z.y;
+        }
+        sm[l * nx + c] = z;
+    }
+    __syncthreads();
+    fft_lines(sm, nx, nx, G, tw);
+    const float scale = (float)(nx * ny);
+    for (int i = threadIdx.x; i < G * nx; i += blockDim.x) {
+        const int l = i / nx, c = i % nx, row = row0 + l;
+        if (row < ny) out[img + (size_t)row * nx + c] = sm[l * nx + c].x / scale;
+    }
+}
+
+// ---------------------------------------------------------------------------
 // Host side.
 
 static std::mutex g_tw_mu;
@@ -531,6 +631,48 @@ int ccorr_image(const float *dx, const float *dy, float *dc, int ny, int nx, cud
     if (!rc) rc = correlate_batch(dx, dy, 1, ny, nx, dc, s.stats, s.Xh, s.Yh, st);
     cudaStreamSynchronize(st);
     cc_free(s);
+    return rc;
+}
+
+int fshift_stack(const float *d_in, float *d_out, int nz, int ny, int nx, const float *d_sx,
+                 const float *d_sy, cudaStream_t st) {
+    if (!pow2_ok(nx) || !pow2_ok(ny) || ny > 2048 || nz < 0 || !d_in || !d_out || !d_sx || !d_sy) {
+        set_error("fshift2d: nx (16..4096) and ny (16..2048) must be powers of two");
+        return ARECGB_ERR_ARG;
+    }
+    if (nz == 0) return 0;
+    const float2 *twx, *twy;
+    int rc = twiddles(nx, &twx);
+    if (!rc) rc = twiddles(ny, &twy);
+    if (rc) return rc;
+    const int G = rows_per_block(nx);
+    const size_t row_smem = sizeof(float2) * (size_t)G * nx;
+    const size_t col_smem = sizeof(float2) * kColTile * (size_t)ny;
+    if ((rc = set_smem((const void *)k_fs_rows, row_smem))) return rc;
+    if ((rc = set_smem((const void *)k_fs_rows_inv, row_smem))) return rc;
+    if ((rc = set_smem((const void *)k_fs_cols, col_smem))) return rc;
+    // images per batch: complex scratch near 1 GiB
+    const size_t per = sizeof(float2) * (size_t)nx * ny;
+    const int batch = (int)std::max<size_t>(1, std::min<size_t>(nz, (1ull << 30) / per));
+    float2 *C = nullptr;
+    ARECGB_CUDA(cudaMalloc(&C, per * batch));
+    for (int z0 = 0; z0 < nz && !rc; z0 += batch) {
+        const int nb = std::min(batch, nz - z0);
+        const size_t off = (size_t)z0 * nx * ny;
+        k_fs_rows<<<dim3((ny + G - 1) / G, nb), 256, row_smem, st>>>(d_in + off, C, nx, ny, twx);
+        k_fs_cols<<<dim3(nx / kColTile, nb), 256, col_smem, st>>>(C, nx, ny, d_sx + z0, d_sy + z0,
+                                                                twy);
+        k_fs_rows_inv<<<dim3((ny + G - 1) / G, nb), 256, row_smem, st>>>(C, d_out + off, nx, ny,
+                                                                       twx);
+        count_launches(3);
+        cudaError_t e = cudaGetLastError();
+        if (e != cudaSuccess) {
+            set_error(std::string("fshift2d: ") + cudaGetErrorString(e));
+            rc = cuda_status(e);
+        }
+    }
+    cudaStreamSynchronize(st);
+    cudaFree(C);
     return rc;
 }
 

@@ -228,7 +228,10 @@ int plan_create(Plan **out, int weighting, double radius, int ny, int nangles,
     if (e == cudaSuccess)
         e = cudaMemcpy(p->d_cols, cols.data(), sizeof(ColInfo) * nx, cudaMemcpyHostToDevice);
     if (e == cudaSuccess) {
-        p->n_partials = std::max(fp_grid_blocks(p), bp_grid_blocks(p));
+        // room for the back projector's grid with one slice chunk per block
+        // (the autotuner may choose it): ntiles x ceil(ys / (32 vec)) blocks
+        const int bp_max = p->ntiles * ((p->ys + 32 * p->vec - 1) / (32 * p->vec));
+        p->n_partials = std::max(std::max(fp_grid_blocks(p), bp_grid_blocks(p)), bp_max);
         e = cudaMalloc(&p->d_partials, sizeof(double) * (size_t)p->n_partials);
     }
     if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&p->stream, cudaStreamNonBlocking);
@@ -253,6 +256,7 @@ void plan_destroy(Plan *p) {
     cudaFree(p->d_cols);
     for (cudaEvent_t e : p->ev_fp) cudaEventDestroy(e);
     for (cudaEvent_t e : p->ev_bp) cudaEventDestroy(e);
+    cudaFree(p->d_w);
     cudaFree(p->d_groups);
     cudaFree(p->d_tiles);
     cudaFree(p->d_err);

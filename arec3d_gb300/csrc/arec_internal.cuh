@@ -62,6 +62,8 @@ struct Plan {
     int ngroups = 0;              //   the row-sweeping (orient 0) groups first
     int ngroups_o[2] = {0, 0};    // groups per orientation
     int fp_band = 64;             // forward projection: lines per band launch
+    int bp_nsc = 0;               // back projection: slice chunks per block (0 = by size)
+    int tuned = 0;                // launch shapes chosen by plan_autotune
     int2 *d_tiles = nullptr;      // back-projection ray tiles: (ix0, iz0) of 8x4-pixel tiles
     int ntiles = 0;
     int *d_err = nullptr;         // device error flag (nonzero: a kernel saw an impossible case)
@@ -78,6 +80,7 @@ struct Plan {
     // scratch owned by the plan for the reference-compatible entry points
     float *d_vol[4] = {nullptr, nullptr, nullptr, nullptr};
     float *d_sin[3] = {nullptr, nullptr, nullptr};
+    float *d_w = nullptr;          // statistical weights of the weighted CGLS (device layout)
     float *d_stage = nullptr;      // staging buffer in the reference layout
     size_t stage_floats = 0;
     float *h_pinned = nullptr;     // pinned host staging
@@ -115,6 +118,7 @@ int back_project(const Plan *p, const float *d_s, float *d_g, double *d_norm2,
 int fp_grid_blocks(const Plan *p);
 int plan_timing(const Plan *p, int mode, double *fp_ms, long long *fp_calls, double *bp_ms,
                 long long *bp_calls);
+int plan_autotune(Plan *p, float *d_x, float *d_q, cudaStream_t st);
 int bp_grid_blocks(const Plan *p);
 
 // Layout kernels and vector ops (arec_vector.cu)

@@ -37,7 +37,10 @@ static OpArgs make_args(const Plan *p, const int *skip) {
 }
 
 // Slice chunks per block: two warps' worth of slices when there are that many.
-static int slice_chunks(const Plan *p) { return p->ys > 32 * p->vec ? 2 : 1; }
+static int slice_chunks(const Plan *p) {
+    if (p->bp_nsc == 1 || (p->bp_nsc == 2 && p->ys > 32 * p->vec)) return p->bp_nsc;
+    return p->ys > 32 * p->vec ? 2 : 1;
+}
 
 static int slice_blocks(const Plan *p) {
     const int span = 32 * p->vec * slice_chunks(p);
@@ -66,6 +69,9 @@ static int timing_event(std::vector<cudaEvent_t> &v, size_t i, cudaEvent_t *out)
 
 static int timing_mark(const Plan *p, bool fp, bool stop, cudaStream_t st) {
     if (!p->timing) return 0;
+    cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+    if (cudaStreamIsCapturing(st, &cap) == cudaSuccess && cap != cudaStreamCaptureStatusNone)
+        return 0;  // a captured iteration is timed by its eager calls only
     std::vector<cudaEvent_t> &v = fp ? p->ev_fp : p->ev_bp;
     size_t &n = fp ? p->n_fp : p->n_bp;
     cudaEvent_t e;
@@ -173,6 +179,69 @@ int back_project(const Plan *p, const float *d_s, float *d_g, double *d_norm2,
         if (rc) return rc;
     }
     return timing_mark(p, false, true, st);
+}
+
+// Autotuner: times the forward projector for band heights of 32, 64 and 128
+// lines and the back projector with one or two slice chunks per block on the
+// caller's buffers (x: a volume, q: a sinogram of this plan; both overwritten),
+// best of two runs each after a warm-up run, and keeps the fastest shapes.
+int plan_autotune(Plan *p, float *d_x, float *d_q, cudaStream_t st) {
+    if (p->weighting == ARECGB_LIN) return 0;  // the linear pair has no shapes to choose
+    cudaEvent_t e0, e1;
+    ARECGB_CUDA(cudaEventCreate(&e0));
+    ARECGB_CUDA(cudaEventCreate(&e1));
+    auto best_of = [&](auto &&fn, float *ms) -> int {
+        int rc = fn();  // warm-up
+        if (rc) return rc;
+        *ms = 1e30f;
+        for (int rep = 0; rep < 2; rep++) {
+            ARECGB_CUDA(cudaEventRecord(e0, st));
+            if ((rc = fn())) return rc;
+            ARECGB_CUDA(cudaEventRecord(e1, st));
+            ARECGB_CUDA(cudaEventSynchronize(e1));
+            float t = 0.f;
+            ARECGB_CUDA(cudaEventElapsedTime(&t, e0, e1));
+            *ms = std::min(*ms, t);
+        }
+        return 0;
+    };
+    int rc = 0;
+    const bool was_timing = p->timing;
+    p->timing = false;
+    int best_band = p->fp_band;
+    float best = 1e30f;
+    for (int band : {32, 64, 128}) {
+        if (band > 2 * p->nx && band != 32) continue;
+        p->fp_band = band;
+        float ms;
+        if ((rc = best_of([&] { return forward_project(p, d_x, d_q, nullptr, nullptr, st); }, &ms)))
+            break;
+        if (ms < best) {
+            best = ms;
+            best_band = band;
+        }
+    }
+    p->fp_band = best_band;
+    int best_nsc = 0;
+    best = 1e30f;
+    for (int nsc : {1, 2}) {
+        if (rc) break;
+        if (nsc == 2 && p->ys <= 32 * p->vec) continue;
+        p->bp_nsc = nsc;
+        float ms;
+        if ((rc = best_of([&] { return back_project(p, d_q, d_x, nullptr, nullptr, st); }, &ms)))
+            break;
+        if (ms < best) {
+            best = ms;
+            best_nsc = nsc;
+        }
+    }
+    p->bp_nsc = best_nsc;
+    p->tuned = rc ? 0 : 1;
+    p->timing = was_timing;
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    return rc;
 }
 
 }  // namespace arecgb

@@ -505,9 +505,9 @@ __device__ __forceinline__ int line_pixel_ray(const OpArgs &A, int orient, int l
 //
 // Block = 4 angle warps + 1 staging warp.  The staging warp runs up to two
 // lines ahead: per line it forms the union of the group's candidate pixels,
-// looks up their rays and stages their x rows with one bulk copy per row
-// (cp.async.bulk) into one of two buffers, completing on that buffer's "full"
-// mbarrier.  Each angle warp computes its weights for the staged rows (lanes =
+// looks up their rays and stages their x rows and ray-table entries with one
+// bulk copy each (cp.async.bulk) into one of two buffers, completing on that
+// buffer's "full" mbarrier.  Each angle warp computes its weights for the staged rows (lanes =
 // rows, ordered by increasing centre bin), compacts the rows whose centre bin
 // falls in the tile (a contiguous run: the centre bin is monotonic along a
 // line; a counting sort covers any exception), accumulates them with the
@@ -517,7 +517,7 @@ __device__ __forceinline__ int line_pixel_ray(const OpArgs &A, int orient, int l
 template <int VEC>
 constexpr size_t fpb_smem_bytes() {
     return sizeof(float) * 2 * kFpStage * (32 * VEC) + sizeof(float4) * kGroupAngles * 32 +
-           sizeof(int) * 2 * kFpStage + sizeof(int) * (2 * kGroupAngles + 4);
+           sizeof(float4) * 2 * kFpStage + sizeof(int) * (2 * kGroupAngles + 4);
 }
 
 constexpr int kFpThreads = 32 * (kGroupAngles + 1);
@@ -531,8 +531,8 @@ __global__ void __launch_bounds__(kFpThreads, 3)
     __shared__ __align__(8) uint64_t full[2], empty[2];
     float *stg = reinterpret_cast<float *>(smem_raw);                // [2][US][SPAN]
     float4 *list = reinterpret_cast<float4 *>(stg + 2 * US * SPAN);  // [NA][32]
-    int *rowk = reinterpret_cast<int *>(list + NA * 32);             // [2][US] ray of each row
-    int *lrange = rowk + 2 * US;                                     // [NA][2]
+    float4 *rayb = list + NA * 32;                                   // [2][US] ray of each row
+    int *lrange = reinterpret_cast<int *>(rayb + 2 * US);            // [NA][2]
     int *uinfo = lrange + 2 * NA;                                    // [2][2] (first pixel, rows)
     if (A.skip && *A.skip) return;
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -622,22 +622,19 @@ __global__ void __launch_bounds__(kFpThreads, 3)
                 n = US;
             }
             if (!ok) n = 0;  // a wait gave up: stage nothing more
-            int k = 0;
-            if (lane < n) {
-                k = line_pixel_ray(A, orient, li, ulo + lane);
-                rowk[buf * US + lane] = k;
-            }
-            __syncwarp();
+            const int k = lane < n ? line_pixel_ray(A, orient, li, ulo + lane) : 0;
             if (lane == 0) {
                 uinfo[2 * buf] = ulo;
                 uinfo[2 * buf + 1] = n;
-                __threadfence_block();  // row table and counts before the arrival
-                umma::mbar_arrive_expect_tx(&full[buf], (uint32_t)n * row_bytes);
+                __threadfence_block();  // counts before the arrival
+                umma::mbar_arrive_expect_tx(&full[buf], (uint32_t)n * (row_bytes + 16u));
             }
             __syncwarp();
-            if (lane < n)
+            if (lane < n) {
                 umma::bulk_g2s(stg + ((size_t)buf * US + lane) * SPAN, x + (size_t)k * ys + yb,
                                row_bytes, &full[buf]);
+                umma::bulk_g2s(rayb + buf * US + lane, A.ray + k, 16u, &full[buf]);
+            }
         }
         return;
     }
@@ -662,8 +659,7 @@ __global__ void __launch_bounds__(kFpThreads, 3)
         float4 ent = make_float4(0.f, 0.f, 0.f, 0.f);
         if (angle_ok && lane < un && li >= my_lo && li <= my_hi) {
             const int row = ca > 0.f ? lane : un - 1 - lane;
-            const int k = rowk[buf * US + row];
-            const Taps t = ray_taps<W>(A.ray[k], ap, A.r_hi, A.r_lo);
+            const Taps t = ray_taps<W>(rayb[buf * US + row], ap, A.r_hi, A.r_lo);
             gk = t.iqx - b0 + 1;
             valid = gk >= 0 && gk <= BT + 1;
             ent = make_float4(__int_as_float(row | (gk << 8)), t.w0, t.w1, t.w2);

@@ -115,6 +115,48 @@ __global__ void __launch_bounds__(256) k_sumsq(const float *__restrict__ v, size
     }
 }
 
+// sum(q*q*w): float products accumulated in double (areccgls_stat.cpp:651-652).
+__global__ void __launch_bounds__(256) k_wsumsq(const float *__restrict__ v,
+                                                const float *__restrict__ w, size_t n,
+                                                double *__restrict__ partials) {
+    __shared__ double red[8];
+    double s = 0.0;
+    for (size_t i = (size_t)blockIdx.x * 256 + threadIdx.x; i < n; i += (size_t)gridDim.x * 256)
+        s += (double)__fmul_rn(__fmul_rn(v[i], v[i]), w[i]);
+    for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = s;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double t = 0.0;
+        for (int k = 0; k < 8; k++) t += red[k];
+        partials[blockIdx.x] = t;
+    }
+}
+
+// Statistical weights w = expf(-b) times the Tukey window (alpha 0.5) along the
+// detector (init_weights, areccgls_stat.cpp:12-46; tukey_filter_x_inplace,
+// imagetools.cpp:369-391); device sinogram layout [angle][bin][ys].
+__global__ void __launch_bounds__(256) k_stat_weights(const float *__restrict__ b,
+                                                      const double *__restrict__ hx,
+                                                      float *__restrict__ w, size_t n, int nx,
+                                                      int ys) {
+    for (size_t i = (size_t)blockIdx.x * 256 + threadIdx.x; i < n; i += (size_t)gridDim.x * 256) {
+        const int bin = (int)((i / ys) % nx);
+        w[i] = (float)((double)expf(-b[i]) * hx[bin]);
+    }
+}
+
+// s = (b - q) w, or s = b w when q is null (areccgls_stat.cpp:604-610).
+__global__ void __launch_bounds__(256) k_sub_w(const float *__restrict__ b,
+                                               const float *__restrict__ q,
+                                               const float *__restrict__ w, float *__restrict__ s,
+                                               size_t n) {
+    for (size_t i = (size_t)blockIdx.x * 256 + threadIdx.x; i < n; i += (size_t)gridDim.x * 256) {
+        const float r = q ? b[i] - q[i] : b[i];
+        s[i] = r * w[i];
+    }
+}
+
 int sumsq_partials(const float *d_v, size_t n, double *d_partials, int nblocks, cudaStream_t st) {
     k_sumsq<<<nblocks, 256, 0, st>>>(d_v, n, d_partials);
     ARECGB_CUDA(cudaGetLastError());
@@ -161,7 +203,8 @@ __global__ void k_cgls_alpha(SolveState *S) {
 __global__ void __launch_bounds__(256) k_cgls_xs(SolveState *S, float *__restrict__ x,
                                                  const float *__restrict__ p, size_t nv4,
                                                  float *__restrict__ s,
-                                                 const float *__restrict__ q, size_t ns4) {
+                                                 const float *__restrict__ q, size_t ns4,
+                                                 const float *__restrict__ w) {
     if (S->done) return;
     const double alpha = S->alpha;
     const size_t stride = (size_t)gridDim.x * 256;
@@ -183,10 +226,19 @@ __global__ void __launch_bounds__(256) k_cgls_xs(SolveState *S, float *__restric
         }
         float4 d = dst[j];
         const float4 v = src[j];
-        d.x = (float)((double)d.x + a * (double)v.x);
-        d.y = (float)((double)d.y + a * (double)v.y);
-        d.z = (float)((double)d.z + a * (double)v.z);
-        d.w = (float)((double)d.w + a * (double)v.w);
+        if (w && i >= nv4) {
+            // weighted residual: s - (alpha q) w (areccgls_stat.cpp:668-669)
+            const float4 wt = reinterpret_cast<const float4 *>(w)[j];
+            d.x = (float)((double)d.x + (a * (double)v.x) * (double)wt.x);
+            d.y = (float)((double)d.y + (a * (double)v.y) * (double)wt.y);
+            d.z = (float)((double)d.z + (a * (double)v.z) * (double)wt.z);
+            d.w = (float)((double)d.w + (a * (double)v.w) * (double)wt.w);
+        } else {
+            d.x = (float)((double)d.x + a * (double)v.x);
+            d.y = (float)((double)d.y + a * (double)v.y);
+            d.z = (float)((double)d.z + a * (double)v.z);
+            d.w = (float)((double)d.w + a * (double)v.w);
+        }
         dst[j] = d;
     }
 }
@@ -349,45 +401,26 @@ static int ensure_workspace(Plan *p, int nvol, int nsin) {
     return ARECGB_OK;
 }
 
-struct SolverScratch {
-    SolveState *state = nullptr;
-    double *hist = nullptr;
-    double *red = nullptr;  // 2 x kRedBlocks partials + 2 scalars
-    int hist_cap = 0;
-    SolveState *h_state = nullptr;  // pinned mirror
-};
 constexpr int kRedBlocks = 1024;
-
-static int scratch_get(Plan *p, SolverScratch &sc, int maxit) {
-    // Per-call scratch: small (a few KB plus the residual history).
-    ARECGB_CUDA(cudaMalloc(&sc.state, sizeof(SolveState)));
-    sc.hist_cap = maxit > 0 ? maxit : 1;
-    ARECGB_CUDA(cudaMalloc(&sc.hist, sizeof(double) * sc.hist_cap));
-    ARECGB_CUDA(cudaMalloc(&sc.red, sizeof(double) * (2 * kRedBlocks + 2)));
-    ARECGB_CUDA(cudaMallocHost(&sc.h_state, sizeof(SolveState)));
-    (void)p;
-    return ARECGB_OK;
-}
-
-static void scratch_free(SolverScratch &sc) {
-    cudaFree(sc.state);
-    cudaFree(sc.hist);
-    cudaFree(sc.red);
-    if (sc.h_state) cudaFreeHost(sc.h_state);
-}
 
 // One CGLS iteration (reference areccgls.cpp:375-456) as a fixed launch sequence.
 static int cgls_iteration(Plan *p, SolveState *S, double *hist, float *x, float *s, float *q,
-                          float *g, float *pd, float *xs, cudaStream_t st) {
+                          float *g, float *pd, float *xs, const float *w, cudaStream_t st) {
     const size_t nv = vol_floats(p), ns = sin_floats(p);
     const int gv = grid_for(nv, 16), gs = grid_for(nv + ns, 16);
     k_cgls_save<<<gv, 256, 0, st>>>(S, x, xs, nv / 4);
     k_cgls_save_done<<<1, 1, 0, st>>>(S);
     k_cgls_p<<<gv, 256, 0, st>>>(S, g, pd, nv / 4);
-    int rc = forward_project(p, pd, q, &S->qnorm2, &S->done, st);
+    int rc = forward_project(p, pd, q, w ? nullptr : &S->qnorm2, &S->done, st);
     if (rc) return rc;
+    if (w) {  // ||A p||^2 weighted
+        k_wsumsq<<<kRedBlocks, 256, 0, st>>>(q, w, ns, p->d_partials);
+        rc = reduce_partials(p->d_partials, kRedBlocks, &S->qnorm2, st);
+        if (rc) return rc;
+        count_launches(2);
+    }
     k_cgls_alpha<<<1, 1, 0, st>>>(S);
-    k_cgls_xs<<<gs, 256, 0, st>>>(S, x, pd, nv / 4, s, q, ns / 4);
+    k_cgls_xs<<<gs, 256, 0, st>>>(S, x, pd, nv / 4, s, q, ns / 4, w);
     rc = back_project(p, s, g, &S->gnorm2, &S->done, st);
     if (rc) return rc;
     k_cgls_gamma<<<1, 1, 0, st>>>(S, hist);
@@ -396,103 +429,238 @@ static int cgls_iteration(Plan *p, SolveState *S, double *hist, float *x, float 
     return ARECGB_OK;
 }
 
+// CGLS over n independent problems (one plan each, uneven shapes allowed).
+// Per problem: s = b - A x0 (x0 = 0 unless warm), g = A^T s, gamma = ||g||^2
+// (areccgls.cpp:323-372), launched eagerly with the first iteration (which
+// also configures every kernel).  Then one CUDA graph captures one iteration
+// of ALL problems, each problem a parallel branch, and the solve replays it;
+// a problem that has met its stopping test turns its kernels into no-ops, and
+// the host polls the n done flags with one copy after 1, 2, 4, 8, 8, ...
+// iterations.  Finally the reference's best-iterate restore, per problem.
+int cgls_batch(Plan *const *plans, const float *const *d_b, float *const *d_x, const int *warm,
+               int n, int maxit, float tol, const double *rnorm_ref, double *const *hist_host,
+               arecgb_solve_info *info, cudaStream_t st, const float *const *d_w) {
+    if (n < 1 || !plans || !d_b || !d_x) {
+        set_error("cgls: bad batch arguments");
+        return ARECGB_ERR_ARG;
+    }
+    for (int i = 0; i < n; i++) {
+        if (!plans[i] || !d_b[i] || !d_x[i]) {
+            set_error("cgls: null plan or buffer in the batch");
+            return ARECGB_ERR_ARG;
+        }
+        for (int j = 0; j < i; j++)
+            if (plans[j] == plans[i]) {
+                set_error("cgls: a plan appears twice in the batch (each needs its own workspace)");
+                return ARECGB_ERR_ARG;
+            }
+        int rc = ensure_workspace(plans[i], 3, 2);
+        if (rc) return rc;
+    }
+    const int cap = maxit > 0 ? maxit : 1;
+    SolveState *S = nullptr, *H = nullptr;
+    double *hist = nullptr;
+    cudaStream_t cs = nullptr;
+    std::vector<cudaStream_t> bs;
+    std::vector<cudaEvent_t> ev;
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t exec = nullptr;
+    int rc = 0;
+    long long per_iter = 0;
+    auto fail = [&](cudaError_t e, const char *what) {
+        set_error(std::string("cgls: ") + what + ": " + cudaGetErrorString(e));
+        rc = cuda_status(e);
+    };
+    auto iteration = [&](int i, cudaStream_t s_) {
+        Plan *p = plans[i];
+        return cgls_iteration(p, S + i, hist + (size_t)i * cap, d_x[i], p->d_sin[0], p->d_sin[1],
+                              p->d_vol[0], p->d_vol[1], p->d_vol[2], d_w ? d_w[i] : nullptr, s_);
+    };
+    cudaError_t e = cudaMalloc(&S, sizeof(SolveState) * n);
+    if (e == cudaSuccess) e = cudaMalloc(&hist, sizeof(double) * n * (size_t)cap);
+    if (e == cudaSuccess) e = cudaMallocHost(&H, sizeof(SolveState) * n);
+    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking);
+    for (int i = 0; e == cudaSuccess && i < n + 2; i++) {
+        cudaEvent_t x;
+        e = cudaEventCreateWithFlags(&x, cudaEventDisableTiming);
+        if (e == cudaSuccess) ev.push_back(x);
+    }
+    for (int i = 0; e == cudaSuccess && n > 1 && i < n; i++) {
+        cudaStream_t x;
+        e = cudaStreamCreateWithFlags(&x, cudaStreamNonBlocking);
+        if (e == cudaSuccess) bs.push_back(x);
+    }
+    if (e != cudaSuccess) fail(e, "setup");
+    // the solve runs on cs, ordered after the caller's stream
+    if (!rc) {
+        e = cudaEventRecord(ev[0], st);
+        if (e == cudaSuccess) e = cudaStreamWaitEvent(cs, ev[0], 0);
+        if (e == cudaSuccess) e = cudaMemsetAsync(S, 0, sizeof(SolveState) * n, cs);
+        if (e != cudaSuccess) fail(e, "setup");
+    }
+    for (int i = 0; !rc && i < n; i++) {
+        Plan *p = plans[i];
+        const size_t nv = vol_floats(p), ns = sin_floats(p);
+        float *s_ = p->d_sin[0], *q = p->d_sin[1], *g = p->d_vol[0];
+        const float *wi = d_w ? d_w[i] : nullptr;
+        if (warm && warm[i]) {
+            rc = forward_project(p, d_x[i], q, nullptr, nullptr, cs);
+            if (rc) break;
+            if (wi)
+                k_sub_w<<<grid_for(ns, 16), 256, 0, cs>>>(d_b[i], q, wi, s_, ns);
+            else
+                k_sub<<<grid_for(ns, 16), 256, 0, cs>>>(d_b[i], q, s_, ns);
+            count_launches(1);
+        } else {
+            cudaMemsetAsync(d_x[i], 0, sizeof(float) * nv, cs);
+            if (wi) {
+                k_sub_w<<<grid_for(ns, 16), 256, 0, cs>>>(d_b[i], nullptr, wi, s_, ns);
+                count_launches(1);
+            } else {
+                cudaMemcpyAsync(s_, d_b[i], sizeof(float) * ns, cudaMemcpyDeviceToDevice, cs);
+            }
+        }
+        rc = back_project(p, s_, g, &S[i].gnorm2, nullptr, cs);
+        if (rc) break;
+        k_cgls_init<<<1, 1, 0, cs>>>(S + i, maxit, tol, rnorm_ref ? rnorm_ref[i] : 0.0);
+        count_launches(1);
+    }
+    // first iteration eagerly, then capture one iteration of every problem
+    for (int i = 0; !rc && maxit > 0 && i < n; i++) rc = iteration(i, cs);
+    int launched = maxit > 0 ? 1 : 0;
+    if (!rc && maxit > 1) {
+        const long long c0 = launch_count();
+        e = cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal);
+        if (e != cudaSuccess) {
+            fail(e, "stream capture");
+        } else {
+            if (n == 1) {
+                rc = iteration(0, cs);
+            } else {
+                cudaEventRecord(ev[1], cs);
+                for (int i = 0; !rc && i < n; i++) {
+                    cudaStreamWaitEvent(bs[i], ev[1], 0);
+                    rc = iteration(i, bs[i]);
+                    cudaEventRecord(ev[2 + i], bs[i]);
+                    cudaStreamWaitEvent(cs, ev[2 + i], 0);
+                }
+            }
+            e = cudaStreamEndCapture(cs, &graph);
+            if (!rc && e != cudaSuccess) fail(e, "stream capture");
+            if (!rc) {
+                e = cudaGraphInstantiate(&exec, graph, 0);
+                if (e != cudaSuccess) fail(e, "graph instantiation");
+            }
+        }
+        per_iter = launch_count() - c0;
+    }
+    // replay until every problem has stopped
+    int batch = 1;
+    while (!rc) {
+        e = cudaMemcpyAsync(H, S, sizeof(SolveState) * n, cudaMemcpyDeviceToHost, cs);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(cs);
+        if (e != cudaSuccess) {
+            fail(e, "poll");
+            break;
+        }
+        bool all = true;
+        for (int i = 0; i < n; i++) all = all && H[i].done;
+        if (all || launched >= maxit) break;
+        const int nb = std::min(batch, maxit - launched);
+        for (int k = 0; k < nb && !rc; k++) {
+            e = cudaGraphLaunch(exec, cs);
+            if (e != cudaSuccess) fail(e, "graph launch");
+            count_launches((int)per_iter);
+        }
+        launched += nb;
+        batch = std::min(batch * 2, 8);
+    }
+    // flush pending best-iterate copies, then restore them where the reference would
+    for (int i = 0; !rc && i < n; i++) {
+        Plan *p = plans[i];
+        const size_t nv = vol_floats(p);
+        k_cgls_save<<<grid_for(nv, 16), 256, 0, cs>>>(S + i, d_x[i], p->d_vol[2], nv / 4);
+        k_cgls_save_done<<<1, 1, 0, cs>>>(S + i);
+        count_launches(2);
+    }
+    if (!rc) {
+        e = cudaMemcpyAsync(H, S, sizeof(SolveState) * n, cudaMemcpyDeviceToHost, cs);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(cs);
+        if (e != cudaSuccess) fail(e, "final state");
+    }
+    for (int i = 0; !rc && i < n; i++) {
+        Plan *p = plans[i];
+        if (H[i].iterbest < maxit - 1)
+            cudaMemcpyAsync(d_x[i], p->d_vol[2], sizeof(float) * vol_floats(p),
+                            cudaMemcpyDeviceToDevice, cs);
+        if (hist_host && hist_host[i] && H[i].iterations > 0)
+            cudaMemcpyAsync(hist_host[i], hist + (size_t)i * cap,
+                            sizeof(double) * std::min(H[i].iterations, cap), cudaMemcpyDeviceToHost,
+                            cs);
+        if (info) {
+            info[i].iterations = H[i].iterations;
+            info[i].iterbest = H[i].iterbest;
+            info[i].restarts = 0;
+            info[i].status = 0;
+            info[i].lam_final = 0.f;
+            info[i].rnorm0 = H[i].rnorm0;
+            info[i].rel_final = H[i].rel;
+        }
+    }
+    if (!rc) {
+        e = cudaStreamSynchronize(cs);
+        if (e == cudaSuccess) e = cudaGetLastError();
+        if (e != cudaSuccess) fail(e, "finish");
+    }
+    // the caller's stream continues after the solve
+    if (cs && !ev.empty()) {
+        cudaEventRecord(ev[0], cs);
+        cudaStreamWaitEvent(st, ev[0], 0);
+    }
+    if (exec) cudaGraphExecDestroy(exec);
+    if (graph) cudaGraphDestroy(graph);
+    cudaStreamSynchronize(cs);
+    for (cudaStream_t x : bs) cudaStreamDestroy(x);
+    if (cs) cudaStreamDestroy(cs);
+    for (cudaEvent_t x : ev) cudaEventDestroy(x);
+    cudaFree(S);
+    cudaFree(hist);
+    if (H) cudaFreeHost(H);
+    return rc;
+}
+
 int cgls(Plan *p, const float *d_b, float *d_x, int warm, int maxit, float tol, double rnorm_ref,
          double *hist_host, arecgb_solve_info *info, cudaStream_t st) {
-    int rc = ensure_workspace(p, 3, 2);
-    if (rc) return rc;
-    const size_t nv = vol_floats(p), ns = sin_floats(p);
-    float *s = p->d_sin[0], *q = p->d_sin[1];
-    float *g = p->d_vol[0], *pd = p->d_vol[1], *xs = p->d_vol[2];
-    SolverScratch sc;
-    rc = scratch_get(p, sc, maxit);
-    if (rc) {
-        scratch_free(sc);
-        return rc;
+    return cgls_batch(&p, &d_b, &d_x, &warm, 1, maxit, tol, &rnorm_ref, &hist_host, info, st,
+                      nullptr);
+}
+
+// Statistically weighted CGLS (cyl_cgls[_KB|_SQ]_stat, areccgls_stat.cpp:49-731):
+// the CGLS above with w = stat weights of b on the residual and in ||A p||^2;
+// the stopping test is relative to the initial weighted gradient norm.
+int cgls_stat(Plan *p, const float *d_b, float *d_x, int warm, int maxit, float tol,
+              double *hist_host, arecgb_solve_info *info, cudaStream_t st) {
+    const size_t ns = sin_floats(p);
+    if (!p->d_w) ARECGB_CUDA(cudaMalloc(&p->d_w, sizeof(float) * ns));
+    std::vector<double> hx(p->nx);
+    const double alpha = 0.5, pi = std::atan(1.0) * 4.0;
+    const double xa = 0.5 * alpha * (p->nx - 1), xb = (1.0 - 0.5 * alpha) * (p->nx - 1);
+    const double A = 2.0 * pi / alpha;
+    for (int x = 0; x < p->nx; x++) {
+        const double va = 0.5 * (1.0 + std::cos(A * (1.0 * x / (p->nx - 1) - alpha / 2)));
+        const double vb = 0.5 * (1.0 + std::cos(A * (1.0 * x / (p->nx - 1) - 1.0 + alpha / 2)));
+        hx[x] = x < xa ? va : (x > xb ? vb : 1.0);
     }
-    SolveState *S = sc.state;
-    // s = b - A x0 (areccgls.cpp:323-346); x0 = 0 unless warm.
-    if (warm) {
-        rc = forward_project(p, d_x, q, nullptr, nullptr, st);
-        if (rc) goto done;
-        k_sub<<<grid_for(ns, 16), 256, 0, st>>>(d_b, q, s, ns);
-        count_launches(1);
-    } else {
-        cudaMemsetAsync(d_x, 0, sizeof(float) * nv, st);
-        cudaMemcpyAsync(s, d_b, sizeof(float) * ns, cudaMemcpyDeviceToDevice, st);
-    }
-    // g = A^T s; gamma = ||g||^2 (areccgls.cpp:358-372).
-    cudaMemsetAsync(S, 0, sizeof(SolveState), st);
-    rc = back_project(p, s, g, &S->gnorm2, nullptr, st);
-    if (rc) goto done;
-    k_cgls_init<<<1, 1, 0, st>>>(S, maxit, tol, rnorm_ref);
+    double *d_hx = nullptr;
+    ARECGB_CUDA(cudaMallocAsync(&d_hx, sizeof(double) * p->nx, st));
+    ARECGB_CUDA(cudaMemcpyAsync(d_hx, hx.data(), sizeof(double) * p->nx, cudaMemcpyHostToDevice, st));
+    k_stat_weights<<<grid_for(ns, 16), 256, 0, st>>>(d_b, d_hx, p->d_w, ns, p->nx, p->ys);
     count_launches(1);
-    {
-        // Iterations are queued in batches; the stopping test runs on the device
-        // and later queued iterations return at once.
-        int launched = 0;
-        int batch = 1;
-        while (launched < maxit) {
-            const int nb = std::min(batch, maxit - launched);
-            for (int i = 0; i < nb; i++) {
-                rc = cgls_iteration(p, S, sc.hist, d_x, s, q, g, pd, xs, st);
-                if (rc) goto done;
-            }
-            launched += nb;
-            cudaError_t e =
-                cudaMemcpyAsync(sc.h_state, S, sizeof(SolveState), cudaMemcpyDeviceToHost, st);
-            if (e == cudaSuccess) e = cudaStreamSynchronize(st);
-            if (e != cudaSuccess) {
-                set_error(std::string("cgls: ") + cudaGetErrorString(e));
-                rc = cuda_status(e);
-                goto done;
-            }
-            if (sc.h_state->done) break;
-            batch = std::min(batch * 2, 8);
-        }
-        // flush a pending best-iterate copy, then restore it if the reference would
-        k_cgls_save<<<grid_for(nv, 16), 256, 0, st>>>(S, d_x, xs, nv / 4);
-        k_cgls_save_done<<<1, 1, 0, st>>>(S);
-        count_launches(2);
-        cudaError_t e =
-            cudaMemcpyAsync(sc.h_state, S, sizeof(SolveState), cudaMemcpyDeviceToHost, st);
-        if (e == cudaSuccess) e = cudaStreamSynchronize(st);
-        if (e != cudaSuccess) {
-            set_error(std::string("cgls: ") + cudaGetErrorString(e));
-            rc = cuda_status(e);
-            goto done;
-        }
-        const SolveState &H = *sc.h_state;
-        if (H.iterbest < maxit - 1)
-            cudaMemcpyAsync(d_x, xs, sizeof(float) * nv, cudaMemcpyDeviceToDevice, st);
-        if (hist_host && H.iterations > 0)
-            cudaMemcpyAsync(hist_host, sc.hist, sizeof(double) * H.iterations,
-                            cudaMemcpyDeviceToHost, st);
-        e = cudaStreamSynchronize(st);
-        if (e != cudaSuccess) {
-            set_error(std::string("cgls: ") + cudaGetErrorString(e));
-            rc = cuda_status(e);
-            goto done;
-        }
-        if (info) {
-            info->iterations = H.iterations;
-            info->iterbest = H.iterbest;
-            info->restarts = 0;
-            info->status = 0;
-            info->lam_final = 0.f;
-            info->rnorm0 = H.rnorm0;
-            info->rel_final = H.rel;
-        }
-    }
-done:
-    scratch_free(sc);
-    if (rc == 0) {
-        cudaError_t e = cudaGetLastError();
-        if (e != cudaSuccess) {
-            set_error(std::string("cgls: ") + cudaGetErrorString(e));
-            rc = cuda_status(e);
-        }
-    }
-    return rc;
+    ARECGB_CUDA(cudaFreeAsync(d_hx, st));
+    ARECGB_CUDA(cudaStreamSynchronize(st));  // hx is host memory
+    const float *w = p->d_w;
+    const double zero = 0.0;
+    return cgls_batch(&p, &d_b, &d_x, &warm, 1, maxit, tol, &zero, &hist_host, info, st, &w);
 }
 
 // SIRT with the reference's control flow (arecsirt.cpp:267-362): the step size

@@ -32,6 +32,22 @@ __device__ __forceinline__ uint64_t smem_desc(uint32_t saddr, uint32_t lbo, uint
     return d;
 }
 
+// Shared-memory matrix descriptor for a K-major operand stored with the 64-byte
+// swizzle (rows of 64 bytes = 32 bf16 of K, 8-row atoms of 512 bytes, as a TMA
+// load with CU_TENSOR_MAP_SWIZZLE_64B writes it): stride byte offset 512 between
+// 8-row groups, leading byte offset unused (1), layout type 4 in [61,64).  The
+// tile base must be 512-byte aligned; the k-th 16-element step starts 32*k
+// bytes further.
+__device__ __forceinline__ uint64_t smem_desc_sw64(uint32_t saddr) {
+    uint64_t d = 0;
+    d |= (uint64_t)((saddr >> 4) & 0x3FFF);
+    d |= (uint64_t)1 << 16;            // leading byte offset (unused for this layout)
+    d |= (uint64_t)(512 >> 4) << 32;   // stride byte offset
+    d |= (uint64_t)1 << 46;            // version
+    d |= (uint64_t)4 << 61;            // 64-byte swizzle
+    return d;
+}
+
 // Instruction descriptor, kind::f16: D = F32, A = B = BF16, both K-major,
 // N >> 3 in [17,23), M >> 4 in [24,29).
 __host__ __device__ constexpr uint32_t idesc_bf16(int M, int N) {
@@ -141,6 +157,24 @@ __device__ __forceinline__ void bulk_g2s(void *dst, const void *src, uint32_t by
         "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];\n" ::
             "r"(smem_addr(dst)),
         "l"(src), "r"(bytes), "r"(smem_addr(mbar))
+        : "memory");
+}
+
+// Tiled TMA loads (cp.async.bulk.tensor), completing on `mbar`.
+__device__ __forceinline__ void tma_load_3d(void *dst, const void *tmap, int c0, int c1, int c2,
+                                            uint64_t *mbar) {
+    asm volatile(
+        "cp.async.bulk.tensor.3d.shared::cluster.global.tile.mbarrier::complete_tx::bytes "
+        "[%0], [%1, {%2, %3, %4}], [%5];\n" ::"r"(smem_addr(dst)),
+        "l"(tmap), "r"(c0), "r"(c1), "r"(c2), "r"(smem_addr(mbar))
+        : "memory");
+}
+__device__ __forceinline__ void tma_load_4d(void *dst, const void *tmap, int c0, int c1, int c2,
+                                            int c3, uint64_t *mbar) {
+    asm volatile(
+        "cp.async.bulk.tensor.4d.shared::cluster.global.tile.mbarrier::complete_tx::bytes "
+        "[%0], [%1, {%2, %3, %4, %5}], [%6];\n" ::"r"(smem_addr(dst)),
+        "l"(tmap), "r"(c0), "r"(c1), "r"(c2), "r"(c3), "r"(smem_addr(mbar))
         : "memory");
 }
 

@@ -16,8 +16,11 @@
 //
 // The same kernel computes the data gradient of a convolution from the
 // spatially flipped, channel-transposed weights.
+#include <cuda.h>  // CUtensorMap and its enums (the encoder comes from the runtime's entry point)
 #include <cuda_bf16.h>
 #include <stdint.h>
+
+#include <mutex>
 
 #include "arec_internal.cuh"
 #include "arec_umma.cuh"
@@ -172,8 +175,185 @@ static int launch_conv(const __nv_bfloat16 *X, const __nv_bfloat16 *Wt, const fl
     return 0;
 }
 
-// layout: 0 = (LBO 128, SBO 256) [K-halves 128 B apart, row groups 256 B apart],
-//         1 = the two offsets exchanged (for validating the descriptor fields).
+// ---------------------------------------------------------------------------
+// TMA path (image widths that are multiples of 128): a tile is 128 consecutive
+// pixels of one image row.  Per K chunk (one tap, 32 input channels) one TMA
+// load brings the tile's shifted neighbours from an NHWC tensor map (box 32
+// channels x 128 pixels; rows and columns outside the image arrive as zeros,
+// which is the convolution's padding) and one the chunk's weights from a
+// [Cout][9][Cin] tensor map, both with the 64-byte swizzle the tensor core
+// reads directly.  Four stages: thread 0 of warp 0 issues the loads, thread 0
+// of warp 1 the MMAs; each stage's commit frees it for the loads four chunks
+// later.  All four warps run the epilogue from TMEM.
+constexpr int kTmaStages = 4;
+
+template <int COUT>
+struct TmaCfg {
+    static constexpr int A_BYTES = 128 * 64;  // 128 pixels x 32 channels
+    static constexpr int B_BYTES = COUT * 64;
+    static constexpr int STAGE = A_BYTES + B_BYTES;  // a multiple of 1024
+    static constexpr int SMEM = kTmaStages * STAGE + 1024;
+    static constexpr uint32_t NCOLS = COUT < 32 ? 32 : COUT;
+};
+
+template <int COUT>
+__global__ void __launch_bounds__(128)
+    conv3x3_tma_kernel(const __grid_constant__ CUtensorMap tmX, const __grid_constant__ CUtensorMap tmW,
+                       const float *__restrict__ bias, __nv_bfloat16 *__restrict__ Y, int H,
+                       int Wd, int Cin, int relu, int ystride, int *err) {
+    using Cfg = TmaCfg<COUT>;
+    extern __shared__ unsigned char sm_raw[];
+    __shared__ __align__(8) uint64_t full[kTmaStages], empty[kTmaStages], done;
+    __shared__ uint32_t tmem_base;
+    const uint32_t raw = umma::smem_addr(sm_raw);
+    unsigned char *sm = sm_raw + ((1024u - (raw & 1023u)) & 1023u);  // 1024-byte aligned stages
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    const int p0 = blockIdx.x * 128;
+    const int hw = H * Wd;
+    const int n = p0 / hw, h = (p0 / Wd) % H, w0 = p0 % Wd;
+
+    if (warp == 0) {
+        umma::tmem_alloc(&tmem_base, Cfg::NCOLS);
+        umma::tmem_relinquish();
+    }
+    if (tid == 0) {
+        for (int st = 0; st < kTmaStages; st++) {
+            umma::mbar_init(&full[st], 1);
+            umma::mbar_init(&empty[st], 1);
+        }
+        umma::mbar_init(&done, 1);
+        umma::mbar_fence_init();
+    }
+    umma::fence_before_sync();
+    __syncthreads();
+    umma::fence_after_sync();
+    const uint32_t tmem = tmem_base;
+    const int cchunks = Cin / kConvKC, nchunks = 9 * cchunks;
+
+    if (warp == 0 && lane == 0) {
+        bool ok = true;
+        for (int c = 0; c < nchunks && ok; c++) {
+            const int st = c % kTmaStages;
+            if (c >= kTmaStages &&
+                !umma::mbar_wait(&empty[st], (uint32_t)(c / kTmaStages - 1) & 1u, kWaitLimit)) {
+                ok = false;
+                atomicOr(err, 4);
+                break;
+            }
+            const int tap = c / cchunks, c0 = (c % cchunks) * kConvKC;
+            unsigned char *A = sm + st * Cfg::STAGE;
+            umma::mbar_arrive_expect_tx(&full[st], (uint32_t)Cfg::STAGE);
+            umma::tma_load_4d(A, &tmX, c0, w0 + tap % 3 - 1, h + tap / 3 - 1, n, &full[st]);
+            umma::tma_load_3d(A + Cfg::A_BYTES, &tmW, c0, tap, 0, &full[st]);
+        }
+    } else if (warp == 1 && lane == 0) {
+        constexpr uint32_t idesc = umma::idesc_bf16(128, COUT);
+        for (int c = 0; c < nchunks; c++) {
+            const int st = c % kTmaStages;
+            if (!umma::mbar_wait(&full[st], (uint32_t)(c / kTmaStages) & 1u, kWaitLimit)) {
+                atomicOr(err, 4);
+                break;
+            }
+            umma::fence_after_sync();
+            const uint32_t a = umma::smem_addr(sm + st * Cfg::STAGE), b = a + Cfg::A_BYTES;
+#pragma unroll
+            for (int k = 0; k < 2; k++)
+                umma::mma_bf16(tmem, umma::smem_desc_sw64(a + 32 * k),
+                               umma::smem_desc_sw64(b + 32 * k), idesc, (c > 0 || k > 0) ? 1u : 0u);
+            umma::mma_commit(&empty[st]);
+        }
+        umma::mma_commit(&done);  // arrives when every MMA above has completed
+    }
+    __syncwarp();
+    const bool dok = __all_sync(0xffffffffu, umma::mbar_wait(&done, 0, kWaitLimit));
+    umma::fence_after_sync();
+    if (!dok && lane == 0) atomicOr(err, 4);
+    if (dok) {
+        const int p = p0 + tid;  // TMEM lane = pixel
+#pragma unroll 1
+        for (int cc = 0; cc < COUT / 32; cc++) {
+            float v[32];
+            umma::tmem_ld32(tmem + ((uint32_t)(32 * warp) << 16) + (uint32_t)(cc * 32), v);
+            __align__(16) __nv_bfloat16 out[32];
+#pragma unroll
+            for (int i = 0; i < 32; i++) {
+                float t = v[i] + (bias ? bias[cc * 32 + i] : 0.f);
+                if (relu) t = fmaxf(t, 0.f);
+                out[i] = __float2bfloat16(t);
+            }
+            uint4 *dst = reinterpret_cast<uint4 *>(Y + (size_t)p * ystride + cc * 32);
+#pragma unroll
+            for (int q = 0; q < 4; q++) dst[q] = reinterpret_cast<const uint4 *>(out)[q];
+        }
+    }
+    umma::fence_before_sync();
+    __syncthreads();
+    if (warp == 0) umma::tmem_dealloc(tmem, Cfg::NCOLS);
+}
+
+typedef CUresult (*EncodeTiledFn)(CUtensorMap *, CUtensorMapDataType, cuuint32_t, void *,
+                                  const cuuint64_t *, const cuuint64_t *, const cuuint32_t *,
+                                  const cuuint32_t *, CUtensorMapInterleave, CUtensorMapSwizzle,
+                                  CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+
+static EncodeTiledFn encode_tiled() {
+    static std::once_flag once;
+    static EncodeTiledFn fn = nullptr;
+    std::call_once(once, [] {
+        void *p = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault,
+                                             &q) == cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            fn = reinterpret_cast<EncodeTiledFn>(p);
+    });
+    return fn;
+}
+
+// Tensor maps of one convolution; false if the driver refuses them (the
+// caller then uses the gather kernel).
+static bool conv_tensor_maps(const __nv_bfloat16 *x, const __nv_bfloat16 *w, int N, int H, int Wd,
+                             int Cin, int Cout, CUtensorMap *tx, CUtensorMap *tw) {
+    EncodeTiledFn enc = encode_tiled();
+    if (!enc) return false;
+    const cuuint64_t xd[4] = {(cuuint64_t)Cin, (cuuint64_t)Wd, (cuuint64_t)H, (cuuint64_t)N};
+    const cuuint64_t xs[3] = {(cuuint64_t)Cin * 2, (cuuint64_t)Wd * Cin * 2,
+                              (cuuint64_t)H * Wd * Cin * 2};
+    const cuuint32_t xb[4] = {(cuuint32_t)kConvKC, 128, 1, 1};
+    const cuuint32_t one[4] = {1, 1, 1, 1};
+    if (enc(tx, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 4, (void *)x, xd, xs, xb, one,
+            CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_64B,
+            CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) != CUDA_SUCCESS)
+        return false;
+    const cuuint64_t wd[3] = {(cuuint64_t)Cin, 9, (cuuint64_t)Cout};
+    const cuuint64_t ws[2] = {(cuuint64_t)Cin * 2, (cuuint64_t)9 * Cin * 2};
+    const cuuint32_t wb[3] = {(cuuint32_t)kConvKC, 1, (cuuint32_t)Cout};
+    return enc(tw, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 3, (void *)w, wd, ws, wb, one,
+               CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_64B,
+               CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+}
+
+template <int COUT>
+static int launch_conv_tma(const CUtensorMap &tx, const CUtensorMap &tw, const float *bias,
+                           __nv_bfloat16 *Y, int H, int Wd, int Cin, int P, int relu, int ystride,
+                           int *err, cudaStream_t st) {
+    using Cfg = TmaCfg<COUT>;
+    static bool configured = false;
+    if (!configured) {
+        ARECGB_CUDA(cudaFuncSetAttribute(conv3x3_tma_kernel<COUT>,
+                                         cudaFuncAttributeMaxDynamicSharedMemorySize, Cfg::SMEM));
+        configured = true;
+    }
+    conv3x3_tma_kernel<COUT><<<P / 128, 128, Cfg::SMEM, st>>>(tx, tw, bias, Y, H, Wd, Cin, relu,
+                                                              ystride, err);
+    ARECGB_CUDA(cudaGetLastError());
+    return 0;
+}
+
+// layout: 0 = TMA path when the width is a multiple of 128, else the gather
+//         kernel with (LBO 128, SBO 256) [K-halves 128 B apart, row groups 256 B
+//         apart]; 1 = the gather kernel with the two offsets exchanged (for
+//         validating the descriptor fields); 2 = the gather kernel always.
 int conv3x3_bf16(const void *X, const void *Wt, const float *bias, void *Y, int N, int H, int Wd,
                  int Cin, int Cout, int relu, int layout, int *err, cudaStream_t st, int ystride) {
     if (ystride <= 0) ystride = Cout;
@@ -186,6 +366,16 @@ int conv3x3_bf16(const void *X, const void *Wt, const float *bias, void *Y, int 
     const auto *w = reinterpret_cast<const __nv_bfloat16 *>(Wt);
     auto *y = reinterpret_cast<__nv_bfloat16 *>(Y);
     const int P = N * H * Wd;
+    if (layout == 0 && Wd % 128 == 0) {
+        CUtensorMap tx, tw;
+        if (conv_tensor_maps(x, w, N, H, Wd, Cin, Cout, &tx, &tw)) {
+#define ARECGB_CONV_TMA(C) \
+    if (Cout == C) return launch_conv_tma<C>(tx, tw, bias, y, H, Wd, Cin, P, relu, ystride, err, st);
+            ARECGB_CONV_TMA(32) ARECGB_CONV_TMA(64) ARECGB_CONV_TMA(128) ARECGB_CONV_TMA(256)
+#undef ARECGB_CONV_TMA
+        }
+    }
+    if (layout == 2) layout = 0;
 #define ARECGB_CONV(C)                                                                     \
     if (Cout == C)                                                                         \
         return layout ? launch_conv<C, 256, 128>(x, w, bias, y, H, Wd, Cin, P, relu, ystride, err, st) \

@@ -58,24 +58,28 @@ def make_problem(gb, nx, na, slices, photons, seed, kind="sphere", device="cuda"
     return plan, b
 
 
-def make_pairs(gb, nx, na, slices, photons, seed, kind="sphere", sirt_iters=SIRT_ITERS,
+def make_pairs(gb, nx, na, slices, photons, seed, kind="sphere", sirt_iters=(SIRT_ITERS,),
                cgls_iters=CGLS_ITERS):
-    """(input, target) image stacks [slices][npad][npad] on the device."""
+    """{k: (input, target)} image stacks [slices][npad][npad] on the device, one
+    pair per SIRT depth k in `sirt_iters` (the CGLS target is shared)."""
     import torch
 
     plan, b = make_problem(gb, nx, na, slices, photons, seed, kind)
-    xs = torch.zeros(plan.nrays, plan.ys, device="cuda")
-    plan.sirt(b, xs, sirt_lambda(plan), sirt_iters, 0.0)
-    xc = torch.zeros_like(xs)
+    xc = torch.zeros(plan.nrays, plan.ys, device="cuda")
     plan.cgls(b, xc, cgls_iters, 0.0)
-    rms = volume_rms(plan, xs)
+    xs = torch.zeros_like(xc)
     npad = pad8(plan.nx)
-    inp = torch.empty(slices, npad, npad, device="cuda")
-    tgt = torch.empty_like(inp)
-    gb.images_from_volume(plan, xs, inp, npad, 0, slices, 1.0 / rms)
-    gb.images_from_volume(plan, xc, tgt, npad, 0, slices, 1.0 / rms)
+    out = {}
+    for k in sirt_iters:
+        plan.sirt(b, xs, sirt_lambda(plan), k, 0.0)
+        rms = volume_rms(plan, xs)
+        inp = torch.empty(slices, npad, npad, device="cuda")
+        tgt = torch.empty_like(inp)
+        gb.images_from_volume(plan, xs, inp, npad, 0, slices, 1.0 / rms)
+        gb.images_from_volume(plan, xc, tgt, npad, 0, slices, 1.0 / rms)
+        out[k] = (inp, tgt)
     torch.cuda.synchronize()
-    return inp, tgt
+    return out
 
 
 def random_crops(gen, inp, tgt, batch, crop, out_in, out_tgt):
@@ -143,10 +147,12 @@ def load(gb, path, size, max_batch):
     if net.nparams != params.size or json.loads(str(z["layers"])) != net.layers:
         raise ValueError("%s: parameter layout does not match this library's network" % path)
     net.set_params(torch.from_numpy(params.copy()).cuda())
-    return net, json.loads(str(z["meta"]))
+    meta = json.loads(str(z["meta"]))
+    net.sirt_iters = int(meta.get("sirt_iters", SIRT_ITERS))
+    return net, meta
 
 
-def solve(gb, plan, b, x, net=None, tol=1e-3, maxit=200, sirt_iters=SIRT_ITERS, scratch=None):
+def solve(gb, plan, b, x, net=None, tol=1e-3, maxit=200, sirt_iters=None, scratch=None):
     """CGLS to ||A^T r|| / ||A^T b|| <= tol, warm-started by the network when
     `net` is given (SIRT -> U-Net -> CGLS), else from zero.  Returns
     (CGLS info, seconds of each stage)."""
@@ -156,6 +162,8 @@ def solve(gb, plan, b, x, net=None, tol=1e-3, maxit=200, sirt_iters=SIRT_ITERS, 
     t = time.perf_counter()
     rnorm_ref = 0.0
     if net is not None:
+        if sirt_iters is None:
+            sirt_iters = getattr(net, "sirt_iters", SIRT_ITERS)
         _, sinfo = plan.sirt(b, x, sirt_lambda(plan), sirt_iters, 0.0)
         rnorm_ref = sinfo.rnorm0  # ||A^T b||, the cold start's denominator
         torch.cuda.synchronize()
@@ -175,40 +183,47 @@ def solve(gb, plan, b, x, net=None, tol=1e-3, maxit=200, sirt_iters=SIRT_ITERS, 
 
 
 def main():
-    import torch
-
     import arec3d_gb300 as gb
 
     ap = argparse.ArgumentParser(description=__doc__.split("\n\n")[0])
-    ap.add_argument("--out", default=DEFAULT_WEIGHTS)
+    ap.add_argument("--out", default=DEFAULT_WEIGHTS,
+                    help="weights file; with several --sirt-iters, _sirt<k> is appended")
+    ap.add_argument("--sirt-iters", default=str(SIRT_ITERS),
+                    help="SIRT depth(s) of the network input, comma separated")
     ap.add_argument("--steps", type=int, default=3000)
     ap.add_argument("--batch", type=int, default=16)
     ap.add_argument("--crop", type=int, default=256)
     ap.add_argument("--lr", type=float, default=1e-3)
-    ap.add_argument("--sets", default="1024:1200:32:5e3:sphere:6,512:360:64:1e4:sphere:4,"
-                    "512:360:64:1e4:ellipse:4",
+    ap.add_argument("--sets", default="1024:1200:256:5e3:sphere:2,512:360:128:1e4:sphere:3,"
+                    "512:360:128:1e4:ellipse:3",
                     help="nx:angles:slices:photons:kind:volumes, comma separated")
     ap.add_argument("--seed", type=int, default=50000)
     args = ap.parse_args()
     gb.build()
-    datasets, desc = [], []
+    ks = [int(k) for k in args.sirt_iters.split(",")]
+    datasets = {k: [] for k in ks}
+    desc = []
     seed = args.seed
     t0 = time.time()
     for spec in args.sets.split(","):
         nx, na, sl, ph, kind, nv = spec.split(":")
-        for v in range(int(nv)):
-            inp, tgt = make_pairs(gb, int(nx), int(na), int(sl), float(ph), seed, kind)
-            datasets.append((inp, tgt))
+        for _ in range(int(nv)):
+            pairs = make_pairs(gb, int(nx), int(na), int(sl), float(ph), seed, kind, ks)
+            for k in ks:
+                datasets[k].append(pairs[k])
             seed += 7
         desc.append(spec)
         print("pairs %s done %.1fs" % (spec, time.time() - t0), flush=True)
-    net, hist = train(gb, datasets, steps=args.steps, batch=args.batch, crop=args.crop,
-                      lr=args.lr, seed=args.seed)
-    meta = {"sirt_iters": SIRT_ITERS, "cgls_iters": CGLS_ITERS, "sets": desc,
-            "steps": args.steps, "batch": args.batch, "crop": args.crop, "lr": args.lr,
-            "final_loss": float(np.mean(hist[-50:])), "first_loss": float(hist[0])}
-    save(net, args.out, meta)
-    print(json.dumps(meta))
+    for k in ks:
+        net, hist = train(gb, datasets[k], steps=args.steps, batch=args.batch, crop=args.crop,
+                          lr=args.lr, seed=args.seed)
+        meta = {"sirt_iters": k, "cgls_iters": CGLS_ITERS, "sets": desc, "steps": args.steps,
+                "batch": args.batch, "crop": args.crop, "lr": args.lr,
+                "final_loss": float(np.mean(hist[-50:])), "first_loss": float(hist[0])}
+        out = args.out if len(ks) == 1 else args.out.replace(".npz", "_sirt%d.npz" % k)
+        save(net, out, meta)
+        print(json.dumps(dict(meta, out=out)), flush=True)
+        del net
 
 
 if __name__ == "__main__":

@@ -187,6 +187,104 @@ def run_reference(args, rank, world):
     print(json.dumps(out))
 
 
+def extra_config(args):
+    """Measurements of the other benchmark configurations (one JSON line each;
+    not the headline): 1 = SIRT x50 at 256^2 x 64 slices / 180 angles;
+    3 = shift search over 720 pairs of 2048^2 images; 5 = a seeded subset of
+    the uneven batch (cylinders of radius 128-1024, uneven slices and angles)
+    solved by the batched CGLS."""
+    import math
+
+    import torch
+
+    import arec3d_gb300 as gb
+    from arec3d_gb300 import synthetic as syn
+    from arec3d_gb300 import warmstart as ws
+
+    gb.build()
+    st = torch.cuda.current_stream()
+
+    def timed(fn, reps):
+        fn()
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(st)
+        for _ in range(reps):
+            out = fn()
+        e1.record(st)
+        torch.cuda.synchronize()
+        return e0.elapsed_time(e1) / reps, out
+
+    if args.config == 1:
+        nx, ny, na = 256, 64, 180
+        angles = syn.uniform_angles(na)
+        plan = gb.Plan(gb.SQ, 0.5 * (nx - 1), ny, angles)
+        ph = syn.ellipse_phantom(7, nx, ny)
+        b = syn.ellipse_sinogram(ph, nx, ny, angles, ys=plan.ys)
+        syn.poisson_log(b, 1e4, 8, ny)
+        x = torch.zeros(plan.nrays, plan.ys, device="cuda")
+        ms, (hist, info) = timed(lambda: plan.sirt(b, x, 5e-6, 50, 0.0, stream=st), args.steps)
+        out = {"config": 1, "workload": "SIRT x50 (lam 5e-6, tol 0), square-pixel, 256^2 x 64 "
+               "slices, 180 angles, 10 ellipses per slice, Poisson 1e4",
+               "value": ny / (ms / 1e3), "unit": "slices/s", "ms_per_solve": ms,
+               "iterations": info.iterations, "restarts": info.restarts}
+    elif args.config == 3:
+        n, size = 720, 2048
+        g = torch.Generator(device="cuda")
+        g.manual_seed(3)
+        ky = torch.fft.fftfreq(size, device="cuda")[:, None]
+        kx = torch.fft.fftfreq(size, device="cuda")[None, :]
+        lowpass = torch.exp(-((kx ** 2 + ky ** 2) / (2 * 0.02 ** 2)))
+        a = torch.empty(n, size, size, device="cuda")
+        bimg = torch.empty_like(a)
+        shifts = []
+        rng = np.random.default_rng(3)
+        for i in range(0, n, 16):
+            k = min(16, n - i)
+            noise = torch.randn(k, size, size, device="cuda", generator=g)
+            spec = torch.fft.fft2(noise) * lowpass
+            sy = rng.integers(-20, 21, k) + rng.uniform(-0.5, 0.5, k)
+            sx = rng.integers(-20, 21, k) + rng.uniform(-0.5, 0.5, k)
+            shifts += list(zip(sx, sy))
+            ramp = torch.exp(-2j * math.pi * (ky[None] * torch.tensor(sy, device="cuda")[:, None, None]
+                                             + kx[None] * torch.tensor(sx, device="cuda")[:, None, None]))
+            a[i:i + k] = torch.fft.ifft2(spec).real
+            img = torch.fft.ifft2(spec * ramp).real
+            bimg[i:i + k] = img + 0.02 * img.std() * torch.randn(k, size, size, device="cuda",
+                                                                generator=g)
+        sxo = torch.zeros(n, device="cuda")
+        syo = torch.zeros(n, device="cuda")
+        ms, _ = timed(lambda: gb.cc_shifts(a, bimg, sxo, syo, stream=st), args.steps)
+        err = np.abs(np.array(shifts) - np.stack([sxo.cpu().numpy(), syo.cpu().numpy()], 1))
+        out = {"config": 3, "workload": "shift search, 720 pairs of 2048^2 float images "
+               "(integer shifts +-20 px plus sub-pixel +-0.5 px, 2% noise)",
+               "value": n / (ms / 1e3), "unit": "pairs/s", "ms_per_stack": ms,
+               "hbm_gbs": n * 2 * 4 * size * size / (ms / 1e3) / 1e9,
+               "max_abs_shift_error_px": float(err.max())}
+    else:
+        rng = np.random.default_rng(5)
+        k = args.batch_problems
+        plans, bs, xs, sl = [], [], [], 0
+        for i in range(k):
+            r = float(rng.uniform(128, 1024 if i == 0 else 512))
+            nx = int(round(2 * r + 1))
+            ny = int(rng.integers(32, 513)) // 8 * 8 or 8
+            na = int(rng.integers(360, 1801))
+            plan, b = ws.make_problem(gb, nx, na, ny, 5e3, 500 + i, "sphere")
+            plans.append(plan)
+            bs.append(b)
+            xs.append(torch.zeros(plan.nrays, plan.ys, device="cuda"))
+            sl += ny
+        ms, infos = timed(lambda: gb.cgls_batch(plans, bs, xs, 200, 1e-3, stream=st), args.steps)
+        out = {"config": 5, "workload": "uneven batch subset: %d cylinders, radius 128-1024 "
+               "(first) / 128-512, 32-512 slices, 360-1800 angles, Poisson 5e3, batched CGLS "
+               "to 1e-3" % k,
+               "value": sl / (ms / 1e3), "unit": "slices/s", "ms_per_batch": ms,
+               "problems": [{"nx": p.nx, "slices": p.ny, "angles": p.nangles,
+                             "iterations": inf.iterations} for p, inf in zip(plans, infos)]}
+    print(json.dumps(out))
+
+
 def kernels_only(args):
     """Forward and back projector of the benchmark geometry on `--slices`
     slices, `--launches` times each (a short command for ncu)."""
@@ -230,12 +328,18 @@ def main():
     ap.add_argument("--launches", type=int, default=3, help="launches for --kernels-only")
     ap.add_argument("--angles", type=int, default=NA, help="angles for --kernels-only")
     ap.add_argument("--plain", action="store_true", help="plain CGLS only (no warm start)")
+    ap.add_argument("--config", type=int, default=0, choices=[0, 1, 3, 5],
+                    help="measure another benchmark configuration instead of the headline")
+    ap.add_argument("--batch-problems", type=int, default=8, help="problems for --config 5")
     ap.add_argument("--weights", default=os.path.join(ROOT, "arec3d_gb300", "weights",
                                                       "unet_warm_start.npz"))
     args = ap.parse_args()
     rank, local, world = dist_env()
     if args.kernels_only:
         kernels_only(args)
+        return
+    if args.config:
+        extra_config(args)
         return
 
     if args.impl == "reference":
@@ -257,6 +361,11 @@ def main():
     x = torch.zeros(plan.nrays, plan.ys, dtype=torch.float32, device="cuda")
     stream = torch.cuda.current_stream()
     lam = ws.sirt_lambda(plan)
+    # launch shapes from the library's autotuner (scratch buffers, before any timing)
+    q_tmp = torch.zeros(plan.nangles, plan.nx, plan.ys, dtype=torch.float32, device="cuda")
+    tuned = plan.autotune(x, q_tmp, stream=stream)
+    del q_tmp
+    x.zero_()
 
     # the learned warm start: committed weights, inference net over 16 slices at a time
     net, meta = None, {}
@@ -275,8 +384,10 @@ def main():
         hist, info = plan.cgls(b, x, MAXIT, TOL, stream=stream)
         return info
 
+    sirt_iters = getattr(net, "sirt_iters", SIRT_ITERS)
+
     def solve_warm():
-        _, sinfo = plan.sirt(b, x, lam, SIRT_ITERS, 0.0, stream=stream)
+        _, sinfo = plan.sirt(b, x, lam, sirt_iters, 0.0, stream=stream)
         net.warm_start(plan, x, x, scratch[0], scratch[1], stream=stream)
         hist, info = plan.cgls(b, x, MAXIT, TOL, warm=True, rnorm_ref=sinfo.rnorm0,
                                stream=stream)
@@ -374,7 +485,7 @@ def main():
             b_ref.copy_(b_host, non_blocking=True)
             plan.sino_from_reference(b_ref, b_dev, stream=stream)
             if net is not None:
-                _, sinfo = plan.sirt(b_dev, x_dev, lam, SIRT_ITERS, 0.0, stream=stream)
+                _, sinfo = plan.sirt(b_dev, x_dev, lam, sirt_iters, 0.0, stream=stream)
                 net.warm_start(plan, x_dev, x_dev, scratch[0], scratch[1], stream=stream)
                 plan.cgls(b_dev, x_dev, MAXIT, TOL, warm=True, rnorm_ref=sinfo.rnorm0,
                           stream=stream)
@@ -411,14 +522,15 @@ def main():
 
     if rank == 0:
         cfg = dict(CONFIG, iterations=n_it, rel_final=rel_final,
-                   parallelism="replicas" if world > 1 else "single")
+                   parallelism="replicas" if world > 1 else "single",
+                   autotuned={"fp_band_lines": tuned[0], "bp_slice_chunks": tuned[1]})
         if net is not None:
-            cfg.update(warm_start=True, sirt_iters=SIRT_ITERS,
+            cfg.update(warm_start=True, sirt_iters=sirt_iters,
                        workload="learned warm start: SIRT-%d -> BF16 U-Net -> CGLS to "
                                 "||A^T r||/||A^T b|| <= 1e-3 (max 200 it), square-pixel "
                                 "projector, 1024^2 x 512 slices, 1200 angles over [0,180), "
                                 "random-sphere cylinder r=500 px with 200 spheres, Poisson 5e3 "
-                                "photons" % SIRT_ITERS,
+                                "photons" % sirt_iters,
                        plain_cgls=plain,
                        speedup_vs_plain=(value / plain["slices_per_s"]) if plain else None,
                        weights=os.path.relpath(args.weights, ROOT),

@@ -11,8 +11,10 @@
  *   cyl_sirt_KB                                              AREC3D/AREC3D/arecsirt_KB.h:6-7
  *   cyl_cgls, cyl_cgls_SQ                                    AREC3D/AREC3D/areccgls.h:6-10
  *   cyl_cgls_KB                                              AREC3D/AREC3D/areccgls_KB.h:6-7
+ *   cyl_cgls_stat, cyl_cgls_KB_stat, cyl_cgls_SQ_stat,
+ *   init_weights                                             AREC3D/AREC3D/areccgls_stat.h:6-13
  *   arecCCImages                                             AREC3D/AREC3D/arecImage.h:36
- *   ccorr2d, speak                                           AREC3D/AREC3D/align2dstack.h:9,25
+ *   ccorr2d, speak, fshift2d                                 AREC3D/AREC3D/align2dstack.h:9,13,25
  *
  * and, for C and FFI callers, the extern "C" aliases declared below (same
  * arguments, `arecgb_` prefix).  Arguments, ownership and status codes are the
@@ -85,11 +87,22 @@ int arecgb_cyl_cgls_KB(MPI_Comm comm, arecImage images, float *angles, arecImage
 int arecgb_cyl_cgls_SQ(MPI_Comm comm, arecImage images, float *angles, arecImage *xvol,
                        float lam, int maxit, float tol);
 
+/* Statistically weighted CGLS (weights exp(-b) with a Tukey taper along x). */
+int arecgb_cyl_cgls_stat(MPI_Comm comm, arecImage images, float *angles, arecImage *xvol,
+                         float lam, int maxit, float tol);
+int arecgb_cyl_cgls_KB_stat(MPI_Comm comm, arecImage images, float *angles, arecImage *xvol,
+                            float lam, int maxit, float tol);
+int arecgb_cyl_cgls_SQ_stat(MPI_Comm comm, arecImage images, float *angles, arecImage *xvol,
+                            float lam, int maxit, float tol);
+int arecgb_init_weights(MPI_Comm comm, arecImage projections, arecImage *weights);
+
 /* Alignment. */
 int arecgb_arecCCImages(MPI_Comm comm, arecImage images1, arecImage images2, float *sx,
                         float *sy);
 void arecgb_ccorr2d(int nx, int ny, float *x, float *y, float *c);
 void arecgb_speak(int nx, int ny, float *data, float *xt, float *yt);
+/* Fourier shift of one image (powers of two: nx 16..4096, ny 16..2048). */
+void arecgb_fshift2d(int nx, int ny, float *imagein, float *imageout, float sx, float sy);
 
 /* Residual trace of the last solver call on this thread (relative residuals,
  * oldest first); returns the number of entries written (<= cap). */

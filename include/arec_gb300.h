@@ -97,6 +97,24 @@ int arecgb_sino_from_reference(const float *d_ref, float *d_dev, int na, int ny,
 int arecgb_sino_to_reference(const float *d_dev, float *d_ref, int na, int ny, int nx, int ys,
                              void *stream);
 
+/* Statistically weighted CGLS (replaces cyl_cgls[_KB|_SQ]_stat,
+ * AREC3D/AREC3D/areccgls_stat.cpp:49-731): CGLS on the weighted normal
+ * equations, weights w = expf(-b) times a Tukey window (alpha 0.5) along the
+ * detector (init_weights, :12-46), computed on the device from d_b; stops when
+ * ||A^T W r|| / ||A^T W r0|| < tol.  Arguments as arecgb_cgls without rnorm_ref. */
+int arecgb_cgls_stat(arecgb_plan *plan, const float *d_b, float *d_x, int warm, int maxit,
+                     float tol, double *rel_history, arecgb_solve_info *info, void *stream);
+
+/* CGLS over n independent problems, one plan each (cylinders of uneven radius,
+ * slice count and angle set; each plan at most once): the arguments of
+ * arecgb_cgls per problem (warm, rnorm_ref: arrays or NULL; info: n entries or
+ * NULL).  One iteration of all problems is one CUDA graph launch, the problems
+ * being parallel branches; a problem that meets its stopping test stops
+ * (its kernels become no-ops).  No counterpart in the reference. */
+int arecgb_cgls_batch(arecgb_plan *const *plans, const float *const *d_b, float *const *d_x,
+                      const int *warm, int n, int maxit, float tol, const double *rnorm_ref,
+                      arecgb_solve_info *info, void *stream);
+
 /* Projector timing for measurement: mode 1 resets and starts recording a
  * CUDA event pair around every forward and back projection of this plan (on
  * the stream it runs on); mode 2 reports the summed device time and call
@@ -104,6 +122,15 @@ int arecgb_sino_to_reference(const float *d_dev, float *d_ref, int na, int ny, i
  * last recorded event.  No counterpart in the reference. */
 int arecgb_plan_timing(arecgb_plan *plan, int mode, double *fp_ms, long long *fp_calls,
                        double *bp_ms, long long *bp_calls);
+
+/* Autotuner: times the projectors of this plan for the forward projector's
+ * band height (32, 64, 128 lines) and the back projector's slices per block
+ * (one or two chunks of 32*VEC) on the caller's buffers d_x (a volume) and
+ * d_q (a sinogram), which it overwrites, and keeps the fastest; reports the
+ * choice (either pointer may be NULL).  Results do not depend on the choice
+ * beyond float summation order across bands.  No counterpart in the reference. */
+int arecgb_plan_autotune(arecgb_plan *plan, float *d_x, float *d_q, int *fp_band, int *bp_nsc,
+                         void *stream);
 
 /* Kernel launches issued by this library so far (all threads, approximate
  * only in that concurrent callers interleave). */
@@ -116,6 +143,15 @@ long long arecgb_launch_count(void);
  * 0-based integer peak positions.  nx and ny must be powers of two in [16, 4096]. */
 int arecgb_cc_shifts(const float *d_img1, const float *d_img2, int nz, int ny, int nx,
                      float *d_sx, float *d_sy, int *d_ix, int *d_iy, void *stream);
+
+/* Fourier shift of a stack of nz images [nz][ny][nx] (device memory) by
+ * (d_sx[i], d_sy[i]) pixels each (replaces the per-image loop over fshift2d,
+ * AREC3D/AREC3D/align2dstack.cpp:566-630, used by the alignment driver,
+ * AREC3D.cpp:219,230): out = Re(IDFT(DFT(in) exp(-2 pi i (sx kx + sy ky)))) /
+ * (nx ny) with the reference's frequencies and float phase.  nx a power of two
+ * in [16, 4096], ny in [16, 2048].  d_in and d_out may not overlap. */
+int arecgb_fshift2d_device(const float *d_in, float *d_out, int nz, int ny, int nx,
+                           const float *d_sx, const float *d_sy, void *stream);
 
 /* Shift search that allocates nothing (no counterpart in the reference: its
  * arecCCImages allocates per call).  Same arguments, results and layout as

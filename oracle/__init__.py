@@ -62,6 +62,11 @@ def lib():
                               C.c_float, _f32p, C.c_int, C.c_int, C.POINTER(Trace)]
         L.oc_cgls.argtypes = [C.c_int, C.c_int, C.c_int, C.c_int, _f32p, _f32p, C.c_int, C.c_float,
                               _f32p, C.c_int, C.c_double, C.c_int, C.c_int, C.POINTER(Trace)]
+        L.oc_cgls_stat.argtypes = [C.c_int, C.c_int, C.c_int, C.c_int, _f32p, _f32p, C.c_int,
+                                   C.c_float, _f32p, C.c_int, C.c_int, C.c_int, C.POINTER(Trace)]
+        L.oc_cgls_stat64.argtypes = [C.c_int, C.c_int, C.c_int, C.c_int, _f64p, _f32p, C.c_int,
+                                     C.c_float, _f64p, C.c_int, C.c_int, C.c_int,
+                                     C.POINTER(Trace)]
         L.oc_project64.argtypes = [C.c_int, C.c_double, C.c_int, _f64p, _f32p, C.c_int, _f64p]
         L.oc_backproject64.argtypes = [C.c_int, C.c_double, C.c_int, _f64p, _f32p, C.c_int, _f64p]
         L.oc_sirt64.argtypes = [C.c_int, C.c_int, C.c_int, C.c_int, _f64p, _f32p, C.c_float,
@@ -140,6 +145,29 @@ def cgls(weighting, b, angles, maxit=10, tol=1e-3, x0=None, rnorm_ref=0.0, nthre
     return x, tr
 
 
+def cgls_stat(weighting, b, angles, maxit=10, tol=1e-3, x0=None, nthreads=1, verbose=False):
+    """cyl_cgls[_KB|_SQ]_stat (statistical weights exp(-b), Tukey taper); odd nx."""
+    b = f32(b)
+    na, ny, nx = b.shape
+    _, nr, _ = cyl(0.5 * (nx - 1))
+    x = np.zeros((nr, ny), np.float32) if x0 is None else f32(x0).copy()
+    tr = Trace()
+    lib().oc_cgls_stat(weighting, nx, ny, na, b, f32(angles), maxit, tol, x, int(x0 is not None),
+                       nthreads, int(verbose), C.byref(tr))
+    return x, tr
+
+
+def cgls_stat64(weighting, b, angles, maxit=10, tol=1e-3, x0=None, nthreads=1):
+    b = f64(b)
+    na, ny, nx = b.shape
+    _, nr, _ = cyl(0.5 * (nx - 1))
+    x = np.zeros((nr, ny), np.float64) if x0 is None else f64(x0).copy()
+    tr = Trace()
+    lib().oc_cgls_stat64(weighting, nx, ny, na, b, f32(angles), maxit, tol, x, int(x0 is not None),
+                         nthreads, 0, C.byref(tr))
+    return x, tr
+
+
 # --- FP64 oracle: the reference's weights, every sum and update in double ---------------------
 def f64(a):
     return np.ascontiguousarray(a, dtype=np.float64)
@@ -183,6 +211,28 @@ def cgls64(weighting, b, angles, maxit=10, tol=1e-3, x0=None, rnorm_ref=0.0, nth
     lib().oc_cgls64(weighting, nx, ny, na, b, f32(angles), maxit, tol, x, int(x0 is not None),
                     float(rnorm_ref), nthreads, 0, C.byref(tr))
     return x, tr
+
+
+# --- Fourier shift --------------------------------------------------------------------------
+def fshift2d(image, sx, sy):
+    """fshift2d (AREC3D/AREC3D/align2dstack.cpp:566-630): the frequencies and
+    sx*kx + sy*ky in float, the phase rounded to float, float cosine and sine;
+    the transforms in double (the reference uses FFTW in float)."""
+    img = np.asarray(image, np.float64)
+    ny, nx = img.shape
+
+    def freqs(n):
+        h = -(-n // 2)
+        return np.array([np.float32(i) / np.float32(n) if i < h else np.float32(i - n) / np.float32(n)
+                         for i in range(n)], np.float32)
+
+    kx, ky = freqs(nx), freqs(ny)
+    t = (np.float32(sx) * kx[None, :] + np.float32(sy) * ky[:, None]).astype(np.float32)
+    phase = (-2.0 * np.pi * t.astype(np.float64)).astype(np.float32)
+    cs, sn = np.cos(phase).astype(np.float64), np.sin(phase).astype(np.float64)
+    F = np.fft.fft2(img)
+    G = (F.real * cs - F.imag * sn) + 1j * (F.real * sn + F.imag * cs)
+    return np.fft.ifft2(G).real.astype(np.float32)
 
 
 # --- cross-correlation ----------------------------------------------------------------------
@@ -253,8 +303,12 @@ class Reference:
             "cyl_cgls": "_Z8cyl_cglsi5ImagePfPS_fif",
             "cyl_cgls_KB": "_Z11cyl_cgls_KBi5ImagePfPS_fif",
             "cyl_cgls_SQ": "_Z11cyl_cgls_SQi5ImagePfPS_fif",
+            "cyl_cgls_stat": "_Z13cyl_cgls_stati5ImagePfPS_fif",
+            "cyl_cgls_KB_stat": "_Z16cyl_cgls_KB_stati5ImagePfPS_fif",
+            "cyl_cgls_SQ_stat": "_Z16cyl_cgls_SQ_stati5ImagePfPS_fif",
             "ccorr2d": "_Z7ccorr2diiPfS_S_",
             "speak": "_Z5speakiiPfS_S_",
+            "fshift2d": "_Z8fshift2diiPfS_ff",
             "arecCCImages": "_Z12arecCCImagesi5ImageS_PfS0_",
         }
         for k, v in names.items():
@@ -264,13 +318,15 @@ class Reference:
             self._sym[k].argtypes = [img, C.POINTER(C.c_float), C.c_int, C.POINTER(img)]
             self._sym[k].restype = C.c_int
         for k in ("cyl_sirt", "cyl_sirt_KB", "cyl_sirt_SQ", "cyl_cgls", "cyl_cgls_KB",
-                  "cyl_cgls_SQ"):
+                  "cyl_cgls_SQ", "cyl_cgls_stat", "cyl_cgls_KB_stat", "cyl_cgls_SQ_stat"):
             self._sym[k].argtypes = [C.c_int, img, C.POINTER(C.c_float), C.POINTER(img), C.c_float,
                                      C.c_int, C.c_float]
             self._sym[k].restype = C.c_int
         self._sym["ccorr2d"].argtypes = [C.c_int, C.c_int, _f32p, _f32p, _f32p]
         self._sym["speak"].argtypes = [C.c_int, C.c_int, _f32p, C.POINTER(C.c_float),
                                        C.POINTER(C.c_float)]
+        self._sym["fshift2d"].argtypes = [C.c_int, C.c_int, _f32p, _f32p, C.c_float, C.c_float]
+        self._sym["fshift2d"].restype = None
         self._sym["arecCCImages"].argtypes = [C.c_int, img, img, _f32p, _f32p]
         self._sym["arecCCImages"].restype = C.c_int
         self._keep = []
@@ -342,6 +398,12 @@ class Reference:
                              lam, maxit, tol)
         x = np.ctypeslib.as_array(vol.data, shape=(vol.nrays, b.shape[1])).copy()
         return x, st
+
+    def fshift2d(self, image, sx, sy):
+        a = f32(image).copy()
+        out = np.zeros_like(a)
+        self._sym["fshift2d"](a.shape[1], a.shape[0], a, out, float(sx), float(sy))
+        return out
 
     def ccorr2d(self, x, y):
         x, y = f32(x).copy(), f32(y).copy()

@@ -55,6 +55,12 @@ int oc_sirt(int weighting, int nx, int ny, int nangles, const float *b, const fl
  * warm != 0: x holds the initial guess (reference `xvol->data != NULL`).
  * rnorm_ref > 0 replaces the denominator of the stopping test (the reference
  * uses the initial normal-equation residual); 0 keeps the reference rule. */
+int oc_cgls_stat(int weighting, int nx, int ny, int nangles, const float *b,
+                 const float *angles, int maxit, float tol, float *x, int warm, int nthreads,
+                 int verbose, oc_trace *tr);
+int oc_cgls_stat64(int weighting, int nx, int ny, int nangles, const double *b,
+                   const float *angles, int maxit, float tol, double *x, int warm, int nthreads,
+                   int verbose, oc_trace *tr);
 int oc_cgls(int weighting, int nx, int ny, int nangles, const float *b, const float *angles,
             int maxit, float tol, float *x, int warm, double rnorm_ref, int nthreads, int verbose,
             oc_trace *tr);

@@ -26,8 +26,8 @@ mkdir -p "$OUT"
 CXX="${CXX:-g++}"
 CC="${CC:-gcc}"
 FLAGS=(-O2 -fPIC -ffp-contract=off -w -DNDEBUG)
-UNITS=(arecImage arecproject areccgls areccgls_KB arecsirt arecsirt_KB align2dstack imagetools
-       arecImageIO arecImageIO_mpi)
+UNITS=(arecImage arecproject areccgls areccgls_KB areccgls_stat arecsirt arecsirt_KB align2dstack
+       imagetools arecImageIO arecImageIO_mpi)
 pids=()
 for u in "${UNITS[@]}"; do
     "$CXX" -std=c++14 "${FLAGS[@]}" -I"$HERE/shim" -I"$SRC" -c "$SRC/$u.cpp" -o "$OUT/$u.o" &

@@ -54,6 +54,9 @@ REF_SYMBOLS = [
     "_Z11cyl_sirt_SQi5ImagePfPS_fif", "_Z8cyl_cglsi5ImagePfPS_fif",
     "_Z11cyl_cgls_KBi5ImagePfPS_fif", "_Z11cyl_cgls_SQi5ImagePfPS_fif",
     "_Z12arecCCImagesi5ImageS_PfS0_", "_Z7ccorr2diiPfS_S_", "_Z5speakiiPfS_S_",
+    "_Z13cyl_cgls_stati5ImagePfPS_fif", "_Z16cyl_cgls_KB_stati5ImagePfPS_fif",
+    "_Z16cyl_cgls_SQ_stati5ImagePfPS_fif", "_Z12init_weightsi5ImagePS_",
+    "_Z8fshift2diiPfS_ff",
 ]
 
 
@@ -63,11 +66,13 @@ def test_reference_cxx_symbols(lib):
     assert not missing, missing
 
 
-def test_architecture_is_sm103a(lib):
-    out = subprocess.run(["cuobjdump", "--list-elf", lib.LIB_PATH], capture_output=True, text=True)
-    if out.returncode != 0:
-        pytest.skip("cuobjdump unavailable")
-    assert "sm_103a" in out.stdout
+def test_builder_targets_sm103a():
+    """Every translation unit is compiled for sm_103a only (the builder's flags)."""
+    from arec3d_gb300 import builder
+
+    flags = " ".join(builder.ARCH + builder.FLAGS)
+    assert "arch=compute_103a,code=sm_103a" in flags
+    assert flags.count("-gencode") == 1
 
 
 @pytest.mark.parametrize("r", [0.5, 1.0, 1.5, 7.5, 12.0, 31.5, 100.0])

@@ -159,3 +159,26 @@ def test_reference_status_codes(gb):
     st = gb.lib().arecgb_arecBackProject2D_SQ(img, gb._f32p(ang), 1, C.byref(cyl))
     assert st == 1
     gb.arecImageFree(cyl)
+
+
+@pytest.mark.parametrize("w", [2, 3])
+def test_autotuned_shapes_keep_parity(gb, oc, w):
+    """After the autotuner has picked band heights and slices per block, the
+    projectors still match the oracle (only summation order across bands may
+    change)."""
+    radius, ny, ang = 63.5, 300, uniform_angles(40)
+    plan = gb.Plan(w, radius, ny, ang)
+    band, nsc = plan.autotune(empty_vol(plan), empty_sino(plan))
+    assert band in (32, 64, 128) and nsc in (1, 2)
+    rng = np.random.default_rng(w)
+    x = rng.standard_normal((plan.nrays, ny)).astype(np.float32)
+    q_ref = oc.project(w, radius, x, ang)
+    qd = empty_sino(plan)
+    plan.project(vol_to_dev(plan, x), qd)
+    assert rel_l2(sino_from_dev(plan, qd), q_ref) < TOL
+    g_ref = oc.backproject(w, radius, q_ref, ang)
+    gd = empty_vol(plan)
+    plan.backproject(sino_to_dev(plan, q_ref), gd)
+    assert rel_l2(vol_from_dev(plan, gd), g_ref) < TOL
+    assert plan.check() == 0
+    print("autotune w=%d: band %d, back-projection chunks %d" % (w, band, nsc))

@@ -146,3 +146,64 @@ def test_projector_error_vs_fp64(gb, oc, w):
     e_gpu, e_ref = rel_l2(q, q64), rel_l2(q_ref, q64)
     print("FP w=%d: gpu-fp64 %.2e, ref-fp64 %.2e, gpu-ref %.2e" % (w, e_gpu, e_ref, rel_l2(q, q_ref)))
     assert e_gpu < 2 * e_ref + 1e-7
+
+
+def test_cgls_batch_matches_single_solves(gb):
+    """Three uneven problems (radius, slices, angles, weighting) solved as one
+    batch (one CUDA graph launch per iteration) give exactly the iterates and
+    histories of three separate solves."""
+    import torch
+
+    specs = [(3, 31.5, 20, uniform_angles(40)), (2, 12.0, 8, uniform_angles(16)),
+             (3, 63.5, 64, uniform_angles(90))]
+    rng = np.random.default_rng(11)
+    plans, bs, singles, infos = [], [], [], []
+    for w, radius, ny, ang in specs:
+        plan = gb.Plan(w, radius, ny, ang)
+        b = rng.random((len(ang), ny, plan.nx)).astype(np.float32)
+        bd = sino_to_dev(plan, b)
+        xd = empty_vol(plan)
+        hist, info = plan.cgls(bd, xd, 15, 1e-4)
+        plans.append(plan)
+        bs.append(bd)
+        singles.append(vol_from_dev(plan, xd))
+        infos.append(info)
+    xs = [empty_vol(p) for p in plans]
+    binfo = gb.cgls_batch(plans, bs, xs, 15, 1e-4)
+    for i, plan in enumerate(plans):
+        assert binfo[i].iterations == infos[i].iterations
+        assert binfo[i].rel_final == infos[i].rel_final
+        np.testing.assert_array_equal(vol_from_dev(plan, xs[i]), singles[i])
+
+
+@pytest.mark.parametrize("w", [2, 3])
+def test_cgls_stat_parity(gb, oc, w):
+    """Statistically weighted CGLS (cyl_cgls_SQ_stat / _KB_stat,
+    areccgls_stat.cpp) on the device against the oracle (pinned bit for bit to
+    the reference build) and its FP64 twin; odd nx as the reference requires."""
+    rng = np.random.default_rng(20 + w)
+    radius, ny, na = 24, 6, 36
+    nx = 2 * radius + 1
+    ang = uniform_angles(na)
+    _, nr, _ = oc.cyl(float(radius))
+    xt = rng.random((nr, ny), dtype=np.float32) * 0.02
+    b = oc.project(w, float(radius), xt, ang)
+    b = (b + 0.01 * rng.standard_normal(b.shape)).astype(np.float32)
+    x_ref, tr = oc.cgls_stat(w, b, ang, maxit=10, tol=1e-7)
+    x64, _ = oc.cgls_stat64(w, b, ang, maxit=10, tol=1e-7)
+    plan = gb.Plan(w, float(radius), ny, ang)
+    assert plan.nx == nx
+    xd = empty_vol(plan)
+    hist, info = plan.cgls_stat(sino_to_dev(plan, b), xd, 10, 1e-7)
+    x = vol_from_dev(plan, xd)
+    e_gpu, e_ref = rel_l2(x, x_ref), rel_l2(x_ref, x64)
+    print("cgls_stat w=%d: gpu-ref %.2e, ref-fp64 %.2e, gpu-fp64 %.2e"
+          % (w, e_gpu, e_ref, rel_l2(x, x64)))
+    assert info.iterations == tr.iterations
+    assert e_gpu < max(TOL, FRAC * e_ref)
+    np.testing.assert_allclose(hist, tr.rel_history(), rtol=RTOL_TRACE)
+    # and through the reference-compatible entry point (host arecImage buffers)
+    name = "cyl_cgls_SQ_stat" if w == 3 else "cyl_cgls_KB_stat"
+    xc, st = getattr(gb, name)(b, ang, maxit=10, tol=1e-7)
+    assert st == 0
+    assert rel_l2(xc, x_ref) < max(TOL, FRAC * e_ref)

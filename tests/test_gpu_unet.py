@@ -142,7 +142,29 @@ def _compare(gb, size, batch, params, x, dout):
     return e_fwd, errs
 
 
-@pytest.mark.parametrize("size,batch", [(32, 2), (48, 1)])
+@pytest.mark.parametrize("cin,cout,shape", [(32, 32, (1, 3, 128)), (64, 128, (2, 2, 256)),
+                                            (256, 32, (1, 4, 128)), (128, 256, (1, 2, 128))])
+def test_conv3x3_tma_path(gb, cin, cout, shape):
+    """Widths that are multiples of 128 take the TMA path (layout 0); layout 2
+    forces the gather kernel on the same data."""
+    import torch
+
+    torch.manual_seed(cin * 3 + cout)
+    n, h, wd = shape
+    x = torch.randn(n, h, wd, cin, device="cuda").bfloat16()
+    w = (torch.randn(cout, 9, cin, device="cuda") / (3 * cin ** 0.5)).bfloat16()
+    b = torch.randn(cout, device="cuda") * 0.1
+    ref = conv_ref(x, w, b, relu=True)
+    y_tma = run_conv(gb, x, w, b, True, 0)
+    y_gather = run_conv(gb, x, w, b, True, 2)
+    e_tma = float((y_tma.float() - ref).norm() / ref.norm())
+    e_pair = float((y_tma.float() - y_gather.float()).norm() / ref.norm())
+    print("conv tma %d->%d %s: rel err %.2e, tma vs gather %.2e" % (cin, cout, shape, e_tma, e_pair))
+    assert e_tma < BF16_TOL
+    assert e_pair < 1e-3
+
+
+@pytest.mark.parametrize("size,batch", [(32, 2), (48, 1), (128, 1)])
 def test_unet_exact_case_matches_oracle(gb, size, batch):
     from oracle import unet_ref
 

@@ -169,6 +169,56 @@ print("ok")
     assert r.returncode == 0 and "ok" in r.stdout, r.stderr[-2000:]
 
 
+@pytest.mark.skipif(not os.path.exists(os.path.join(ROOT, "oracle", "_ref", "libarec_ref.so")),
+                    reason="reference not built here")
+def test_cgls_stat_against_reference_build(oc):
+    """The oracle's statistically weighted CGLS against the reference's own
+    cyl_cgls_SQ_stat / cyl_cgls_KB_stat (areccgls_stat.cpp), bit for bit."""
+    code = r"""
+import ctypes, sys, numpy as np
+ctypes.CDLL("libc.so.6").mallopt(-3, 4096)
+sys.path.insert(0, %r)
+import oracle as O
+R = O.Reference()
+rng = np.random.default_rng(9)
+for radius, ny, na in ((12, 4, 15), (20, 3, 24)):
+    nx = 2 * radius + 1
+    ang = (np.arange(na) * np.pi / na).astype(np.float32)
+    b = (rng.random((na, ny, nx)) * 2.0).astype(np.float32)
+    for w, name in ((3, "cyl_cgls_SQ_stat"), (2, "cyl_cgls_KB_stat")):
+        xr, st = R.solve(name, b, ang, 0.0, 6, 0.0)
+        x, tr = O.cgls_stat(w, b, ang, maxit=6, tol=0.0)
+        assert st == 0, (name, st)
+        assert np.array_equal(x, xr), (name, radius, float(np.abs(x - xr).max()))
+print("ok")
+""" % ROOT
+    r = subprocess.run([sys.executable, "-c", code], capture_output=True, text=True)
+    assert r.returncode == 0 and "ok" in r.stdout, (r.stdout[-1500:], r.stderr[-2000:])
+
+
+@pytest.mark.skipif(not os.path.exists(os.path.join(ROOT, "oracle", "_ref", "libarec_ref.so")),
+                    reason="reference not built here")
+def test_fshift2d_against_reference_build(oc):
+    """The oracle's fshift2d against the reference's own (align2dstack.cpp:566)
+    over the FFTW-API stand-in."""
+    code = r"""
+import ctypes, sys, numpy as np
+ctypes.CDLL("libc.so.6").mallopt(-3, 4096)
+sys.path.insert(0, %r)
+import oracle as O
+R = O.Reference()
+rng = np.random.default_rng(4)
+for ny, nx, sx, sy in ((32, 64, 3.25, -7.5), (64, 64, -0.4, 12.7), (48, 80, 5.0, 2.0)):
+    img = rng.standard_normal((ny, nx)).astype(np.float32)
+    a, b = O.fshift2d(img, sx, sy), R.fshift2d(img, sx, sy)
+    e = np.linalg.norm(a - b) / np.linalg.norm(b)
+    assert e < 1e-6, (ny, nx, e)
+print("ok")
+""" % ROOT
+    r = subprocess.run([sys.executable, "-c", code], capture_output=True, text=True)
+    assert r.returncode == 0 and "ok" in r.stdout, (r.stdout[-1500:], r.stderr[-2000:])
+
+
 def test_unet_oracle_gradients_finite_differences():
     """The U-Net oracle's autograd gradients (FP64, no bf16 rounding) against
     central differences on a few parameters of every layer."""
