@@ -77,6 +77,12 @@ def lib():
         L.arecgb_fshift2d_device.argtypes = [vp, vp, C.c_int, C.c_int, C.c_int, vp, vp, vp]
         L.arecgb_fshift2d.argtypes = [C.c_int, C.c_int, fp, fp, C.c_float, C.c_float]
         L.arecgb_fshift2d.restype = None
+        L.arecgb_rot_cc_images.argtypes = [vp, vp, C.c_int, C.c_int, C.c_int, C.c_int, vp, vp]
+        L.arecgb_rotate_images.argtypes = [vp, C.c_int, C.c_int, C.c_int, vp, vp]
+        L.arecgb_rotate_images_skew.argtypes = [vp, C.c_int, C.c_int, C.c_int, vp, vp]
+        L.arecgb_rotate_images_skew_safe.argtypes = [vp, vp, C.c_int, C.c_int, C.c_int, vp,
+                                                     C.POINTER(C.c_int), C.POINTER(C.c_double), vp]
+        L.arecgb_ncc_filtered.argtypes = [vp, vp, C.c_int, C.c_int, C.c_int, vp, vp]
         L.arecgb_cc_shifts_static.argtypes = [vp, vp, C.c_int, C.c_int, C.c_int, vp, vp, vp, vp,
                                               vp]
         img, pimg = ArecImage, C.POINTER(ArecImage)
@@ -91,6 +97,12 @@ def lib():
             f.argtypes = [C.c_int, img, fp, pimg, C.c_float, C.c_int, C.c_float]
             f.restype = C.c_int
         L.arecgb_arecCCImages.argtypes = [C.c_int, img, img, fp, fp]
+        L.arecgb_arecRotCCImages.argtypes = [C.c_int, img, img, C.c_int, fp]
+        for n in ("arecgb_arecRotateImages", "arecgb_arecRotateImages_skew"):
+            getattr(L, n).argtypes = [pimg, fp]
+            getattr(L, n).restype = None
+        L.arecgb_arecRotateImages_skew_safe.argtypes = [pimg, pimg, fp]
+        L.arecgb_arecRotateImages_skew_safe.restype = None
         L.arecgb_ccorr2d.argtypes = [C.c_int, C.c_int, fp, fp, fp]
         L.arecgb_ccorr2d.restype = None
         L.arecgb_speak.argtypes = [C.c_int, C.c_int, fp, fp, fp]
@@ -386,6 +398,48 @@ def fshift2d(image, sx, sy):
     return out
 
 
+def rot_cc_images(images1, images2, r2, angles, stream=None):
+    """Rotation (degrees) of each device image of images2 against images1
+    (arecRotCCImages) into the device vector angles."""
+    nz, ny, nx = images1.shape
+    _check(lib().arecgb_rot_cc_images(_ptr(images1), _ptr(images2), nz, ny, nx, int(r2),
+                                      _ptr(angles), _stream(stream)), "arecgb_rot_cc_images")
+
+
+def rotate_images(images, angles, stream=None):
+    """Bilinear rotation of a device stack in place (arecRotateImages)."""
+    nz, ny, nx = images.shape
+    _check(lib().arecgb_rotate_images(_ptr(images), nz, ny, nx, _ptr(angles), _stream(stream)),
+           "arecgb_rotate_images")
+
+
+def rotate_images_skew(images, angles, stream=None):
+    """Shear rotation of a device stack in place; angles updated
+    (arecRotateImages_skew)."""
+    nz, ny, nx = images.shape
+    _check(lib().arecgb_rotate_images_skew(_ptr(images), nz, ny, nx, _ptr(angles),
+                                           _stream(stream)), "arecgb_rotate_images_skew")
+
+
+def rotate_images_skew_safe(images, ref, angles, stream=None):
+    """Guarded shear rotation of a device stack against ref, in place; returns
+    (slices rotated, mean kept correlation) (arecRotateImages_skew_safe)."""
+    nz, ny, nx = images.shape
+    n_rot, mean_cc = C.c_int(), C.c_double()
+    _check(lib().arecgb_rotate_images_skew_safe(_ptr(images), _ptr(ref), nz, ny, nx, _ptr(angles),
+                                                C.byref(n_rot), C.byref(mean_cc),
+                                                _stream(stream)), "arecgb_rotate_images_skew_safe")
+    return n_rot.value, mean_cc.value
+
+
+def ncc_filtered(a, b, cc, stream=None):
+    """Tukey-filtered normalised cross-correlation per device image pair into
+    the float64 device vector cc."""
+    nz, ny, nx = a.shape
+    _check(lib().arecgb_ncc_filtered(_ptr(a), _ptr(b), nz, ny, nx, _ptr(cc), _stream(stream)),
+           "arecgb_ncc_filtered")
+
+
 def ccorr2d_device(x, y, c, stream=None):
     ny, nx = x.shape
     _check(lib().arecgb_ccorr2d_device(_ptr(x), _ptr(y), _ptr(c), ny, nx, _stream(stream)),
@@ -556,6 +610,34 @@ def arecCCImages(images1, images2):
     sy = np.zeros(a.shape[0], np.float32)
     st = lib().arecgb_arecCCImages(0, _cb_image(a), _cb_image(b), _f32p(sx), _f32p(sy))
     return sx, sy, st
+
+
+def arecRotCCImages(images1, images2, r2):
+    """(angles, status): rotation of each images2[i] against images1[i] (degrees)."""
+    a = np.ascontiguousarray(images1, dtype=np.float32)
+    b = np.ascontiguousarray(images2, dtype=np.float32)
+    ang = np.zeros(a.shape[0], np.float32)
+    st = lib().arecgb_arecRotCCImages(0, _cb_image(a), _cb_image(b), int(r2), _f32p(ang))
+    return ang, st
+
+
+def arecRotateImages(images, angles, kind=""):
+    """(rotated copy, angles) of a host stack; kind "" (bilinear) or "_skew"."""
+    a = np.ascontiguousarray(images, dtype=np.float32).copy()
+    ang = np.ascontiguousarray(angles, dtype=np.float32).copy()
+    im = _cb_image(a)
+    getattr(lib(), "arecgb_arecRotateImages" + kind)(C.byref(im), _f32p(ang))
+    return a, ang
+
+
+def arecRotateImages_skew_safe(images, ref, angles):
+    """(rotated copy, angles) of a host stack against ref."""
+    a = np.ascontiguousarray(images, dtype=np.float32).copy()
+    r = np.ascontiguousarray(ref, dtype=np.float32)
+    ang = np.ascontiguousarray(angles, dtype=np.float32).copy()
+    im, rf = _cb_image(a), _cb_image(r)
+    lib().arecgb_arecRotateImages_skew_safe(C.byref(im), C.byref(rf), _f32p(ang))
+    return a, ang
 
 
 def ccorr2d(x, y):

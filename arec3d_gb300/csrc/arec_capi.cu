@@ -35,6 +35,12 @@ int fshift_stack(const float *d_in, float *d_out, int nz, int ny, int nx, const 
                  const float *d_sy, cudaStream_t st);
 int peak_search(const float *dc, int nz, int ny, int nx, float *sx, float *sy, int *ix, int *iy,
                 cudaStream_t st);
+int rot_cc_angles(const float *d1, const float *d2, int nz, int ny, int nx, int r2, float *d_angles,
+                  cudaStream_t st);
+int rotate_stack(float *d_img, const float *d_ref, int nz, int ny, int nx, float *d_angles,
+                 int kind, int *n_rot, double *mean_cc, cudaStream_t st);
+int ncc_filtered(const float *d_a, const float *d_a2, const float *d_b, int nz, int ny, int nx,
+                 double *d_cc, int npairs, cudaStream_t st);
 }  // namespace arecgb
 
 using namespace arecgb;
@@ -205,6 +211,35 @@ int arecgb_ccorr2d_device(const float *d_x, const float *d_y, float *d_c, int ny
 int arecgb_fshift2d_device(const float *d_in, float *d_out, int nz, int ny, int nx,
                            const float *d_sx, const float *d_sy, void *stream) {
     return fshift_stack(d_in, d_out, nz, ny, nx, d_sx, d_sy, (cudaStream_t)stream);
+}
+
+int arecgb_rot_cc_images(const float *d_img1, const float *d_img2, int nz, int ny, int nx, int r2,
+                         float *d_angles, void *stream) {
+    return rot_cc_angles(d_img1, d_img2, nz, ny, nx, r2, d_angles, (cudaStream_t)stream);
+}
+
+int arecgb_rotate_images(float *d_img, int nz, int ny, int nx, const float *d_angles,
+                         void *stream) {
+    // kind 0 only reads the angles
+    return rotate_stack(d_img, nullptr, nz, ny, nx, const_cast<float *>(d_angles), 0, nullptr,
+                        nullptr, (cudaStream_t)stream);
+}
+
+int arecgb_rotate_images_skew(float *d_img, int nz, int ny, int nx, float *d_angles,
+                              void *stream) {
+    return rotate_stack(d_img, nullptr, nz, ny, nx, d_angles, 1, nullptr, nullptr,
+                        (cudaStream_t)stream);
+}
+
+int arecgb_rotate_images_skew_safe(float *d_img, const float *d_ref, int nz, int ny, int nx,
+                                   float *d_angles, int *n_rot, double *mean_cc, void *stream) {
+    return rotate_stack(d_img, d_ref, nz, ny, nx, d_angles, 2, n_rot, mean_cc,
+                        (cudaStream_t)stream);
+}
+
+int arecgb_ncc_filtered(const float *d_a, const float *d_b, int nz, int ny, int nx, double *d_cc,
+                        void *stream) {
+    return ncc_filtered(d_a, nullptr, d_b, nz, ny, nx, d_cc, 1, (cudaStream_t)stream);
 }
 
 }  // extern "C"
@@ -756,6 +791,94 @@ int arecgb_arecCCImages(MPI_Comm, arecImage i1, arecImage i2, float *sx, float *
     return rc;
 }
 
+// Rotational alignment over host stacks: copy in, run on the device, copy out.
+// kind -1: arecRotCCImages (angles out); 0, 1, 2: arecRotateImages, _skew,
+// _skew_safe (images and angles in place).
+static int rot_host(const char *who, int kind, const arecImage &a, const arecImage *b, int r2,
+                    float *angles, int *n_rot, double *mean_cc) {
+    const int nx = a.nx, ny = a.ny, nz = a.nz;
+    if (nz <= 0) return 0;
+    std::lock_guard<std::mutex> lk(g_mu);
+    const size_t n = (size_t)nx * ny * nz;
+    const bool two = b != nullptr;
+    float *d1 = nullptr, *d2 = nullptr, *da = nullptr;
+    cudaStream_t st = nullptr;
+    int rc = 0;
+    cudaError_t e = cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaMalloc(&d1, sizeof(float) * n);
+    if (e == cudaSuccess && two) e = cudaMalloc(&d2, sizeof(float) * n);
+    if (e == cudaSuccess) e = cudaMalloc(&da, sizeof(float) * nz);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(d1, a.data, sizeof(float) * n, cudaMemcpyHostToDevice, st);
+    if (e == cudaSuccess && two)
+        e = cudaMemcpyAsync(d2, b->data, sizeof(float) * n, cudaMemcpyHostToDevice, st);
+    if (e == cudaSuccess && kind >= 0)
+        e = cudaMemcpyAsync(da, angles, sizeof(float) * nz, cudaMemcpyHostToDevice, st);
+    if (e != cudaSuccess) {
+        set_error(std::string(who) + ": " + cudaGetErrorString(e));
+        rc = cuda_status(e);
+    }
+    if (!rc) {
+        if (kind < 0)
+            rc = rot_cc_angles(d1, d2, nz, ny, nx, r2, da, st);
+        else
+            rc = rotate_stack(d1, d2, nz, ny, nx, da, kind, n_rot, mean_cc, st);
+    }
+    if (!rc) {
+        e = cudaMemcpyAsync(angles, da, sizeof(float) * nz, cudaMemcpyDeviceToHost, st);
+        if (e == cudaSuccess && kind >= 0)
+            e = cudaMemcpyAsync(a.data, d1, sizeof(float) * n, cudaMemcpyDeviceToHost, st);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+        if (e != cudaSuccess) {
+            set_error(std::string(who) + ": " + cudaGetErrorString(e));
+            rc = cuda_status(e);
+        }
+    }
+    if (st) cudaStreamSynchronize(st);
+    cudaFree(d1);
+    cudaFree(d2);
+    cudaFree(da);
+    if (st) cudaStreamDestroy(st);
+    return rc;
+}
+
+// arecRotCCImages (AREC3D/AREC3D/arecImage.cpp:555-598): rotation of each image
+// of images2 against the same-index image of images1, degrees.
+int arecgb_arecRotCCImages(MPI_Comm, arecImage i1, arecImage i2, int r2, float *angles) {
+    if (i1.nx != i2.nx || i1.ny != i2.ny || i1.nz != i2.nz) {
+        if (!quiet()) fprintf(stderr, "arecRotCCImages2: mismatch in dimension:\n");
+        return -1;
+    }
+    return rot_host("arecRotCCImages", -1, i1, &i2, r2, angles, nullptr, nullptr);
+}
+
+// arecRotateImages (AREC3D/AREC3D/arecImage.cpp:674-690): bilinear rotation.
+void arecgb_arecRotateImages(arecImage *images, float *angles) {
+    if (rot_host("arecRotateImages", 0, *images, nullptr, 0, angles, nullptr, nullptr) &&
+        !quiet())
+        fprintf(stderr, "arecRotateImages: %s\n", last_error());
+}
+
+// arecRotateImages_skew (AREC3D/AREC3D/arecImage.cpp:692-738).
+void arecgb_arecRotateImages_skew(arecImage *images, float *angles) {
+    if (rot_host("arecRotateImages_skew", 1, *images, nullptr, 0, angles, nullptr, nullptr) &&
+        !quiet())
+        fprintf(stderr, "arecRotateImages_skew: %s\n", last_error());
+}
+
+// arecRotateImages_skew_safe (AREC3D/AREC3D/arecImage.cpp:740-790).
+void arecgb_arecRotateImages_skew_safe(arecImage *images, arecImage *images_ref, float *angles) {
+    int n_rot = 0;
+    double mean_cc = 0.0;
+    const int rc = rot_host("arecRotateImages_skew_safe", 2, *images, images_ref, 0, angles,
+                            &n_rot, &mean_cc);
+    if (quiet()) return;
+    if (rc)
+        fprintf(stderr, "arecRotateImages_skew_safe: %s\n", last_error());
+    else
+        printf("arecRotateImages_skew_safe: Mean CC=%4.4f n_rot=%d/%d\n", mean_cc, n_rot,
+               images->nz);
+}
+
 // ccorr2d (AREC3D/AREC3D/align2dstack.cpp:480-521).
 void arecgb_ccorr2d(int nx, int ny, float *x, float *y, float *c) {
     std::lock_guard<std::mutex> lk(g_mu);
@@ -838,3 +961,7 @@ int arecCCImages(MPI_Comm m, arecImage a, arecImage b, float *sx, float *sy) { r
 void ccorr2d(int nx, int ny, float *x, float *y, float *c) { arecgb_ccorr2d(nx, ny, x, y, c); }
 void speak(int nx, int ny, float *d, float *xt, float *yt) { arecgb_speak(nx, ny, d, xt, yt); }
 void fshift2d(int nx, int ny, float *in, float *out, float sx, float sy) { arecgb_fshift2d(nx, ny, in, out, sx, sy); }
+int arecRotCCImages(MPI_Comm m, arecImage a, arecImage b, int r2, float *ang) { return arecgb_arecRotCCImages(m, a, b, r2, ang); }
+void arecRotateImages(arecImage *i, float *ang) { arecgb_arecRotateImages(i, ang); }
+void arecRotateImages_skew(arecImage *i, float *ang) { arecgb_arecRotateImages_skew(i, ang); }
+void arecRotateImages_skew_safe(arecImage *i, arecImage *r, float *ang) { arecgb_arecRotateImages_skew_safe(i, r, ang); }

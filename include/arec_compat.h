@@ -14,6 +14,9 @@
  *   cyl_cgls_stat, cyl_cgls_KB_stat, cyl_cgls_SQ_stat,
  *   init_weights                                             AREC3D/AREC3D/areccgls_stat.h:6-13
  *   arecCCImages                                             AREC3D/AREC3D/arecImage.h:36
+ *   arecRotCCImages                                          AREC3D/AREC3D/arecImage.h:37
+ *   arecRotateImages, arecRotateImages_skew,
+ *   arecRotateImages_skew_safe                               AREC3D/AREC3D/arecImage.h:46-48
  *   ccorr2d, speak, fshift2d                                 AREC3D/AREC3D/align2dstack.h:9,13,25
  *
  * and, for C and FFI callers, the extern "C" aliases declared below (same
@@ -103,6 +106,12 @@ void arecgb_ccorr2d(int nx, int ny, float *x, float *y, float *c);
 void arecgb_speak(int nx, int ny, float *data, float *xt, float *yt);
 /* Fourier shift of one image (powers of two: nx 16..4096, ny 16..2048). */
 void arecgb_fshift2d(int nx, int ny, float *imagein, float *imageout, float sx, float sy);
+/* Rotation search and rotations (2 <= r2 <= min(2048, nx/2, ny/2)). */
+int arecgb_arecRotCCImages(MPI_Comm comm, arecImage images1, arecImage images2, int r2,
+                           float *angles);
+void arecgb_arecRotateImages(arecImage *images, float *angles);
+void arecgb_arecRotateImages_skew(arecImage *images, float *angles);
+void arecgb_arecRotateImages_skew_safe(arecImage *images, arecImage *images_ref, float *angles);
 
 /* Residual trace of the last solver call on this thread (relative residuals,
  * oldest first); returns the number of entries written (<= cap). */

@@ -153,6 +153,47 @@ int arecgb_cc_shifts(const float *d_img1, const float *d_img2, int nz, int ny, i
 int arecgb_fshift2d_device(const float *d_in, float *d_out, int nz, int ny, int nx,
                            const float *d_sx, const float *d_sy, void *stream);
 
+/* Rotation search over nz image pairs, device memory [nz][ny][nx] (replaces
+ * arecRotCCImages, AREC3D/AREC3D/arecImage.cpp:555-598): per pair, radial
+ * profiles over n = (int)(2 pi r2) directions (sum over radii 0..r2-1 of the
+ * bilinear sample times the radius, getRadialProfile :534-553), their circular
+ * cross-correlation (ccorr1d, align2dstack.cpp:437-476), the 7-point
+ * polynomial fit around the first maximum (findPeak1d / PRB1D), converted to
+ * degrees in (-180, 180]; |angle| > 45 gives 0.  d_angles: nz floats (device).
+ * 2 <= r2 <= min(2048, nx/2, ny/2).  Synchronises `stream` before returning. */
+int arecgb_rot_cc_images(const float *d_img1, const float *d_img2, int nz, int ny, int nx, int r2,
+                         float *d_angles, void *stream);
+
+/* Bilinear rotation of each image by d_angles[i] degrees about (nx/2, ny/2),
+ * zero outside (replaces arecRotateImages, AREC3D/AREC3D/arecImage.cpp:674-690,
+ * with rotate2d, align2dstack.cpp:774-816).  In place. */
+int arecgb_rotate_images(float *d_img, int nz, int ny, int nx, const float *d_angles,
+                         void *stream);
+
+/* Rotation by three circular shears (replaces arecRotateImages_skew,
+ * AREC3D/AREC3D/arecImage.cpp:692-738): an angle below -180 / above 180 moves
+ * by one turn; |angle| > 45 is set to 0 and leaves the image; 10 < |angle| <= 45
+ * rotates bilinearly; otherwise shear x by -tan(-a/2), y by sin(-a), x again
+ * (shearX_circ / shearY_circ, imagetools.cpp:244-291: integer circular shift
+ * plus a linear sub-pixel tap).  Images and d_angles are updated in place. */
+int arecgb_rotate_images_skew(float *d_img, int nz, int ny, int nx, float *d_angles,
+                              void *stream);
+
+/* Guarded shear rotation (replaces arecRotateImages_skew_safe,
+ * AREC3D/AREC3D/arecImage.cpp:740-790): a slice keeps its rotation only when
+ * its Tukey-filtered normalised cross-correlation with d_ref[i] rises by more
+ * than 1e-5, and its angle is then halved; otherwise the slice is restored and
+ * its angle set to 0.  n_rot and mean_cc (host, optional) receive the number of
+ * slices rotated and the mean of the kept correlations.  Synchronises. */
+int arecgb_rotate_images_skew_safe(float *d_img, const float *d_ref, int nz, int ny, int nx,
+                                   float *d_angles, int *n_rot, double *mean_cc, void *stream);
+
+/* Tukey-window (alpha 0.3) normalised cross-correlation of each image pair,
+ * FP64 sums (replaces getNormalizedCrossCorrelationWithFilter,
+ * AREC3D/AREC3D/imagetools.cpp:415-446).  d_cc: nz doubles (device). */
+int arecgb_ncc_filtered(const float *d_a, const float *d_b, int nz, int ny, int nx, double *d_cc,
+                        void *stream);
+
 /* Shift search that allocates nothing (no counterpart in the reference: its
  * arecCCImages allocates per call).  Same arguments, results and layout as
  * arecgb_cc_shifts, for callers that cannot allocate device memory while they

@@ -310,6 +310,16 @@ class Reference:
             "speak": "_Z5speakiiPfS_S_",
             "fshift2d": "_Z8fshift2diiPfS_ff",
             "arecCCImages": "_Z12arecCCImagesi5ImageS_PfS0_",
+            "arecRotCCImages": "_Z15arecRotCCImagesi5ImageS_iPf",
+            "arecRotateImages": "_Z16arecRotateImagesP5ImagePf",
+            "arecRotateImages_skew": "_Z21arecRotateImages_skewP5ImagePf",
+            "arecRotateImages_skew_safe": "_Z26arecRotateImages_skew_safeP5ImageS0_Pf",
+            "getRadialProfile": "_Z16getRadialProfile5ImageiPfii",
+            "findPeak1d": "_Z10findPeak1diPf",
+            "shearX_circ": "_Z11shearX_circPffii",
+            "shearY_circ": "_Z11shearY_circPffii",
+            "rotate2d": "_Z8rotate2diiPfS_f",
+            "ncc_filtered": "_Z39getNormalizedCrossCorrelationWithFilterPfS_ii",
         }
         for k, v in names.items():
             self._sym[k] = getattr(L, v)
@@ -329,6 +339,24 @@ class Reference:
         self._sym["fshift2d"].restype = None
         self._sym["arecCCImages"].argtypes = [C.c_int, img, img, _f32p, _f32p]
         self._sym["arecCCImages"].restype = C.c_int
+        self._sym["arecRotCCImages"].argtypes = [C.c_int, img, img, C.c_int, _f32p]
+        self._sym["arecRotCCImages"].restype = C.c_int
+        for k in ("arecRotateImages", "arecRotateImages_skew"):
+            self._sym[k].argtypes = [C.POINTER(img), _f32p]
+            self._sym[k].restype = None
+        self._sym["arecRotateImages_skew_safe"].argtypes = [C.POINTER(img), C.POINTER(img), _f32p]
+        self._sym["arecRotateImages_skew_safe"].restype = None
+        self._sym["getRadialProfile"].argtypes = [img, C.c_int, _f32p, C.c_int, C.c_int]
+        self._sym["getRadialProfile"].restype = None
+        self._sym["findPeak1d"].argtypes = [C.c_int, _f32p]
+        self._sym["findPeak1d"].restype = C.c_float
+        for k in ("shearX_circ", "shearY_circ"):
+            self._sym[k].argtypes = [_f32p, C.c_float, C.c_int, C.c_int]
+            self._sym[k].restype = None
+        self._sym["rotate2d"].argtypes = [C.c_int, C.c_int, _f32p, _f32p, C.c_float]
+        self._sym["rotate2d"].restype = None
+        self._sym["ncc_filtered"].argtypes = [_f32p, _f32p, C.c_int, C.c_int]
+        self._sym["ncc_filtered"].restype = C.c_double
         self._keep = []
 
     # helpers building arecImage views over numpy buffers
@@ -404,6 +432,56 @@ class Reference:
         out = np.zeros_like(a)
         self._sym["fshift2d"](a.shape[1], a.shape[0], a, out, float(sx), float(sy))
         return out
+
+    # rotational alignment (AREC3D/AREC3D/arecImage.cpp:534-790, imagetools.cpp)
+    def rot_cc_images(self, stack1, stack2, r2):
+        a, b = self._cb(f32(stack1).copy()), self._cb(f32(stack2).copy())
+        ang = np.zeros(len(stack1), np.float32)
+        st = self._sym["arecRotCCImages"](0, a, b, r2, ang)
+        return ang, st
+
+    def rotate_images(self, stack, angles, kind=""):
+        """kind "", "_skew": the stack rotated in place (a copy) and the angles."""
+        arr = f32(stack).copy()
+        ang = f32(angles).copy()
+        im = self._cb(arr)
+        self._sym["arecRotateImages" + kind](C.byref(im), ang)
+        return arr, ang
+
+    def rotate_images_skew_safe(self, stack, ref, angles):
+        arr = f32(stack).copy()
+        ang = f32(angles).copy()
+        im, rf = self._cb(arr), self._cb(f32(ref).copy())
+        self._sym["arecRotateImages_skew_safe"](C.byref(im), C.byref(rf), ang)
+        return arr, ang
+
+    def radial_profile(self, img, n, R):
+        arr = f32(img)[None].copy()
+        out = np.zeros(n, np.float32)
+        self._sym["getRadialProfile"](self._cb(arr), 0, out, n, R)
+        return out
+
+    def find_peak_1d(self, c):
+        c = f32(c).copy()
+        return self._sym["findPeak1d"](len(c), c)
+
+    def shear(self, img, shear, axis):
+        a = f32(img).copy()
+        ny, nx = a.shape
+        self._sym["shearX_circ" if axis == "x" else "shearY_circ"](a, float(shear), nx, ny)
+        return a
+
+    def rotate2d(self, img, theta):
+        a = f32(img).copy()
+        ny, nx = a.shape
+        out = np.zeros_like(a)
+        self._sym["rotate2d"](nx, ny, a, out, float(theta))
+        return out
+
+    def ncc_filtered(self, a, b):
+        a, b = f32(a).copy(), f32(b).copy()
+        ny, nx = a.shape
+        return self._sym["ncc_filtered"](a, b, nx, ny)
 
     def ccorr2d(self, x, y):
         x, y = f32(x).copy(), f32(y).copy()

@@ -3,7 +3,9 @@ itself (AREC3D, compiled from its own sources into oracle/_ref by
 oracle/build_ref.sh) on small seeded inputs.  Run in the container that has the
 reference checkout:
 
-    bash oracle/build_ref.sh && python tests/golden/make_golden.py
+    bash oracle/build_ref.sh && python tests/golden/make_golden.py [--rotation]
+
+(--rotation writes only reference_rotation.npz.)
 
 The reference's linear weighting (pmethod=1) reads two entries past its
 coordinate table; to make those reads return zero (as they do for large tables
@@ -98,5 +100,52 @@ def main():
     print("wrote", os.path.join(HERE, "reference_small.npz"))
 
 
+def blobs(ny, nx, angle_deg, rng):
+    """Seeded test image: two Gaussian blobs and a bar, rotated by angle_deg about
+    the centre, plus 1 % noise."""
+    yy, xx = np.mgrid[0:ny, 0:nx].astype(np.float64)
+    t = np.deg2rad(angle_deg)
+    x, y = xx - nx / 2, yy - ny / 2
+    xr, yr = x * np.cos(t) + y * np.sin(t), -x * np.sin(t) + y * np.cos(t)
+    s = nx / 64.0
+    img = (np.exp(-((xr - 6 * s) ** 2 / (30 * s * s) + (yr - 3 * s) ** 2 / (8 * s * s))) +
+           0.6 * np.exp(-((xr + 8 * s) ** 2 / (10 * s * s) + (yr + 5 * s) ** 2 / (20 * s * s))) +
+           0.3 * ((np.abs(xr) < 12 * s) & (np.abs(yr - 9 * s) < 2 * s)))
+    return (img + 0.01 * rng.standard_normal(img.shape)).astype(np.float32)
+
+
+def rotation():
+    """Rotation search and rotations (arecRotCCImages, arecRotateImages,
+    _skew, _skew_safe) on a 4-slice 48 x 64 stack."""
+    import oracle as O
+
+    R = O.Reference()
+    rng = np.random.default_rng(20261204)
+    ny, nx = 48, 64
+    truth = [7.5, -4.0, 30.0, 0.0]
+    ref = np.stack([blobs(ny, nx, 0.0, rng) for _ in truth])
+    rot = np.stack([blobs(ny, nx, a, rng) for a in truth])
+    out = {"rot_ref": ref, "rot_img": rot}
+    ang, st = R.rot_cc_images(ref, rot, 20)
+    assert st == 0
+    out["rotcc_r2"] = np.array(20)
+    out["rotcc_angles"] = ang
+    skew_in = np.array([3.0, 25.0, -60.0, 370.0], np.float32)
+    out["skew_angles_in"] = skew_in
+    out["skew_img"], out["skew_angles"] = R.rotate_images(rot, skew_in, "_skew")
+    out["bilinear_img"], _ = R.rotate_images(rot, skew_in, "")
+    safe_in = np.array(ang, np.float32).copy()
+    safe_in[3] = 5.0  # a slice the rotation makes worse
+    out["safe_angles_in"] = safe_in
+    out["safe_img"], out["safe_angles"] = R.rotate_images_skew_safe(rot, ref, safe_in)
+    out["ncc"] = np.array([R.ncc_filtered(a, b) for a, b in zip(ref, rot)])
+    np.savez_compressed(os.path.join(HERE, "reference_rotation.npz"), **out)
+    print("wrote", os.path.join(HERE, "reference_rotation.npz"))
+
+
 if __name__ == "__main__":
-    main()
+    if "--rotation" in sys.argv:
+        rotation()
+    else:
+        main()
+        rotation()

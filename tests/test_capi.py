@@ -56,7 +56,8 @@ REF_SYMBOLS = [
     "_Z12arecCCImagesi5ImageS_PfS0_", "_Z7ccorr2diiPfS_S_", "_Z5speakiiPfS_S_",
     "_Z13cyl_cgls_stati5ImagePfPS_fif", "_Z16cyl_cgls_KB_stati5ImagePfPS_fif",
     "_Z16cyl_cgls_SQ_stati5ImagePfPS_fif", "_Z12init_weightsi5ImagePS_",
-    "_Z8fshift2diiPfS_ff",
+    "_Z8fshift2diiPfS_ff", "_Z15arecRotCCImagesi5ImageS_iPf", "_Z16arecRotateImagesP5ImagePf",
+    "_Z21arecRotateImages_skewP5ImagePf", "_Z26arecRotateImages_skew_safeP5ImageS0_Pf",
 ]
 
 

@@ -250,3 +250,65 @@ def test_unet_oracle_gradients_finite_differences():
             q2[off] -= h
             fd = (f(q1) - f(q2)) / (2 * h)
             assert abs(fd - g[off]) <= 1e-5 * max(1.0, abs(fd)), (l["name"], off, fd, g[off])
+
+
+# ---- rotational alignment (arecRotCCImages, arecRotateImages*) --------------------------------
+ROT_GOLD = os.path.join(ROOT, "tests", "golden", "reference_rotation.npz")
+
+
+def test_golden_rotation_oracle():
+    """The oracle's rotation search and rotations against the reference's own
+    outputs on the golden stack: rotations bit for bit (the shears, the bilinear
+    rotation, the guarded shear rotation and their angle updates), the
+    rotation search within the FFT rounding of its float cross-correlation."""
+    from oracle import rotation as R
+
+    g = np.load(ROT_GOLD)
+    ref, img = g["rot_ref"], g["rot_img"]
+    ang = R.rot_cc_angles(ref, img, int(g["rotcc_r2"]))
+    # the reference's ccorr1d output is float (FFTW-API stand-in); 1e-3 deg is
+    # 0.0022 of a profile sample at r2 = 20 (125 samples per turn)
+    assert np.abs(ang - g["rotcc_angles"]).max() < 1e-3, (ang, g["rotcc_angles"])
+    out, a = R.rotate_images_skew(img, g["skew_angles_in"])
+    assert np.array_equal(out, g["skew_img"]) and np.array_equal(a, g["skew_angles"])
+    assert np.array_equal(R.rotate_images(img, g["skew_angles_in"]), g["bilinear_img"])
+    out, a, n_rot, mean_cc = R.rotate_images_skew_safe(img, ref, g["safe_angles_in"])
+    assert np.array_equal(out, g["safe_img"]) and np.array_equal(a, g["safe_angles"])
+    assert n_rot == 3
+    cc = [R.ncc_filtered(x, y) for x, y in zip(ref, img)]
+    assert np.allclose(cc, g["ncc"], rtol=1e-12, atol=0)
+
+
+@pytest.mark.skipif(not os.path.exists(os.path.join(ROOT, "oracle", "_ref", "libarec_ref.so")),
+                    reason="reference not built here")
+def test_rotation_pieces_against_reference_build():
+    """Each piece of the oracle's rotation path against the reference's own
+    function: shearX_circ / shearY_circ, rotate2d, getRadialProfile (bit for
+    bit), findPeak1d on the same correlation, the filtered NCC."""
+    code = r"""
+import sys, numpy as np
+sys.path.insert(0, %r)
+import oracle as O
+from oracle import rotation as R
+Ref = O.Reference()
+rng = np.random.default_rng(11)
+for ny, nx in ((48, 64), (33, 50)):
+    img = rng.standard_normal((ny, nx)).astype(np.float32)
+    # shifts stay shorter than the row / column: a longer one makes the
+    # reference's circShiftX / circShiftY read outside their buffers
+    for sh in (0.0, 0.031, -0.113, 0.41, -0.9):
+        assert np.array_equal(Ref.shear(img, sh, "x"), R.shear_x(img, np.float32(sh))), sh
+        assert np.array_equal(Ref.shear(img, sh, "y"), R.shear_y(img, np.float32(sh))), sh
+    for th in (0.0, 3.3, -12.5, 44.0, -179.0, 200.0):
+        assert np.array_equal(Ref.rotate2d(img, th), R.rotate2d(img, np.float32(th))), th
+    for r2 in (2, 7, min(nx, ny) // 2):
+        n = int(r2 * 2 * R.PI)
+        assert np.array_equal(Ref.radial_profile(img, n, r2), R.radial_profile(img, n, r2)), r2
+    img2 = rng.standard_normal((ny, nx)).astype(np.float32)
+    assert abs(Ref.ncc_filtered(img, img2) - R.ncc_filtered(img, img2)) < 1e-13
+    c = rng.standard_normal(97).astype(np.float32)
+    assert Ref.find_peak_1d(c) == R.find_peak_1d(c)
+print("ok")
+""" % ROOT
+    r = subprocess.run([sys.executable, "-c", code], capture_output=True, text=True)
+    assert r.returncode == 0 and "ok" in r.stdout, (r.stdout[-1500:], r.stderr[-2000:])
