@@ -83,6 +83,11 @@ def lib():
         L.arecgb_rotate_images_skew_safe.argtypes = [vp, vp, C.c_int, C.c_int, C.c_int, vp,
                                                      C.POINTER(C.c_int), C.POINTER(C.c_double), vp]
         L.arecgb_ncc_filtered.argtypes = [vp, vp, C.c_int, C.c_int, C.c_int, vp, vp]
+        ip_ = C.POINTER(C.c_int)
+        L.arecgb_mrc_read_header.argtypes = [C.c_char_p, ip_, ip_, ip_, ip_]
+        L.arecgb_mrc_read_device.argtypes = [C.c_char_p, C.c_int, C.c_int, C.c_int, vp,
+                                             C.c_size_t, ip_, ip_, ip_, vp]
+        L.arecgb_mrc_write_device.argtypes = [C.c_char_p, vp, C.c_int, C.c_int, C.c_int, vp]
         L.arecgb_cc_shifts_static.argtypes = [vp, vp, C.c_int, C.c_int, C.c_int, vp, vp, vp, vp,
                                               vp]
         img, pimg = ArecImage, C.POINTER(ArecImage)
@@ -98,6 +103,15 @@ def lib():
             f.restype = C.c_int
         L.arecgb_arecCCImages.argtypes = [C.c_int, img, img, fp, fp]
         L.arecgb_arecRotCCImages.argtypes = [C.c_int, img, img, C.c_int, fp]
+        L.arecgb_arecReadImageHeader.argtypes = [C.c_char_p, ip, ip, ip]
+        L.arecgb_arecReadImage.argtypes = [C.c_char_p, pimg]
+        L.arecgb_arecWriteImage.argtypes = [C.c_char_p, img]
+        for n in ("arecgb_arecReadImageDistbyZ", "arecgb_arecReadImageDistbyY"):
+            getattr(L, n).argtypes = [C.c_int, C.c_char_p, pimg]
+            getattr(L, n).restype = None
+        for n in ("arecgb_arecWriteImageMergeY", "arecgb_arecWriteImageMergeZ"):
+            getattr(L, n).argtypes = [C.c_int, C.c_char_p, img]
+            getattr(L, n).restype = None
         for n in ("arecgb_arecRotateImages", "arecgb_arecRotateImages_skew"):
             getattr(L, n).argtypes = [pimg, fp]
             getattr(L, n).restype = None
@@ -440,6 +454,38 @@ def ncc_filtered(a, b, cc, stream=None):
            "arecgb_ncc_filtered")
 
 
+def mrc_read_header(fname):
+    """(nx, ny, nz, mode) of an MRC file."""
+    v = [C.c_int() for _ in range(4)]
+    _check(lib().arecgb_mrc_read_header(os.fsencode(fname), *[C.byref(x) for x in v]),
+           "arecgb_mrc_read_header")
+    return tuple(x.value for x in v)
+
+
+def mrc_read_device(fname, rank=0, nranks=1, by_y=False, stream=None):
+    """This rank's part of an MRC stack as a float32 CUDA tensor [nz][ny][nx]
+    (by_y: the reference's distribution by rows, else by images)."""
+    import torch
+
+    nx, nyl, nzl = C.c_int(), C.c_int(), C.c_int()
+    L = lib()
+    _check(L.arecgb_mrc_read_device(os.fsencode(fname), rank, nranks, int(by_y), None, 0,
+                                    C.byref(nx), C.byref(nyl), C.byref(nzl), None),
+           "arecgb_mrc_read_device")
+    out = torch.empty(nzl.value, nyl.value, nx.value, dtype=torch.float32, device="cuda")
+    _check(L.arecgb_mrc_read_device(os.fsencode(fname), rank, nranks, int(by_y), _ptr(out),
+                                    out.numel(), C.byref(nx), C.byref(nyl), C.byref(nzl),
+                                    _stream(stream)), "arecgb_mrc_read_device")
+    return out
+
+
+def mrc_write_device(fname, images, stream=None):
+    """Write a float32 CUDA tensor [nz][ny][nx] as a mode-2 MRC file."""
+    nz, ny, nx = images.shape
+    _check(lib().arecgb_mrc_write_device(os.fsencode(fname), _ptr(images), nz, ny, nx,
+                                         _stream(stream)), "arecgb_mrc_write_device")
+
+
 def ccorr2d_device(x, y, c, stream=None):
     ny, nx = x.shape
     _check(lib().arecgb_ccorr2d_device(_ptr(x), _ptr(y), _ptr(c), ny, nx, _stream(stream)),
@@ -638,6 +684,43 @@ def arecRotateImages_skew_safe(images, ref, angles):
     im, rf = _cb_image(a), _cb_image(r)
     lib().arecgb_arecRotateImages_skew_safe(C.byref(im), C.byref(rf), _f32p(ang))
     return a, ang
+
+
+def _take_image(im):
+    """Copy an arecImage the library allocated into numpy and free it."""
+    if not im.data:
+        return None
+    a = np.ctypeslib.as_array(im.data, shape=(im.nz, im.ny, im.nx)).copy()
+    arecImageFree(im)
+    return a
+
+
+def arecReadImage(fname, dist=""):
+    """(stack [nz][ny][nx], status) through arecReadImage, or through
+    arecReadImageDistbyZ / DistbyY with dist "Z" / "Y"."""
+    im = ArecImage()
+    if dist:
+        getattr(lib(), "arecgb_arecReadImageDistby" + dist)(0, os.fsencode(fname), C.byref(im))
+        st = 0 if im.data else -1
+    else:
+        st = lib().arecgb_arecReadImage(os.fsencode(fname), C.byref(im))
+    return _take_image(im), st
+
+
+def arecReadImageHeader(fname):
+    nx, ny, nz = C.c_int(), C.c_int(), C.c_int()
+    st = lib().arecgb_arecReadImageHeader(os.fsencode(fname), C.byref(nx), C.byref(ny),
+                                          C.byref(nz))
+    return (nx.value, ny.value, nz.value), st
+
+
+def arecWriteImage(fname, stack, merge=""):
+    """arecWriteImage, or arecWriteImageMergeY / MergeZ with merge "Y" / "Z"."""
+    a = np.ascontiguousarray(stack, dtype=np.float32)
+    if merge:
+        getattr(lib(), "arecgb_arecWriteImageMerge" + merge)(0, os.fsencode(fname), _cb_image(a))
+        return 0
+    return lib().arecgb_arecWriteImage(os.fsencode(fname), _cb_image(a))
 
 
 def ccorr2d(x, y):

@@ -17,6 +17,9 @@
  *   arecRotCCImages                                          AREC3D/AREC3D/arecImage.h:37
  *   arecRotateImages, arecRotateImages_skew,
  *   arecRotateImages_skew_safe                               AREC3D/AREC3D/arecImage.h:46-48
+ *   arecReadImageHeader, arecReadImage, arecWriteImage       AREC3D/AREC3D/arecImageIO.h:65-67
+ *   arecReadImageDistbyZ, arecReadImageDistbyY,
+ *   arecWriteImageMergeY, arecWriteImageMergeZ               AREC3D/AREC3D/arecImageIO_mpi.h:3-6
  *   ccorr2d, speak, fshift2d                                 AREC3D/AREC3D/align2dstack.h:9,13,25
  *
  * and, for C and FFI callers, the extern "C" aliases declared below (same
@@ -112,6 +115,16 @@ int arecgb_arecRotCCImages(MPI_Comm comm, arecImage images1, arecImage images2, 
 void arecgb_arecRotateImages(arecImage *images, float *angles);
 void arecgb_arecRotateImages_skew(arecImage *images, float *angles);
 void arecgb_arecRotateImages_skew_safe(arecImage *images, arecImage *images_ref, float *angles);
+
+/* MRC files (one rank: the distributed forms read and write the whole stack;
+ * failures print and leave image->data NULL where the reference aborts). */
+int arecgb_arecReadImageHeader(char *fname, int *nx, int *ny, int *nz);
+int arecgb_arecReadImage(char *fname, arecImage *image);
+int arecgb_arecWriteImage(char *fname, arecImage image);
+void arecgb_arecReadImageDistbyZ(MPI_Comm comm, const char *fname, arecImage *image);
+void arecgb_arecReadImageDistbyY(MPI_Comm comm, const char *fname, arecImage *image);
+void arecgb_arecWriteImageMergeY(MPI_Comm comm, const char *fname, arecImage image);
+void arecgb_arecWriteImageMergeZ(MPI_Comm comm, const char *fname, arecImage image);
 
 /* Residual trace of the last solver call on this thread (relative residuals,
  * oldest first); returns the number of entries written (<= cap). */

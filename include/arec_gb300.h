@@ -194,6 +194,29 @@ int arecgb_rotate_images_skew_safe(float *d_img, const float *d_ref, int nz, int
 int arecgb_ncc_filtered(const float *d_a, const float *d_b, int nz, int ny, int nx, double *d_cc,
                         void *stream);
 
+/* ---- MRC image stacks (the reference's file format, arecImageIO.h:12-63) ----
+ * Header of an MRC file: sizes and mode (1, 6: 16-bit, read as signed; 2:
+ * float32).  (Replaces arecReadImageHeader, AREC3D/AREC3D/arecImageIO.cpp:10.) */
+int arecgb_mrc_read_header(const char *fname, int *nx, int *ny, int *nz, int *mode);
+
+/* Read one rank's part of an MRC stack straight into device memory
+ * [nz_loc][ny_loc][nx] as float: by_y = 0 splits the images (replaces
+ * arecReadImageDistbyZ, AREC3D/AREC3D/arecImageIO_mpi.cpp:7-124), by_y = 1 the
+ * rows of every image (arecReadImageDistbyY, :126-260), the first n % nranks
+ * ranks taking one more; rank 0 of 1 reads the whole stack (arecReadImage,
+ * arecImageIO.cpp:31-82).  The file streams through two pinned buffers
+ * (read and copy overlap); 16-bit data converts on the device.  d_out NULL:
+ * only report the sizes.  cap_floats: capacity of d_out.  Synchronises. */
+int arecgb_mrc_read_device(const char *fname, int rank, int nranks, int by_y, float *d_out,
+                           size_t cap_floats, int *nx, int *ny_loc, int *nz_loc, void *stream);
+
+/* Write a device stack [nz][ny][nx] as a mode-2 MRC file with the header of
+ * arecWriteImage (AREC3D/AREC3D/arecImageIO.cpp:84-173; min, max and FP64 mean
+ * computed on the device; the header fields the reference leaves unset are
+ * zero).  Copy-back and file writes overlap.  Synchronises. */
+int arecgb_mrc_write_device(const char *fname, const float *d_in, int nz, int ny, int nx,
+                            void *stream);
+
 /* Shift search that allocates nothing (no counterpart in the reference: its
  * arecCCImages allocates per call).  Same arguments, results and layout as
  * arecgb_cc_shifts, for callers that cannot allocate device memory while they

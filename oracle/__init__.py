@@ -483,6 +483,38 @@ class Reference:
         ny, nx = a.shape
         return self._sym["ncc_filtered"](a, b, nx, ny)
 
+    # MRC files (AREC3D/AREC3D/arecImageIO.cpp, arecImageIO_mpi.cpp; one rank)
+    def write_image(self, fname, stack, merge=""):
+        a = f32(stack).copy()
+        im = self._cb(a)
+        if merge:
+            f = getattr(self.L, "_Z20arecWriteImageMerge%siPKc5Image" % merge)
+            f.argtypes = [C.c_int, C.c_char_p, ArecImage]
+            f.restype = None
+            f(0, os.fsencode(fname), im)
+            return 0
+        f = self.L._Z14arecWriteImagePc5Image
+        f.argtypes = [C.c_char_p, ArecImage]
+        f.restype = C.c_int
+        return f(os.fsencode(fname), im)
+
+    def read_image(self, fname, dist=""):
+        im = ArecImage()
+        if dist:
+            f = getattr(self.L, "_Z20arecReadImageDistby%siPKcP5Image" % dist)
+            f.argtypes = [C.c_int, C.c_char_p, C.POINTER(ArecImage)]
+            f.restype = None
+            f(0, os.fsencode(fname), C.byref(im))
+            st = 0
+        else:
+            f = self.L._Z13arecReadImagePcP5Image
+            f.argtypes = [C.c_char_p, C.POINTER(ArecImage)]
+            f.restype = C.c_int
+            st = f(os.fsencode(fname), C.byref(im))
+        a = np.ctypeslib.as_array(im.data, shape=(im.nz, im.ny, im.nx)).copy()
+        C.CDLL("libc.so.6").free(C.cast(im.data, C.c_void_p))
+        return a, st
+
     def ccorr2d(self, x, y):
         x, y = f32(x).copy(), f32(y).copy()
         ny, nx = x.shape
