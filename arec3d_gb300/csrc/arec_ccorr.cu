@@ -167,20 +167,22 @@ __global__ void __launch_bounds__(256) k_cc_rows_fwd(const float *__restrict__ x
     }
 }
 
-// Pass 2: columns.  CT columns of Xh and Yh per block; W = IDFT_col(conj(X)*Y)
-// overwrites Xh.
+// Pass 2: columns.  ct columns of Xh and Yh per block (ct = col_tile(ny): the
+// two arrays' ct columns stay within 64 KB of shared memory, so several blocks
+// share an SM); W = IDFT_col(conj(X)*Y) overwrites Xh.
 constexpr int kColTile = 4;
+static inline int col_tile(int ny) { return ny <= 1024 ? 4 : (ny <= 2048 ? 2 : 1); }
 __global__ void __launch_bounds__(256) k_cc_cols(float2 *__restrict__ Xh,
                                                  const float2 *__restrict__ Yh, int nx, int ny,
-                                                 const float2 *__restrict__ tw) {
+                                                 const float2 *__restrict__ tw, int ct) {
     extern __shared__ float2 sm[];
     const int H = nx / 2 + 1;
-    const int c0 = blockIdx.x * kColTile, pair = blockIdx.y;
-    const int nc = min(kColTile, H - c0);
+    const int c0 = blockIdx.x * ct, pair = blockIdx.y;
+    const int nc = min(ct, H - c0);
     const size_t half = (size_t)pair * ny * H;
-    float2 *sx = sm, *sy = sm + kColTile * ny;
-    for (int i = threadIdx.x; i < kColTile * ny; i += blockDim.x) {
-        const int row = i / kColTile, c = i % kColTile;
+    float2 *sx = sm, *sy = sm + ct * ny;
+    for (int i = threadIdx.x; i < ct * ny; i += blockDim.x) {
+        const int row = i / ct, c = i % ct;
         float2 a = make_float2(0.f, 0.f), b = a;
         if (c < nc) {
             a = Xh[half + (size_t)row * H + c0 + c];
@@ -191,19 +193,19 @@ __global__ void __launch_bounds__(256) k_cc_cols(float2 *__restrict__ Xh,
     }
     __syncthreads();
     const int G = max(1, 256 / (ny / 16));
-    for (int l0 = 0; l0 < 2 * kColTile; l0 += G)
-        fft_lines(sm + (size_t)l0 * ny, ny, ny, min(G, 2 * kColTile - l0), tw);
+    for (int l0 = 0; l0 < 2 * ct; l0 += G)
+        fft_lines(sm + (size_t)l0 * ny, ny, ny, min(G, 2 * ct - l0), tw);
     // conj(X)*Y, conjugated again for the inverse transform (IDFT = conj DFT conj)
-    for (int i = threadIdx.x; i < kColTile * ny; i += blockDim.x) {
+    for (int i = threadIdx.x; i < ct * ny; i += blockDim.x) {
         const float2 a = sx[i], b = sy[i];
         const float2 cc = make_float2(a.x * b.x + a.y * b.y, a.x * b.y - a.y * b.x);
         sx[i] = make_float2(cc.x, -cc.y);
     }
     __syncthreads();
-    for (int l0 = 0; l0 < kColTile; l0 += G)
-        fft_lines(sm + (size_t)l0 * ny, ny, ny, min(G, kColTile - l0), tw);
-    for (int i = threadIdx.x; i < kColTile * ny; i += blockDim.x) {
-        const int row = i / kColTile, c = i % kColTile;
+    for (int l0 = 0; l0 < ct; l0 += G)
+        fft_lines(sm + (size_t)l0 * ny, ny, ny, min(G, ct - l0), tw);
+    for (int i = threadIdx.x; i < ct * ny; i += blockDim.x) {
+        const int row = i / ct, c = i % ct;
         if (c < nc) {
             const float2 w = sx[c * ny + row];
             Xh[half + (size_t)row * H + c0 + c] = make_float2(w.x, -w.y);
@@ -556,14 +558,15 @@ static int correlate_batch(const float *d1, const float *d2, int np, int ny, int
     if (!rc) rc = twiddles(ny, &twy);
     if (rc) return rc;
     const int G = rows_per_block(nx);
+    const int ct = col_tile(ny);
     const size_t row_smem = sizeof(float2) * (size_t)G * nx;
-    const size_t col_smem = sizeof(float2) * 2 * kColTile * (size_t)ny;
+    const size_t col_smem = sizeof(float2) * 2 * ct * (size_t)ny;
     if ((rc = set_smem((const void *)k_cc_rows_fwd, row_smem))) return rc;
     if ((rc = set_smem((const void *)k_cc_rows_inv, row_smem))) return rc;
     if ((rc = set_smem((const void *)k_cc_cols, col_smem))) return rc;
     const int H = nx / 2 + 1;
     k_cc_rows_fwd<<<dim3((ny + G - 1) / G, np), 256, row_smem, st>>>(d1, d2, Xh, Yh, nx, ny, twx);
-    k_cc_cols<<<dim3((H + kColTile - 1) / kColTile, np), 256, col_smem, st>>>(Xh, Yh, nx, ny, twy);
+    k_cc_cols<<<dim3((H + ct - 1) / ct, np), 256, col_smem, st>>>(Xh, Yh, nx, ny, twy, ct);
     k_cc_rows_inv<<<dim3((ny + G - 1) / G, np), 256, row_smem, st>>>(Xh, c, stats, nx, ny, twx);
     ARECGB_CUDA(cudaGetLastError());
     return 0;
@@ -817,7 +820,8 @@ int cc_shifts_static(const float *d1, const float *d2, int nz, int ny, int nx, f
     if ((rc = set_smem((const void *)k_cc_cols, col_smem))) return rc;
     const int H = nx / 2 + 1;
     k_cc_rows_fwd<<<dim3((ny + G - 1) / G, nz), 256, row_smem, st>>>(d1, d2, Xh, Yh, nx, ny, twx);
-    k_cc_cols<<<dim3((H + kColTile - 1) / kColTile, nz), 256, col_smem, st>>>(Xh, Yh, nx, ny, twy);
+    k_cc_cols<<<dim3((H + kColTile - 1) / kColTile, nz), 256, col_smem, st>>>(Xh, Yh, nx, ny, twy,
+                                                                            kColTile);
     k_cc_rows_inv<<<dim3((ny + G - 1) / G, nz), 256, row_smem, st>>>(Xh, c, stats, nx, ny, twx);
     k_peak<<<nz, 256, 0, st>>>(c, stats, nx, ny, sx, sy, ix, iy);
     cudaError_t e = cudaGetLastError();

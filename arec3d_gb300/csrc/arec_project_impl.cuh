@@ -191,6 +191,19 @@ __device__ __forceinline__ void cp_async_wait() {
     asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory");
 }
 
+// One staged footprint row (a bin's slices) into a lane's registers; a bin off
+// the detector was never copied and reads as zero.
+template <int VEC>
+__device__ __forceinline__ void foot_row(const float *row, int bin, int nx, int lane,
+                                         float (&v)[VEC]) {
+    if ((unsigned)bin < (unsigned)nx) {
+        lds_lane<VEC>(row, lane, v);
+    } else {
+#pragma unroll
+        for (int q = 0; q < VEC; q++) v[q] = 0.f;
+    }
+}
+
 constexpr int kBpAngles = 32;  // angles per weight chunk
 constexpr int kBpFoot = 16;    // staged footprint width in bins (an 8x4 tile spans <= 12)
 
@@ -199,18 +212,21 @@ constexpr int kBpBuf = 3;  // footprint buffers in flight
 template <int VEC, int NSC>
 constexpr size_t bp_smem_bytes() {
     return sizeof(float) * kBpBuf * kBpFoot * (NSC * 32 * VEC) + sizeof(float4) * kBpAngles * 32 +
-           sizeof(int) * kBpAngles + sizeof(double) * (4 * NSC + 1);
+           sizeof(int) * 2 * kBpAngles + sizeof(double) * (4 * NSC + 1);
 }
 
 // Square-pixel and Kaiser-Bessel weightings.  Block = 4*NSC accumulating warps
 // (8 rays x 32*VEC slices each) + 1 staging warp.  Per chunk of 32 angles the
 // weights of the tile's 32 rays are computed once (lanes = rays) into shared
-// memory; then the staging warp copies the footprint of each angle (<= 16 bins,
-// each a contiguous row of the block's slices) with one bulk copy per bin
-// (cp.async.bulk) into one of three buffers, two angles ahead, completing on
-// the buffer's "full" mbarrier, and the accumulating warps release buffers on
-// its "empty" mbarrier: no block-wide barrier per angle.  Bins off the detector
-// are not copied and their taps are skipped, as the reference skips them.
+// memory; then the staging warp copies the footprint of each angle (the bins
+// the tile's taps reach, <= 16, each a contiguous row of the block's slices)
+// with one bulk copy per bin (cp.async.bulk) into one of three buffers, two
+// angles ahead, completing on the buffer's "full" mbarrier, and the
+// accumulating warps release buffers on its "empty" mbarrier: no block-wide
+// barrier per angle.  Each accumulating warp walks its 8 rays through a
+// three-row register ring (one shared-memory row read per ray instead of
+// three).  Bins off the detector are not copied and their taps add nothing, as
+// the reference skips them.
 template <int W, int VEC, int NSC>
 __global__ void __launch_bounds__(128 * NSC + 32)
     bp_kernel(OpArgs A, const float *__restrict__ s, float *__restrict__ g) {
@@ -220,8 +236,9 @@ __global__ void __launch_bounds__(128 * NSC + 32)
     __shared__ __align__(8) uint64_t full[NB], empty[NB];
     float *foot = reinterpret_cast<float *>(smem_raw);               // [NB][FW][SPAN]
     float4 *sw = reinterpret_cast<float4 *>(foot + NB * FW * SPAN);  // [AC][32]
-    int *fb = reinterpret_cast<int *>(sw + AC * 32);                 // [AC]
-    double *red = reinterpret_cast<double *>(fb + AC);               // [NCW + 1]
+    int *fb = reinterpret_cast<int *>(sw + AC * 32);                 // [AC] first bin
+    int *fn = fb + AC;                                               // [AC] bins spanned
+    double *red = reinterpret_cast<double *>(fn + AC);               // [NCW + 1]
     if (A.skip && *A.skip) return;
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const bool stager = warp == NCW;
@@ -275,6 +292,7 @@ __global__ void __launch_bounds__(128 * NSC + 32)
             if (lane == 0) {
                 if (hi - lo + 3 > FW && lo != INT_MAX) atomicOr(A.err, 2);
                 fb[ai] = lo == INT_MAX ? 0 : lo;
+                fn[ai] = lo == INT_MAX ? 0 : min(FW, hi - lo + 3);
             }
         }
         __syncthreads();  // weights and footprint bases of this chunk (barriers initialised)
@@ -287,7 +305,7 @@ __global__ void __launch_bounds__(128 * NSC + 32)
                     if (lane == 0) atomicOr(A.err, 16);
                 }
                 const int bin = fb[ai] + lane;
-                const bool on = ok && lane < FW && (unsigned)bin < (unsigned)A.nx;
+                const bool on = ok && lane < fn[ai] && (unsigned)bin < (unsigned)A.nx;
                 const unsigned m = __ballot_sync(0xffffffffu, on);
                 if (lane == 0) umma::mbar_arrive_expect_tx(&full[buf], (uint32_t)__popc(m) * row_bytes);
                 __syncwarp();
@@ -306,20 +324,50 @@ __global__ void __launch_bounds__(128 * NSC + 32)
                 if (ok && yok) {
                     const float *F = foot + (size_t)buf * FW * SPAN + yw;
                     const int fb0 = fb[ai];
+                    // Three-bin window of footprint rows in registers, kept as a
+                    // ring: slot s holds bin cb + ((s - m) mod 3).  The 8 rays
+                    // are consecutive pixels of one row, so the centre bin moves
+                    // by at most one bin from ray to ray (|cos| <= 1): the ring
+                    // replaces one slot and rotates the weights instead of
+                    // reloading three rows.  Bins off the detector read as zero
+                    // (w * 0 adds nothing).
+                    float R0[VEC], R1[VEC], R2[VEC];
+#pragma unroll
+                    for (int q = 0; q < VEC; q++) R0[q] = R1[q] = R2[q] = 0.f;
+                    int cb = INT_MIN / 4, m = 0;  // bin held in slot m (none yet)
 #pragma unroll
                     for (int r = 0; r < 8; r++) {
                         const float4 e = sw[ai * 32 + rg * 8 + r];
                         const int b = __float_as_int(e.x), rb = b - fb0;
                         if (rb >= 0 && rb <= FW - 3) {
+                            const int d = b - cb;
+                            if (d == 1) {  // bin cb (slot m) leaves, bin b + 2 enters
+                                const float *row = F + (rb + 2) * SPAN;
+                                if (m == 0) foot_row<VEC>(row, b + 2, A.nx, lane, R0);
+                                else if (m == 1) foot_row<VEC>(row, b + 2, A.nx, lane, R1);
+                                else foot_row<VEC>(row, b + 2, A.nx, lane, R2);
+                                m = m == 2 ? 0 : m + 1;
+                            } else if (d == -1) {  // bin cb + 2 leaves, bin b enters
+                                m = m == 0 ? 2 : m - 1;
+                                const float *row = F + rb * SPAN;
+                                if (m == 0) foot_row<VEC>(row, b, A.nx, lane, R0);
+                                else if (m == 1) foot_row<VEC>(row, b, A.nx, lane, R1);
+                                else foot_row<VEC>(row, b, A.nx, lane, R2);
+                            } else if (d != 0) {
+                                foot_row<VEC>(F + rb * SPAN, b, A.nx, lane, R0);
+                                foot_row<VEC>(F + (rb + 1) * SPAN, b + 1, A.nx, lane, R1);
+                                foot_row<VEC>(F + (rb + 2) * SPAN, b + 2, A.nx, lane, R2);
+                                m = 0;
+                            }
+                            cb = b;
+                            const float w0 = m == 0 ? e.y : (m == 1 ? e.w : e.z);
+                            const float w1 = m == 0 ? e.z : (m == 1 ? e.y : e.w);
+                            const float w2 = m == 0 ? e.w : (m == 1 ? e.z : e.y);
 #pragma unroll
-                            for (int j = 0; j < 3; j++) {
-                                if ((unsigned)(b + j) < (unsigned)A.nx) {
-                                    const float w = j == 0 ? e.y : (j == 1 ? e.z : e.w);
-                                    float v[VEC];
-                                    lds_lane<VEC>(F + (rb + j) * SPAN, lane, v);
-#pragma unroll
-                                    for (int q = 0; q < VEC; q++) acc[r][q] = fmaf(w, v[q], acc[r][q]);
-                                }
+                            for (int q = 0; q < VEC; q++) {
+                                acc[r][q] = fmaf(w0, R0[q], acc[r][q]);
+                                acc[r][q] = fmaf(w1, R1[q], acc[r][q]);
+                                acc[r][q] = fmaf(w2, R2[q], acc[r][q]);
                             }
                         }
                     }

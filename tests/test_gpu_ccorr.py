@@ -56,7 +56,7 @@ def test_ccorr2d_image(gb, oc, shape):
     assert rel_l2(gb.ccorr2d(a[0], b[0]), c_ref) < 1e-5
 
 
-@pytest.mark.parametrize("shape", [(64, 64), (128, 256), (512, 512)])
+@pytest.mark.parametrize("shape", [(64, 64), (128, 256), (512, 512), (2048, 128), (4096, 64)])
 def test_shift_search(gb, oc, shape):
     import torch
 
