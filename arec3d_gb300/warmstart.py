@@ -30,9 +30,10 @@ SIRT_ITERS = 10
 CGLS_ITERS = 200
 
 
-def sirt_lambda(plan):
-    """Landweber step below 2 / ||A||^2 (||A||^2 ~ nangles * chord length)."""
-    return 1.0 / (plan.nangles * plan.nx)
+def sirt_lambda(plan, scale=1.0):
+    """Landweber step scale / (nangles * nx), below the stability limit
+    2 / ||A||^2 for scale < 2 (||A||^2 ~ nangles * chord length)."""
+    return scale / (plan.nangles * plan.nx)
 
 
 def pad8(n):
@@ -59,7 +60,7 @@ def make_problem(gb, nx, na, slices, photons, seed, kind="sphere", device="cuda"
 
 
 def make_pairs(gb, nx, na, slices, photons, seed, kind="sphere", sirt_iters=(SIRT_ITERS,),
-               cgls_iters=CGLS_ITERS):
+               cgls_iters=CGLS_ITERS, lam_scale=1.0):
     """{k: (input, target)} image stacks [slices][npad][npad] on the device, one
     pair per SIRT depth k in `sirt_iters` (the CGLS target is shared)."""
     import torch
@@ -71,7 +72,7 @@ def make_pairs(gb, nx, na, slices, photons, seed, kind="sphere", sirt_iters=(SIR
     npad = pad8(plan.nx)
     out = {}
     for k in sirt_iters:
-        plan.sirt(b, xs, sirt_lambda(plan), k, 0.0)
+        plan.sirt(b, xs, sirt_lambda(plan, lam_scale), k, 0.0)
         rms = volume_rms(plan, xs)
         inp = torch.empty(slices, npad, npad, device="cuda")
         tgt = torch.empty_like(inp)
@@ -149,6 +150,7 @@ def load(gb, path, size, max_batch):
     net.set_params(torch.from_numpy(params.copy()).cuda())
     meta = json.loads(str(z["meta"]))
     net.sirt_iters = int(meta.get("sirt_iters", SIRT_ITERS))
+    net.sirt_lam_scale = float(meta.get("sirt_lam_scale", 1.0))
     return net, meta
 
 
@@ -164,7 +166,8 @@ def solve(gb, plan, b, x, net=None, tol=1e-3, maxit=200, sirt_iters=None, scratc
     if net is not None:
         if sirt_iters is None:
             sirt_iters = getattr(net, "sirt_iters", SIRT_ITERS)
-        _, sinfo = plan.sirt(b, x, sirt_lambda(plan), sirt_iters, 0.0)
+        lam = sirt_lambda(plan, getattr(net, "sirt_lam_scale", 1.0))
+        _, sinfo = plan.sirt(b, x, lam, sirt_iters, 0.0)
         rnorm_ref = sinfo.rnorm0  # ||A^T b||, the cold start's denominator
         torch.cuda.synchronize()
         st["sirt"] = time.perf_counter() - t
@@ -190,6 +193,8 @@ def main():
                     help="weights file; with several --sirt-iters, _sirt<k> is appended")
     ap.add_argument("--sirt-iters", default=str(SIRT_ITERS),
                     help="SIRT depth(s) of the network input, comma separated")
+    ap.add_argument("--sirt-lam-scale", type=float, default=1.0,
+                    help="SIRT step as a multiple of 1/(nangles*nx)")
     ap.add_argument("--steps", type=int, default=3000)
     ap.add_argument("--batch", type=int, default=16)
     ap.add_argument("--crop", type=int, default=256)
@@ -208,7 +213,8 @@ def main():
     for spec in args.sets.split(","):
         nx, na, sl, ph, kind, nv = spec.split(":")
         for _ in range(int(nv)):
-            pairs = make_pairs(gb, int(nx), int(na), int(sl), float(ph), seed, kind, ks)
+            pairs = make_pairs(gb, int(nx), int(na), int(sl), float(ph), seed, kind, ks,
+                               lam_scale=args.sirt_lam_scale)
             for k in ks:
                 datasets[k].append(pairs[k])
             seed += 7
@@ -217,7 +223,8 @@ def main():
     for k in ks:
         net, hist = train(gb, datasets[k], steps=args.steps, batch=args.batch, crop=args.crop,
                           lr=args.lr, seed=args.seed)
-        meta = {"sirt_iters": k, "cgls_iters": CGLS_ITERS, "sets": desc, "steps": args.steps,
+        meta = {"sirt_iters": k, "sirt_lam_scale": args.sirt_lam_scale,
+                "cgls_iters": CGLS_ITERS, "sets": desc, "steps": args.steps,
                 "batch": args.batch, "crop": args.crop, "lr": args.lr,
                 "final_loss": float(np.mean(hist[-50:])), "first_loss": float(hist[0])}
         out = args.out if len(ks) == 1 else args.out.replace(".npz", "_sirt%d.npz" % k)

@@ -229,7 +229,7 @@ def extra_config(args):
                "value": ny / (ms / 1e3), "unit": "slices/s", "ms_per_solve": ms,
                "iterations": info.iterations, "restarts": info.restarts}
     elif args.config == 3:
-        n, size = 720, 2048
+        n, size = args.pairs, 2048
         g = torch.Generator(device="cuda")
         g.manual_seed(3)
         ky = torch.fft.fftfreq(size, device="cuda")[:, None]
@@ -256,8 +256,8 @@ def extra_config(args):
         syo = torch.zeros(n, device="cuda")
         ms, _ = timed(lambda: gb.cc_shifts(a, bimg, sxo, syo, stream=st), args.steps)
         err = np.abs(np.array(shifts) - np.stack([sxo.cpu().numpy(), syo.cpu().numpy()], 1))
-        out = {"config": 3, "workload": "shift search, 720 pairs of 2048^2 float images "
-               "(integer shifts +-20 px plus sub-pixel +-0.5 px, 2% noise)",
+        out = {"config": 3, "workload": "shift search, %d pairs of 2048^2 float images "
+               "(integer shifts +-20 px plus sub-pixel +-0.5 px, 2%% noise)" % n,
                "value": n / (ms / 1e3), "unit": "pairs/s", "ms_per_stack": ms,
                "hbm_gbs": n * 2 * 4 * size * size / (ms / 1e3) / 1e9,
                "max_abs_shift_error_px": float(err.max())}
@@ -283,6 +283,35 @@ def extra_config(args):
                "problems": [{"nx": p.nx, "slices": p.ny, "angles": p.nangles,
                              "iterations": inf.iterations} for p, inf in zip(plans, infos)]}
     print(json.dumps(out))
+
+
+def unet_only(args):
+    """U-Net inference on --launches batches of 16 images of 1024^2 (the warm
+    start's network and batch), for profiling."""
+    import torch
+
+    import arec3d_gb300 as gb
+    from arec3d_gb300 import warmstart as ws
+
+    gb.build()
+    net, _ = ws.load(gb, args.weights, NX, 16)
+    g = torch.Generator(device="cuda")
+    g.manual_seed(0)
+    x = torch.rand(16, NX, NX, device="cuda", generator=g)
+    y = torch.empty_like(x)
+    for _ in range(args.launches):
+        net.forward(x, y)
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for _ in range(args.launches):
+        net.forward(x, y)
+    e1.record()
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1) / args.launches
+    flops = 2 * 188928 * 16 * NX * NX  # multiply-adds of the 3x3 layers per pixel x 2
+    print(json.dumps({"unet_only": True, "ms_per_16_images": ms,
+                      "tensor_tflops": flops / (ms / 1e3) / 1e12}))
 
 
 def kernels_only(args):
@@ -331,12 +360,18 @@ def main():
     ap.add_argument("--config", type=int, default=0, choices=[0, 1, 3, 5],
                     help="measure another benchmark configuration instead of the headline")
     ap.add_argument("--batch-problems", type=int, default=8, help="problems for --config 5")
+    ap.add_argument("--pairs", type=int, default=720, help="image pairs for --config 3")
+    ap.add_argument("--unet-only", action="store_true",
+                    help="run only the warm-start network's inference (for profiling)")
     ap.add_argument("--weights", default=os.path.join(ROOT, "arec3d_gb300", "weights",
                                                       "unet_warm_start.npz"))
     args = ap.parse_args()
     rank, local, world = dist_env()
     if args.kernels_only:
         kernels_only(args)
+        return
+    if args.unet_only:
+        unet_only(args)
         return
     if args.config:
         extra_config(args)
@@ -385,6 +420,7 @@ def main():
         return info
 
     sirt_iters = getattr(net, "sirt_iters", SIRT_ITERS)
+    lam = ws.sirt_lambda(plan, getattr(net, "sirt_lam_scale", 1.0))
 
     def solve_warm():
         _, sinfo = plan.sirt(b, x, lam, sirt_iters, 0.0, stream=stream)
