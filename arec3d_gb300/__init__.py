@@ -83,6 +83,9 @@ def lib():
         L.arecgb_rotate_images_skew_safe.argtypes = [vp, vp, C.c_int, C.c_int, C.c_int, vp,
                                                      C.POINTER(C.c_int), C.POINTER(C.c_double), vp]
         L.arecgb_ncc_filtered.argtypes = [vp, vp, C.c_int, C.c_int, C.c_int, vp, vp]
+        L.arecgb_take_log.argtypes = [vp, C.c_size_t, vp]
+        L.arecgb_profile_shifts.argtypes = [vp, C.c_int, C.c_int, C.c_int, C.c_int, dp, dp, vp]
+        L.arecgb_periodic_decomposition.argtypes = [vp, C.c_int, C.c_int, C.c_int, vp, vp]
         ip_ = C.POINTER(C.c_int)
         L.arecgb_mrc_read_header.argtypes = [C.c_char_p, ip_, ip_, ip_, ip_]
         L.arecgb_mrc_read_device.argtypes = [C.c_char_p, C.c_int, C.c_int, C.c_int, vp,
@@ -103,6 +106,11 @@ def lib():
             f.restype = C.c_int
         L.arecgb_arecCCImages.argtypes = [C.c_int, img, img, fp, fp]
         L.arecgb_arecRotCCImages.argtypes = [C.c_int, img, img, C.c_int, fp]
+        for n in ("arecgb_arecImageTakeLog", "arecgb_periodicDecomposition"):
+            getattr(L, n).argtypes = [img]
+            getattr(L, n).restype = None
+        L.arecgb_makePeriodicSlice.argtypes = [C.c_int, C.c_int, fp, fp]
+        L.arecgb_makePeriodicSlice.restype = None
         L.arecgb_arecReadImageHeader.argtypes = [C.c_char_p, ip, ip, ip]
         L.arecgb_arecReadImage.argtypes = [C.c_char_p, pimg]
         L.arecgb_arecWriteImage.argtypes = [C.c_char_p, img]
@@ -454,6 +462,32 @@ def ncc_filtered(a, b, cc, stream=None):
            "arecgb_ncc_filtered")
 
 
+def profile_shifts(profiles, pad, successive=False, stream=None):
+    """(shifts, spread) of Prealign's profile alignment over a CUDA tensor of
+    profiles [prof_y][prof_x]; the caller applies sY -= shifts."""
+    prof_y, prof_x = profiles.shape
+    out = np.zeros(prof_y, np.float64)
+    spread = C.c_double()
+    _check(lib().arecgb_profile_shifts(_ptr(profiles), prof_y, prof_x, int(pad), int(successive),
+                                       out.ctypes.data_as(C.POINTER(C.c_double)),
+                                       C.byref(spread), _stream(stream)), "arecgb_profile_shifts")
+    return out, spread.value
+
+
+def take_log(data, stream=None):
+    """-log(v) for v > 0, else 0, in place on a float32 CUDA tensor."""
+    _check(lib().arecgb_take_log(_ptr(data), data.numel(), _stream(stream)), "arecgb_take_log")
+
+
+def periodic_decomposition(images, smooth=None, stream=None):
+    """Periodic-plus-smooth decomposition of a CUDA stack [nz][ny][nx] in place
+    (or, with `smooth`, its smooth parts written there and the images left)."""
+    nz, ny, nx = images.shape
+    _check(lib().arecgb_periodic_decomposition(_ptr(images), nz, ny, nx,
+                                               _ptr(smooth) if smooth is not None else None,
+                                               _stream(stream)), "arecgb_periodic_decomposition")
+
+
 def mrc_read_header(fname):
     """(nx, ny, nz, mode) of an MRC file."""
     v = [C.c_int() for _ in range(4)]
@@ -705,6 +739,28 @@ def arecReadImage(fname, dist=""):
     else:
         st = lib().arecgb_arecReadImage(os.fsencode(fname), C.byref(im))
     return _take_image(im), st
+
+
+def arecImageTakeLog(stack):
+    """arecImageTakeLog on a copy of a host stack [nz][ny][nx]."""
+    a = np.ascontiguousarray(stack, dtype=np.float32).copy()
+    lib().arecgb_arecImageTakeLog(_cb_image(a))
+    return a
+
+
+def periodicDecomposition(stack):
+    """periodicDecomposition on a copy of a host stack [nz][ny][nx]."""
+    a = np.ascontiguousarray(stack, dtype=np.float32).copy()
+    lib().arecgb_periodicDecomposition(_cb_image(a))
+    return a
+
+
+def makePeriodicSlice(image):
+    """The smooth part S of one host image [ny][nx]."""
+    a = np.ascontiguousarray(image, dtype=np.float32).copy()
+    out = np.zeros_like(a)
+    lib().arecgb_makePeriodicSlice(a.shape[1], a.shape[0], _f32p(a), _f32p(out))
+    return out
 
 
 def arecReadImageHeader(fname):

@@ -41,6 +41,10 @@ int rotate_stack(float *d_img, const float *d_ref, int nz, int ny, int nx, float
                  int kind, int *n_rot, double *mean_cc, cudaStream_t st);
 int ncc_filtered(const float *d_a, const float *d_a2, const float *d_b, int nz, int ny, int nx,
                  double *d_cc, int npairs, cudaStream_t st);
+int take_log(float *d_x, size_t n, cudaStream_t st);
+int profile_shifts(const float *d_prof, int prof_y, int prof_x, int pad, int successive,
+                   double *shifts, double *spread, cudaStream_t st);
+int periodic_decomp(float *d, int nz, int ny, int nx, float *s_out, cudaStream_t st);
 }  // namespace arecgb
 
 using namespace arecgb;
@@ -240,6 +244,21 @@ int arecgb_rotate_images_skew_safe(float *d_img, const float *d_ref, int nz, int
 int arecgb_ncc_filtered(const float *d_a, const float *d_b, int nz, int ny, int nx, double *d_cc,
                         void *stream) {
     return ncc_filtered(d_a, nullptr, d_b, nz, ny, nx, d_cc, 1, (cudaStream_t)stream);
+}
+
+int arecgb_profile_shifts(const float *d_profiles, int prof_y, int prof_x, int pad,
+                          int successive, double *shifts, double *spread, void *stream) {
+    return profile_shifts(d_profiles, prof_y, prof_x, pad, successive, shifts, spread,
+                          (cudaStream_t)stream);
+}
+
+int arecgb_take_log(float *d_data, size_t n, void *stream) {
+    return take_log(d_data, n, (cudaStream_t)stream);
+}
+
+int arecgb_periodic_decomposition(float *d_images, int nz, int ny, int nx, float *d_smooth,
+                                  void *stream) {
+    return periodic_decomp(d_images, nz, ny, nx, d_smooth, (cudaStream_t)stream);
 }
 
 }  // extern "C"
@@ -879,6 +898,66 @@ void arecgb_arecRotateImages_skew_safe(arecImage *images, arecImage *images_ref,
                images->nz);
 }
 
+// Preprocessing over host stacks: copy in, run on the device, copy out.
+// kind 0: arecImageTakeLog (n values); 1: periodicDecomposition; 2:
+// makePeriodicSlice (smooth part of one image into out).
+static int pre_host(const char *who, int kind, float *data, size_t n, int nz, int ny, int nx,
+                    float *out) {
+    if (n == 0) return 0;
+    std::lock_guard<std::mutex> lk(g_mu);
+    float *d = nullptr;
+    cudaStream_t st = nullptr;
+    int rc = 0;
+    const size_t nbuf = kind == 2 ? 2 * n : n;
+    cudaError_t e = cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaMalloc(&d, sizeof(float) * nbuf);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(d, data, sizeof(float) * n, cudaMemcpyHostToDevice, st);
+    if (e != cudaSuccess) {
+        set_error(std::string(who) + ": " + cudaGetErrorString(e));
+        rc = cuda_status(e);
+    }
+    if (!rc) {
+        if (kind == 0)
+            rc = take_log(d, n, st);
+        else
+            rc = periodic_decomp(d, nz, ny, nx, kind == 2 ? d + n : nullptr, st);
+    }
+    if (!rc) {
+        e = cudaMemcpyAsync(kind == 2 ? out : data, kind == 2 ? d + n : d, sizeof(float) * n,
+                            cudaMemcpyDeviceToHost, st);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+        if (e != cudaSuccess) {
+            set_error(std::string(who) + ": " + cudaGetErrorString(e));
+            rc = cuda_status(e);
+        }
+    }
+    if (st) cudaStreamSynchronize(st);
+    cudaFree(d);
+    if (st) cudaStreamDestroy(st);
+    return rc;
+}
+
+// arecImageTakeLog (AREC3D/AREC3D/arecImage.cpp:358-381): in place.
+void arecgb_arecImageTakeLog(arecImage image) {
+    const size_t n = image.is_cyl != 1 ? (size_t)image.nx * image.ny * image.nz : (size_t)image.nnz;
+    if (pre_host("arecImageTakeLog", 0, image.data, n, 0, 0, 0, nullptr) && !quiet())
+        fprintf(stderr, "arecImageTakeLog: %s\n", last_error());
+}
+
+// periodicDecomposition (AREC3D/AREC3D/imagetools.cpp:77-114): in place.
+void arecgb_periodicDecomposition(arecImage img) {
+    const size_t n = (size_t)img.nx * img.ny * img.nz;
+    if (pre_host("periodicDecomposition", 1, img.data, n, img.nz, img.ny, img.nx, nullptr) &&
+        !quiet())
+        fprintf(stderr, "periodicDecomposition: %s\n", last_error());
+}
+
+// makePeriodicSlice (AREC3D/AREC3D/imagetools.cpp:17-75): smooth part of one image.
+void arecgb_makePeriodicSlice(int nx, int ny, float *data, float *out) {
+    if (pre_host("makePeriodicSlice", 2, data, (size_t)nx * ny, 1, ny, nx, out) && !quiet())
+        fprintf(stderr, "makePeriodicSlice: %s\n", last_error());
+}
+
 // ccorr2d (AREC3D/AREC3D/align2dstack.cpp:480-521).
 void arecgb_ccorr2d(int nx, int ny, float *x, float *y, float *c) {
     std::lock_guard<std::mutex> lk(g_mu);
@@ -965,3 +1044,6 @@ int arecRotCCImages(MPI_Comm m, arecImage a, arecImage b, int r2, float *ang) { 
 void arecRotateImages(arecImage *i, float *ang) { arecgb_arecRotateImages(i, ang); }
 void arecRotateImages_skew(arecImage *i, float *ang) { arecgb_arecRotateImages_skew(i, ang); }
 void arecRotateImages_skew_safe(arecImage *i, arecImage *r, float *ang) { arecgb_arecRotateImages_skew_safe(i, r, ang); }
+void arecImageTakeLog(arecImage i) { arecgb_arecImageTakeLog(i); }
+void periodicDecomposition(arecImage i) { arecgb_periodicDecomposition(i); }
+void makePeriodicSlice(int nx, int ny, float *d, float *o) { arecgb_makePeriodicSlice(nx, ny, d, o); }

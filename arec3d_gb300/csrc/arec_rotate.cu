@@ -10,6 +10,9 @@
 //                     arecRotateImages_skew_safe  arecImage.cpp:740-790
 //                       shearX_circ, shearY_circ   imagetools.cpp:171-291
 //   ncc_filtered      getNormalizedCrossCorrelationWithFilter  imagetools.cpp:331-366, 415-446
+//   profile_shifts    Prealign TubeAlign::profile_gc_img / profile_cc_img
+//                       (Prealign/Prealign/TubeAlign.cpp:128-223) with ccorr1d and
+//                       findMaxCC_fit (TubeAlign_utils.cpp:220-253, 465-479)
 //
 // Images are the reference layout [nz][ny][nx] in device memory.  The
 // reference's mixed float / double expressions are kept operation for
@@ -81,17 +84,20 @@ __global__ void k_radial_profile(const float *__restrict__ img1, const float *__
 
 constexpr int kPeakThreads = 512;
 
-__global__ void __launch_bounds__(kPeakThreads)
-    k_rot_peak(const float *__restrict__ prof, int nz, int n, float *__restrict__ angles) {
-    extern __shared__ float sh[];
-    float *x = sh, *y = sh + n, *c = sh + 3 * n;  // y holds two periods
+// Whole block: c[k] = sum_i x[i] y[(i + k) mod n] for the n values at x and y
+// (global memory), through shared memory sh (4n floats); then the first arg
+// max of c and the 7-point parabola vertex around it (PRB1D, NPOINT = 7,
+// relative to the centre; 0 when the fit is flat).  Thread 0 receives maxind
+// and pos.
+__device__ void block_ccorr_fit(const float *__restrict__ xg, const float *__restrict__ yg, int n,
+                                float *sh, int &maxind, double &pos) {
     __shared__ float bv[kPeakThreads / 32];
     __shared__ int bi[kPeakThreads / 32];
-    const int z = blockIdx.x, t = threadIdx.x;
-    const float *p1 = prof + (size_t)z * n, *p2 = prof + ((size_t)nz + z) * n;
+    float *x = sh, *y = sh + n, *c = sh + 3 * n;  // y holds two periods
+    const int t = threadIdx.x;
     for (int i = t; i < n; i += blockDim.x) {
-        x[i] = p1[i];
-        const float v = p2[i];
+        x[i] = xg[i];
+        const float v = yg[i];
         y[i] = v;
         y[i + n] = v;
     }
@@ -137,7 +143,7 @@ __global__ void __launch_bounds__(kPeakThreads)
                 bidx = bi[w];
             }
         // a profile of NaNs leaves no maximum: the reference's scan keeps index 0
-        const int maxind = bidx == INT_MAX ? 0 : bidx;
+        maxind = bidx == INT_MAX ? 0 : bidx;
         double B[7];
         for (int k = -3; k <= 3; k++) B[k + 3] = c[((maxind + k) % n + n) % n];
         // least-squares parabola through 7 points (PRB1D, NPOINT = 7)
@@ -153,14 +159,64 @@ __global__ void __launch_bounds__(kPeakThreads)
         c3 = __dsub_rn(c3, __dmul_rn(4.0, B[3]));
         c3 = __dsub_rn(c3, __dmul_rn(3.0, B[4]));
         c3 = __dadd_rn(c3, __dmul_rn(5.0, B[6]));
-        double pos = 0.0;
+        pos = 0.0;
         if (c3 != 0.0) pos = __dsub_rn(__ddiv_rn(c2, __dmul_rn(2.0, c3)), 4.0);
-        float a = (float)__dadd_rn(pos, (double)maxind);
+    }
+}
+
+__global__ void __launch_bounds__(kPeakThreads)
+    k_rot_peak(const float *__restrict__ prof, int nz, int n, float *__restrict__ angles) {
+    extern __shared__ float sh[];
+    const int z = blockIdx.x;
+    int maxind = 0;
+    double pos = 0.0;
+    block_ccorr_fit(prof + (size_t)z * n, prof + ((size_t)nz + z) * n, n, sh, maxind, pos);
+    if (threadIdx.x == 0) {
+        float a = (float)__dadd_rn(pos, (double)maxind);  // findPeak1d
         a = (float)__dmul_rn((double)a, 2.0 * kPi / n);  // index to radians
         if ((double)a > kPi) a = (float)__dsub_rn((double)a, 2.0 * kPi);
         a = (float)__dmul_rn((double)a, 180.0 / kPi);  // to degrees
         if (fabsf(a) > 45.0f) a = 0.0f;                 // "probably bad CC, do nothing"
         angles[z] = a;
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Prealign's vertical profile alignment (TubeAlign.cpp:128-223): per profile j
+// the correlation of its segment [pad, pad + L) with the mean profile
+// (ref != NULL) or with profile j - 1 (ref == NULL, j >= 1), and
+// findMaxCC_fit (TubeAlign_utils.cpp:465-479): the fitted peak, wrapped to
+// (-L, L/2].
+
+// mean profile in the reference's order: m[i] += p[j][i] / prof_y (float)
+__global__ void k_mean_profile(const float *__restrict__ prof, int prof_y, int prof_x,
+                               float *__restrict__ m) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= prof_x) return;
+    float s = 0.0f;
+    for (int j = 0; j < prof_y; j++)
+        s = __fadd_rn(s, __fdiv_rn(prof[(size_t)j * prof_x + i], (float)prof_y));
+    m[i] = s;
+}
+
+__global__ void __launch_bounds__(kPeakThreads)
+    k_profile_peak(const float *__restrict__ prof, int prof_x, int pad, int L,
+                   const float *__restrict__ ref, double *__restrict__ out) {
+    extern __shared__ float sh[];
+    const int j = blockIdx.x;
+    if (!ref && j == 0) {
+        if (threadIdx.x == 0) out[0] = 0.0;
+        return;
+    }
+    const float *x = prof + (size_t)j * prof_x + pad;
+    const float *y = ref ? ref + pad : prof + (size_t)(j - 1) * prof_x + pad;
+    int maxind = 0;
+    double pos = 0.0;
+    block_ccorr_fit(x, y, L, sh, maxind, pos);
+    if (threadIdx.x == 0) {
+        double r = 1.0 * (maxind + pos);
+        if (r > L / 2) r -= L;
+        out[j] = r;
     }
 }
 
@@ -455,6 +511,61 @@ int rot_cc_angles(const float *d1, const float *d2, int nz, int ny, int nx, int 
     ARECGB_CUDA(cudaGetLastError());
     // the scratch is freed after the work that reads it
     ARECGB_CUDA(cudaStreamSynchronize(st));
+    return 0;
+}
+
+// TubeAlign::profile_gc_img (successive = 0) / profile_cc_img (successive = 1)
+// (Prealign/Prealign/TubeAlign.cpp:128-223): the per-profile shifts after the
+// reference's damping (global: |s| > 10 -> s * pad / s^2) or integration
+// (successive: running sum), with their mean removed, into shifts (host,
+// prof_y values); spread = |max - min| before the mean removal.  The caller
+// applies sY[j] -= shifts[j] as the reference does.
+int profile_shifts(const float *d_prof, int prof_y, int prof_x, int pad, int successive,
+                   double *shifts, double *spread, cudaStream_t st) {
+    const int L = prof_x - 2 * pad;
+    if (prof_y < 1 || pad < 0 || L < 1 || L > 14000) {
+        set_error("profile_shifts: need prof_y >= 1, pad >= 0, 1 <= prof_x - 2 pad <= 14000");
+        return ARECGB_ERR_ARG;
+    }
+    DevBuf buf;
+    ARECGB_CUDA(cudaMalloc(&buf.p, sizeof(double) * prof_y + sizeof(float) * prof_x));
+    double *d_out = (double *)buf.p;
+    float *d_mean = (float *)(d_out + prof_y);
+    if (!successive) {
+        k_mean_profile<<<(prof_x + 127) / 128, 128, 0, st>>>(d_prof, prof_y, prof_x, d_mean);
+        count_launches(1);
+    }
+    const size_t smem = sizeof(float) * 4 * (size_t)L;
+    ARECGB_CUDA(cudaFuncSetAttribute(k_profile_peak, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     (int)smem));
+    k_profile_peak<<<prof_y, kPeakThreads, smem, st>>>(d_prof, prof_x, pad, L,
+                                                      successive ? nullptr : d_mean, d_out);
+    count_launches(1);
+    ARECGB_CUDA(cudaGetLastError());
+    std::vector<double> s(prof_y);
+    ARECGB_CUDA(cudaMemcpyAsync(s.data(), d_out, sizeof(double) * prof_y, cudaMemcpyDeviceToHost,
+                                st));
+    ARECGB_CUDA(cudaStreamSynchronize(st));
+    if (!successive) {
+        for (int j = 0; j < prof_y; j++) {
+            const double shift = std::fabs(s[j]);
+            if (shift > 10.0) {
+                s[j] *= pad;
+                s[j] /= shift * shift;
+            }
+        }
+    } else {
+        for (int j = 1; j < prof_y; j++) s[j] += s[j - 1];
+    }
+    double mn = s[0], mx = s[0], mean = 0.0;
+    for (int j = 0; j < prof_y; j++) {
+        if (s[j] < mn) mn = s[j];
+        if (s[j] > mx) mx = s[j];
+        mean += s[j];
+    }
+    mean /= prof_y;
+    for (int j = 0; j < prof_y; j++) shifts[j] = s[j] - mean;
+    if (spread) *spread = std::fabs(mx - mn);
     return 0;
 }
 

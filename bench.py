@@ -503,7 +503,13 @@ def main():
                          "frac": flops / t_dom / 1e12 / fp32_peak},
                 "fp_ms": fp_avg * 1e3, "bp_ms": bp_avg * 1e3,
                 "fp_calls": fp_calls, "bp_calls": bp_calls,
-                "projector_share_of_step": (fp_ms + bp_ms) / (ms_step * args.steps)}
+                # projections per step: the timed (non-graph) calls plus one forward and
+                # one back projection per CGLS iteration replayed from the CUDA graph
+                "projector_ms_per_step": (fp_avg * (fp_calls / args.steps + n_it) +
+                                          bp_avg * (bp_calls / args.steps + n_it)) * 1e3,
+                "projector_share_of_step": (fp_avg * (fp_calls / args.steps + n_it) +
+                                            bp_avg * (bp_calls / args.steps + n_it)) * 1e3 /
+                ms_step}
 
     # End to end through the C ABI over pinned host buffers: the reference
     # layout sinogram goes up, the reconstruction comes back, every step.

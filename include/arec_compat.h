@@ -17,6 +17,8 @@
  *   arecRotCCImages                                          AREC3D/AREC3D/arecImage.h:37
  *   arecRotateImages, arecRotateImages_skew,
  *   arecRotateImages_skew_safe                               AREC3D/AREC3D/arecImage.h:46-48
+ *   arecImageTakeLog                                         AREC3D/AREC3D/arecImage.h:34
+ *   makePeriodicSlice, periodicDecomposition                 AREC3D/AREC3D/imagetools.h:4-5
  *   arecReadImageHeader, arecReadImage, arecWriteImage       AREC3D/AREC3D/arecImageIO.h:65-67
  *   arecReadImageDistbyZ, arecReadImageDistbyY,
  *   arecWriteImageMergeY, arecWriteImageMergeZ               AREC3D/AREC3D/arecImageIO_mpi.h:3-6
@@ -115,6 +117,11 @@ int arecgb_arecRotCCImages(MPI_Comm comm, arecImage images1, arecImage images2, 
 void arecgb_arecRotateImages(arecImage *images, float *angles);
 void arecgb_arecRotateImages_skew(arecImage *images, float *angles);
 void arecgb_arecRotateImages_skew_safe(arecImage *images, arecImage *images_ref, float *angles);
+
+/* Preprocessing (in place on host stacks). */
+void arecgb_arecImageTakeLog(arecImage image);
+void arecgb_periodicDecomposition(arecImage img);
+void arecgb_makePeriodicSlice(int nx, int ny, float *data, float *out);
 
 /* MRC files (one rank: the distributed forms read and write the whole stack;
  * failures print and leave image->data NULL where the reference aborts). */

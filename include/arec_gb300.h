@@ -194,6 +194,35 @@ int arecgb_rotate_images_skew_safe(float *d_img, const float *d_ref, int nz, int
 int arecgb_ncc_filtered(const float *d_a, const float *d_b, int nz, int ny, int nx, double *d_cc,
                         void *stream);
 
+/* ---- Preprocessing of the image stack (AREC3D/AREC3D/AREC3D.cpp:81,105) ----
+ * -log(v) for v > 0, else 0, in place over n floats (replaces arecImageTakeLog,
+ * AREC3D/AREC3D/arecImage.cpp:358-381). */
+int arecgb_take_log(float *d_data, size_t n, void *stream);
+
+/* Periodic-plus-smooth decomposition of each image of a device stack
+ * [nz][ny][nx] (replaces periodicDecomposition, AREC3D/AREC3D/imagetools.cpp:
+ * 77-114, with makePeriodicSlice :17-75): S solves the periodic Poisson
+ * equation for the boundary jumps (DFT, divide by 2cos + 2cos - 4, zero mean),
+ * and the image loses exp(-dist^2/50) S, dist = distance to the border.  Any
+ * nx in [2, 65536], ny in [2, 65535].  d_smooth != NULL: write S there instead
+ * and leave the images.  Synchronises. */
+int arecgb_periodic_decomposition(float *d_images, int nz, int ny, int nx, float *d_smooth,
+                                  void *stream);
+
+/* Prealign's vertical alignment of projection profiles (replaces the
+ * correlation loops of TubeAlign::profile_gc_img, successive = 0, and
+ * TubeAlign::profile_cc_img, successive = 1; Prealign/Prealign/TubeAlign.cpp:
+ * 128-223, with ccorr1d and findMaxCC_fit, TubeAlign_utils.cpp:220-253,
+ * 465-479).  d_profiles: prof_y profiles of prof_x floats (device).  Each
+ * profile's segment [pad, prof_x - pad) is correlated with the mean profile's
+ * (global) or with the previous profile's (successive); the fitted peaks are
+ * damped (global: |s| > 10 -> s pad / s^2) or summed (successive), and their
+ * mean removed: shifts (host, prof_y doubles); spread (host, optional) =
+ * max - min before the mean removal.  The caller applies sY[j] -= shifts[j].
+ * Synchronises. */
+int arecgb_profile_shifts(const float *d_profiles, int prof_y, int prof_x, int pad,
+                          int successive, double *shifts, double *spread, void *stream);
+
 /* ---- MRC image stacks (the reference's file format, arecImageIO.h:12-63) ----
  * Header of an MRC file: sizes and mode (1, 6: 16-bit, read as signed; 2:
  * float32).  (Replaces arecReadImageHeader, AREC3D/AREC3D/arecImageIO.cpp:10.) */

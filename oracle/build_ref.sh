@@ -5,6 +5,8 @@
 #                                cross-correlation) over the single-rank MPI and
 #                                FFTW-API stand-ins in oracle/shim/
 #   oracle/_ref/arec_ref_catch   the reference's own Catch unit tests
+#   oracle/_ref/libprealign_ref.so  Prealign's profile correlation
+#                                (TubeAlign_utils.cpp) over the same stand-ins
 # Test infrastructure only: nothing in the product links these.
 #
 # FP contraction is switched off (-ffp-contract=off) so that the build's double
@@ -44,6 +46,19 @@ objs=()
 for u in "${UNITS[@]}"; do objs+=("$OUT/$u.o"); done
 "$CXX" -shared -o "$OUT/libarec_ref.so" "${objs[@]}" "$OUT/mpi_shim.o" "$OUT/fftw_shim.o" \
     "$OUT/fft64.o" -lm -Wl,--no-undefined
+
+# Prealign's profile correlation (ccorr1d, findMaxCC_fit) in its own library:
+# its ccorr1d has the same C++ name as AREC3D's.
+PRE="$REF/Prealign/Prealign"
+if [ -f "$PRE/TubeAlign_utils.cpp" ]; then
+    "$CXX" -std=c++17 "${FLAGS[@]}" -I"$HERE/shim" -I"$PRE" -c "$PRE/TubeAlign_utils.cpp" \
+        -o "$OUT/TubeAlign_utils.o"
+    "$CXX" -std=c++17 "${FLAGS[@]}" -I"$PRE" -c "$PRE/mpfit.cpp" -o "$OUT/mpfit.o"
+    "$CC" -std=c99 "${FLAGS[@]}" -I"$HERE/shim" -c "$HERE/shim/fftw_shim.c" -o "$OUT/fftw_shim2.o"
+    "$CC" -std=c99 "${FLAGS[@]}" -c "$HERE/fft64.c" -o "$OUT/fft64_2.o"
+    "$CXX" -shared -o "$OUT/libprealign_ref.so" "$OUT/TubeAlign_utils.o" "$OUT/mpfit.o" \
+        "$OUT/fftw_shim2.o" "$OUT/fft64_2.o" -lm -Wl,--no-undefined
+fi
 
 # The Catch suite is stored as UTF-16; convert a copy into _ref and build it.
 if [ -f "$TST/AREC3D_test.cpp" ]; then

@@ -3,9 +3,10 @@ itself (AREC3D, compiled from its own sources into oracle/_ref by
 oracle/build_ref.sh) on small seeded inputs.  Run in the container that has the
 reference checkout:
 
-    bash oracle/build_ref.sh && python tests/golden/make_golden.py [--rotation]
+    bash oracle/build_ref.sh && python tests/golden/make_golden.py [--rotation|--preprocess|--prealign]
 
-(--rotation writes only reference_rotation.npz.)
+(each flag writes only its own file: reference_rotation.npz,
+reference_preprocess.npz, reference_prealign.npz.)
 
 The reference's linear weighting (pmethod=1) reads two entries past its
 coordinate table; to make those reads return zero (as they do for large tables
@@ -143,9 +144,94 @@ def rotation():
     print("wrote", os.path.join(HERE, "reference_rotation.npz"))
 
 
+def preprocess():
+    """arecImageTakeLog and periodicDecomposition / makePeriodicSlice on seeded
+    stacks (sizes 3 x 24 x 40 and 1 x 33 x 50: even and odd)."""
+    import ctypes as C
+
+    import oracle as O
+
+    R = O.Reference()
+    rng = np.random.default_rng(20261205)
+    out = {}
+    raw = (rng.random((3, 24, 40)) * 2.0).astype(np.float32)
+    raw[0, 0, :4] = [0.0, -1.0, 1.0, 1e-30]
+    out["log_in"] = raw
+    a = raw.copy()
+    f = R.L._Z16arecImageTakeLog5Image
+    f.argtypes = [O.ArecImage]
+    f.restype = None
+    f(R._cb(a))
+    out["log_out"] = a
+    pd = R.L._Z21periodicDecomposition5Image
+    pd.argtypes = [O.ArecImage]
+    pd.restype = None
+    mk = R.L._Z17makePeriodicSliceiiPfS_
+    mk.argtypes = [C.c_int, C.c_int, O._f32p, O._f32p]
+    mk.restype = None
+    for tag, shape in (("even", (3, 24, 40)), ("odd", (1, 33, 50))):
+        nz, ny, nx = shape
+        img = (rng.random(shape) + np.linspace(0, 4, nx)[None, None, :] +
+               np.linspace(0, 2, ny)[None, :, None]).astype(np.float32)
+        out["pd_%s_in" % tag] = img
+        s = np.zeros((ny, nx), np.float32)
+        mk(nx, ny, img[0].copy(), s)
+        out["pd_%s_smooth0" % tag] = s
+        a = img.copy()
+        pd(R._cb(a))
+        out["pd_%s_out" % tag] = a
+    np.savez_compressed(os.path.join(HERE, "reference_preprocess.npz"), **out)
+    print("wrote", os.path.join(HERE, "reference_preprocess.npz"))
+
+
+def prealign():
+    """Prealign's profile alignment: the two TubeAlign correlation loops as the
+    oracle restates them, with ccorr1d and findMaxCC_fit taken from the
+    reference's own TubeAlign_utils.cpp (oracle/_ref/libprealign_ref.so)."""
+    import ctypes as C
+
+    from oracle import prealign as P
+
+    L = C.CDLL(os.path.join(ROOT, "oracle", "_ref", "libprealign_ref.so"))
+    f32p = np.ctypeslib.ndpointer(np.float32, flags="C_CONTIGUOUS")
+    cc = L._Z7ccorr1diPfS_S_
+    cc.argtypes = [C.c_int, f32p, f32p, f32p]
+    cc.restype = None
+    fit = L._Z13findMaxCC_fitPKfi
+    fit.argtypes = [f32p, C.c_int]
+    fit.restype = C.c_double
+
+    def ref_pair(x, y):
+        n = len(x)
+        c = np.zeros(n, np.float32)
+        cc(n, np.ascontiguousarray(x, np.float32).copy(), np.ascontiguousarray(y, np.float32).copy(), c)
+        return fit(c, n)
+
+    rng = np.random.default_rng(20261206)
+    prof_y, prof_x, pad = 12, 200, 20
+    t = np.arange(prof_x)
+    drift = np.cumsum(rng.normal(0, 1.5, prof_y))
+    prof = np.stack([np.exp(-((t - 100 - d) / 18.0) ** 2) + 0.4 * np.exp(-((t - 60 - d) / 6.0) ** 2)
+                     for d in drift]).astype(np.float32)
+    prof += (0.01 * rng.standard_normal(prof.shape)).astype(np.float32)
+    out = {"profiles": prof, "pad": np.array(pad)}
+    for tag, succ in (("global", False), ("successive", True)):
+        s, spread = P.profile_shifts(prof, pad, succ, fit_pair=ref_pair)
+        out[tag + "_shifts"] = s
+        out[tag + "_spread"] = np.array(spread)
+    np.savez_compressed(os.path.join(HERE, "reference_prealign.npz"), **out)
+    print("wrote", os.path.join(HERE, "reference_prealign.npz"))
+
+
 if __name__ == "__main__":
     if "--rotation" in sys.argv:
         rotation()
+    elif "--preprocess" in sys.argv:
+        preprocess()
+    elif "--prealign" in sys.argv:
+        prealign()
     else:
         main()
         rotation()
+        preprocess()
+        prealign()

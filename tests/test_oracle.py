@@ -312,3 +312,67 @@ print("ok")
 """ % ROOT
     r = subprocess.run([sys.executable, "-c", code], capture_output=True, text=True)
     assert r.returncode == 0 and "ok" in r.stdout, (r.stdout[-1500:], r.stderr[-2000:])
+
+
+# ---- preprocessing (arecImageTakeLog, periodicDecomposition) ---------------------------------
+PRE_GOLD = os.path.join(ROOT, "tests", "golden", "reference_preprocess.npz")
+
+
+def test_golden_preprocess_oracle():
+    """The oracle's take-log (bit for bit) and periodic decomposition against
+    the reference's outputs; the decomposition within one float rounding of
+    its FFTs (the reference's spectrum passes through float)."""
+    from oracle import preprocess as P
+
+    g = np.load(PRE_GOLD)
+    assert np.array_equal(P.take_log(g["log_in"]), g["log_out"])
+    for tag in ("even", "odd"):
+        img = g["pd_%s_in" % tag]
+        s = P.make_periodic_slice(img[0])
+        ref_s = g["pd_%s_smooth0" % tag]
+        assert np.abs(s - ref_s).max() <= 1e-6 * np.abs(ref_s).max()
+        out = P.periodic_decomposition(img)
+        assert np.abs(out - g["pd_%s_out" % tag]).max() <= 1e-6 * np.abs(img).max()
+
+
+# ---- Prealign profile alignment ---------------------------------------------------------------
+PRE_REF = os.path.join(ROOT, "oracle", "_ref", "libprealign_ref.so")
+
+
+def test_golden_prealign_oracle():
+    """The oracle's TubeAlign profile loops (its own ccorr1d and findMaxCC_fit)
+    against the same loops over the reference's pieces: within the float
+    rounding of the correlation as the 7-point fit sees it (1e-5 px)."""
+    from oracle import prealign as P
+
+    g = np.load(os.path.join(ROOT, "tests", "golden", "reference_prealign.npz"))
+    for tag, succ in (("global", False), ("successive", True)):
+        s, spread = P.profile_shifts(g["profiles"], int(g["pad"]), succ)
+        assert np.abs(s - g[tag + "_shifts"]).max() < 1e-5
+        assert abs(spread - float(g[tag + "_spread"])) < 1e-5
+
+
+@pytest.mark.skipif(not os.path.exists(PRE_REF), reason="reference not built here")
+def test_prealign_pieces_against_reference_build():
+    """findMaxCC_fit bit for bit on the reference's own correlation, and the
+    oracle's ccorr1d within float rounding of the reference's."""
+    import ctypes as C
+
+    from oracle import prealign as P
+
+    L = C.CDLL(PRE_REF)
+    f32p = np.ctypeslib.ndpointer(np.float32, flags="C_CONTIGUOUS")
+    cc = L._Z7ccorr1diPfS_S_
+    cc.argtypes = [C.c_int, f32p, f32p, f32p]
+    cc.restype = None
+    fit = L._Z13findMaxCC_fitPKfi
+    fit.argtypes = [f32p, C.c_int]
+    fit.restype = C.c_double
+    rng = np.random.default_rng(2)
+    for n in (7, 64, 97, 300):
+        x = rng.standard_normal(n).astype(np.float32)
+        y = (np.roll(x, 3) + 0.1 * rng.standard_normal(n)).astype(np.float32)
+        c = np.zeros(n, np.float32)
+        cc(n, x.copy(), y.copy(), c)
+        assert np.abs(c - P.ccorr1d(x, y)).max() <= 1e-6 * np.abs(c).max()
+        assert fit(c, n) == P.find_max_cc_fit(c)
