@@ -202,6 +202,18 @@ int arecgb_plan_autotune(arecgb_plan *plan, float *d_x, float *d_q, int *fp_band
     return rc;
 }
 
+int arecgb_plan_shapes(const arecgb_plan *plan, int *fp_band, int *bp_vec, int *bp_nsc) {
+    if (!plan) {
+        set_error("arecgb_plan_shapes: null plan");
+        return ARECGB_ERR_ARG;
+    }
+    const Plan *p = reinterpret_cast<const Plan *>(plan);
+    if (fp_band) *fp_band = p->fp_band;
+    if (bp_vec) *bp_vec = p->bp_vec ? p->bp_vec : p->vec;
+    if (bp_nsc) *bp_nsc = p->bp_nsc;
+    return 0;
+}
+
 int arecgb_cc_shifts(const float *d_img1, const float *d_img2, int nz, int ny, int nx,
                      float *d_sx, float *d_sy, int *d_ix, int *d_iy, void *stream) {
     return cc_shifts(d_img1, d_img2, nz, ny, nx, d_sx, d_sy, d_ix, d_iy, (cudaStream_t)stream);

@@ -229,8 +229,10 @@ int plan_create(Plan **out, int weighting, double radius, int ny, int nangles,
         e = cudaMemcpy(p->d_cols, cols.data(), sizeof(ColInfo) * nx, cudaMemcpyHostToDevice);
     if (e == cudaSuccess) {
         // room for the back projector's grid with one slice chunk per block
-        // (the autotuner may choose it): ntiles x ceil(ys / (32 vec)) blocks
-        const int bp_max = p->ntiles * ((p->ys + 32 * p->vec - 1) / (32 * p->vec));
+        // at half the vector width (the autotuner may choose it):
+        // ntiles x ceil(ys / (32 max(1, vec / 2))) blocks
+        const int hv = std::max(1, p->vec / 2);
+        const int bp_max = p->ntiles * ((p->ys + 32 * hv - 1) / (32 * hv));
         p->n_partials = std::max(std::max(fp_grid_blocks(p), bp_grid_blocks(p)), bp_max);
         e = cudaMalloc(&p->d_partials, sizeof(double) * (size_t)p->n_partials);
     }

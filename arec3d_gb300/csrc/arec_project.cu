@@ -36,14 +36,18 @@ static OpArgs make_args(const Plan *p, const int *skip) {
     return A;
 }
 
+// Back projection: floats per lane (the plan's, or the autotuner's choice).
+static int bp_vec(const Plan *p) { return p->bp_vec ? p->bp_vec : p->vec; }
+
 // Slice chunks per block: two warps' worth of slices when there are that many.
 static int slice_chunks(const Plan *p) {
-    if (p->bp_nsc == 1 || (p->bp_nsc == 2 && p->ys > 32 * p->vec)) return p->bp_nsc;
-    return p->ys > 32 * p->vec ? 2 : 1;
+    const int v = bp_vec(p);
+    if (p->bp_nsc == 1 || (p->bp_nsc == 2 && p->ys > 32 * v)) return p->bp_nsc;
+    return p->ys > 32 * v ? 2 : 1;
 }
 
 static int slice_blocks(const Plan *p) {
-    const int span = 32 * p->vec * slice_chunks(p);
+    const int span = 32 * bp_vec(p) * slice_chunks(p);
     return (p->ys + span - 1) / span;
 }
 
@@ -167,11 +171,11 @@ int back_project(const Plan *p, const float *d_s, float *d_g, double *d_norm2,
     if (rc) return rc;
     count_launches(d_norm2 ? 2 : 1);
     if (p->weighting == ARECGB_LIN)
-        rc = launch_bp_lin(A, p->vec, nsc, grid, d_s, d_g, st);
+        rc = launch_bp_lin(A, bp_vec(p), nsc, grid, d_s, d_g, st);
     else if (p->weighting == ARECGB_KB)
-        rc = launch_bp_kb(A, p->vec, nsc, grid, d_s, d_g, st);
+        rc = launch_bp_kb(A, bp_vec(p), nsc, grid, d_s, d_g, st);
     else
-        rc = launch_bp_sq(A, p->vec, nsc, grid, d_s, d_g, st);
+        rc = launch_bp_sq(A, bp_vec(p), nsc, grid, d_s, d_g, st);
     ARECGB_CUDA(cudaGetLastError());
     if (rc) return ARECGB_ERR_ARG;
     if (d_norm2) {
@@ -222,11 +226,17 @@ int plan_autotune(Plan *p, float *d_x, float *d_q, cudaStream_t st) {
         }
     }
     p->fp_band = best_band;
-    int best_nsc = 0;
+    // back projection: (floats per lane, slice chunks per block) in
+    // {(vec, 1), (vec, 2), (vec / 2, 1)}: half the vector width halves the
+    // accumulators and the staged rows (more blocks per SM)
+    int best_nsc = 0, best_vec = 0;
     best = 1e30f;
-    for (int nsc : {1, 2}) {
+    const int shapes[3][2] = {{p->vec, 1}, {p->vec, 2}, {p->vec / 2, 1}};
+    for (const auto &sh : shapes) {
         if (rc) break;
-        if (nsc == 2 && p->ys <= 32 * p->vec) continue;
+        const int v = sh[0], nsc = sh[1];
+        if (v < 1 || (nsc == 2 && p->ys <= 32 * v)) continue;
+        p->bp_vec = v;
         p->bp_nsc = nsc;
         float ms;
         if ((rc = best_of([&] { return back_project(p, d_q, d_x, nullptr, nullptr, st); }, &ms)))
@@ -234,9 +244,11 @@ int plan_autotune(Plan *p, float *d_x, float *d_q, cudaStream_t st) {
         if (ms < best) {
             best = ms;
             best_nsc = nsc;
+            best_vec = v;
         }
     }
     p->bp_nsc = best_nsc;
+    p->bp_vec = best_vec;
     p->tuned = rc ? 0 : 1;
     p->timing = was_timing;
     cudaEventDestroy(e0);

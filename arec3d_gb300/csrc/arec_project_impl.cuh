@@ -194,13 +194,30 @@ __device__ __forceinline__ void cp_async_wait() {
 // One staged footprint row (a bin's slices) into a lane's registers; a bin off
 // the detector was never copied and reads as zero.
 template <int VEC>
-__device__ __forceinline__ void foot_row(const float *row, int bin, int nx, int lane,
-                                         float (&v)[VEC]) {
-    if ((unsigned)bin < (unsigned)nx) {
+__device__ __forceinline__ void foot_row(const float *row, bool on, int lane, float (&v)[VEC]) {
+    if (on) {
         lds_lane<VEC>(row, lane, v);
     } else {
 #pragma unroll
         for (int q = 0; q < VEC; q++) v[q] = 0.f;
+    }
+}
+
+// acc += w * v element-wise, in pairs on the packed FP32 FMA (each lane of the
+// pair is fmaf(w, v, acc), rounded once).
+template <int VEC>
+__device__ __forceinline__ void fma_row(float (&acc)[VEC], float w, const float (&v)[VEC]) {
+    if constexpr (VEC >= 2) {
+        const float2 w2 = make_float2(w, w);
+#pragma unroll
+        for (int q = 0; q < VEC; q += 2) {
+            const float2 r = __ffma2_rn(w2, make_float2(v[q], v[q + 1]),
+                                        make_float2(acc[q], acc[q + 1]));
+            acc[q] = r.x;
+            acc[q + 1] = r.y;
+        }
+    } else {
+        acc[0] = fmaf(w, v[0], acc[0]);
     }
 }
 
@@ -277,18 +294,60 @@ __global__ void __launch_bounds__(128 * NSC + 32)
         const int nac = min(AC, A.na - a0);
         for (int ai = warp; ai < AC; ai += NCW + 1) {
             const int a = a0 + ai;
-            float4 e = make_float4(__int_as_float(INT_MIN / 2), 0.f, 0.f, 0.f);
-            int lo = INT_MAX, hi = INT_MIN;
+            Taps t{};
+            int b = INT_MIN / 2, lo = INT_MAX, hi = INT_MIN;
             if (a < A.na && k >= 0) {
-                const Taps t = ray_taps<W>(myray, A.ang[a], A.r_hi, A.r_lo);
-                e = make_float4(__int_as_float(t.iqx - 1), t.w0, t.w1, t.w2);
-                lo = hi = t.iqx - 1;
+                t = ray_taps<W>(myray, A.ang[a], A.r_hi, A.r_lo);
+                b = lo = hi = t.iqx - 1;
             }
-            sw[ai * 32 + lane] = e;
             for (int o = 16; o > 0; o >>= 1) {
                 lo = min(lo, __shfl_xor_sync(0xffffffffu, lo, o));
                 hi = max(hi, __shfl_xor_sync(0xffffffffu, hi, o));
             }
+            // The accumulating warp of each row of 8 rays keeps the three bins
+            // b .. b+2 of its current ray in a register ring; plan, per ray,
+            // which ring slot takes which footprint row (the centre bin moves
+            // by at most one bin between neighbouring pixels), and rotate the
+            // weights to the slots.  code: bits 0-1 action (0 skip, 1 same
+            // bins, 2 one row enters slot bits 2-3, 3 three rows), bits 4-6
+            // bins on the detector, bits 8+ footprint row.
+            const bool use = b != INT_MIN / 2 && b - lo <= FW - 3;
+            const int gbase = lane & ~7;
+            int cb = INT_MIN / 4, m = 0, my_code = 0, my_m = 0;
+#pragma unroll
+            for (int r = 0; r < 8; r++) {
+                const int br = __shfl_sync(0xffffffffu, b, gbase + r);
+                const int ur = __shfl_sync(0xffffffffu, (int)use, gbase + r);
+                int code = 0;
+                if (ur) {
+                    const int d = br - cb, rr = br - lo;
+                    if (d == 0) {
+                        code = 1;
+                    } else if (d == 1) {  // bin cb (slot m) leaves, bin br + 2 enters
+                        code = 2 | (m << 2) | ((unsigned)(br + 2) < (unsigned)A.nx ? 16 : 0) |
+                               ((rr + 2) << 8);
+                        m = m == 2 ? 0 : m + 1;
+                    } else if (d == -1) {  // bin cb + 2 leaves, bin br enters
+                        m = m == 0 ? 2 : m - 1;
+                        code = 2 | (m << 2) | ((unsigned)br < (unsigned)A.nx ? 16 : 0) | (rr << 8);
+                    } else {
+                        code = 3 | ((unsigned)br < (unsigned)A.nx ? 16 : 0) |
+                               ((unsigned)(br + 1) < (unsigned)A.nx ? 32 : 0) |
+                               ((unsigned)(br + 2) < (unsigned)A.nx ? 64 : 0) | (rr << 8);
+                        m = 0;
+                    }
+                    cb = br;
+                }
+                if ((lane & 7) == r) {
+                    my_code = code;
+                    my_m = m;
+                }
+            }
+            // slot s holds bin b + ((s - m) mod 3): its weight is w_{(s - m) mod 3}
+            const float wa = my_m == 0 ? t.w0 : (my_m == 1 ? t.w2 : t.w1);
+            const float wb = my_m == 0 ? t.w1 : (my_m == 1 ? t.w0 : t.w2);
+            const float wc = my_m == 0 ? t.w2 : (my_m == 1 ? t.w1 : t.w0);
+            sw[ai * 32 + lane] = make_float4(__int_as_float(my_code), wa, wb, wc);
             if (lane == 0) {
                 if (hi - lo + 3 > FW && lo != INT_MAX) atomicOr(A.err, 2);
                 fb[ai] = lo == INT_MAX ? 0 : lo;
@@ -323,53 +382,32 @@ __global__ void __launch_bounds__(128 * NSC + 32)
                 }
                 if (ok && yok) {
                     const float *F = foot + (size_t)buf * FW * SPAN + yw;
-                    const int fb0 = fb[ai];
-                    // Three-bin window of footprint rows in registers, kept as a
-                    // ring: slot s holds bin cb + ((s - m) mod 3).  The 8 rays
-                    // are consecutive pixels of one row, so the centre bin moves
-                    // by at most one bin from ray to ray (|cos| <= 1): the ring
-                    // replaces one slot and rotates the weights instead of
-                    // reloading three rows.  Bins off the detector read as zero
-                    // (w * 0 adds nothing).
-                    float R0[VEC], R1[VEC], R2[VEC];
+                    float R0[VEC], R1[VEC], R2[VEC];  // the ring (slots 0, 1, 2)
 #pragma unroll
                     for (int q = 0; q < VEC; q++) R0[q] = R1[q] = R2[q] = 0.f;
-                    int cb = INT_MIN / 4, m = 0;  // bin held in slot m (none yet)
 #pragma unroll
                     for (int r = 0; r < 8; r++) {
                         const float4 e = sw[ai * 32 + rg * 8 + r];
-                        const int b = __float_as_int(e.x), rb = b - fb0;
-                        if (rb >= 0 && rb <= FW - 3) {
-                            const int d = b - cb;
-                            if (d == 1) {  // bin cb (slot m) leaves, bin b + 2 enters
-                                const float *row = F + (rb + 2) * SPAN;
-                                if (m == 0) foot_row<VEC>(row, b + 2, A.nx, lane, R0);
-                                else if (m == 1) foot_row<VEC>(row, b + 2, A.nx, lane, R1);
-                                else foot_row<VEC>(row, b + 2, A.nx, lane, R2);
-                                m = m == 2 ? 0 : m + 1;
-                            } else if (d == -1) {  // bin cb + 2 leaves, bin b enters
-                                m = m == 0 ? 2 : m - 1;
-                                const float *row = F + rb * SPAN;
-                                if (m == 0) foot_row<VEC>(row, b, A.nx, lane, R0);
-                                else if (m == 1) foot_row<VEC>(row, b, A.nx, lane, R1);
-                                else foot_row<VEC>(row, b, A.nx, lane, R2);
-                            } else if (d != 0) {
-                                foot_row<VEC>(F + rb * SPAN, b, A.nx, lane, R0);
-                                foot_row<VEC>(F + (rb + 1) * SPAN, b + 1, A.nx, lane, R1);
-                                foot_row<VEC>(F + (rb + 2) * SPAN, b + 2, A.nx, lane, R2);
-                                m = 0;
-                            }
-                            cb = b;
-                            const float w0 = m == 0 ? e.y : (m == 1 ? e.w : e.z);
-                            const float w1 = m == 0 ? e.z : (m == 1 ? e.y : e.w);
-                            const float w2 = m == 0 ? e.w : (m == 1 ? e.z : e.y);
-#pragma unroll
-                            for (int q = 0; q < VEC; q++) {
-                                acc[r][q] = fmaf(w0, R0[q], acc[r][q]);
-                                acc[r][q] = fmaf(w1, R1[q], acc[r][q]);
-                                acc[r][q] = fmaf(w2, R2[q], acc[r][q]);
-                            }
+                        const int code = __float_as_int(e.x), act = code & 3;
+                        if (act == 0) continue;
+                        const float *row = F + (code >> 8) * SPAN;
+                        if (act == 2) {
+                            const int slot = (code >> 2) & 3;
+                            const bool on = code & 16;
+                            if (slot == 0)
+                                foot_row<VEC>(row, on, lane, R0);
+                            else if (slot == 1)
+                                foot_row<VEC>(row, on, lane, R1);
+                            else
+                                foot_row<VEC>(row, on, lane, R2);
+                        } else if (act == 3) {
+                            foot_row<VEC>(row, code & 16, lane, R0);
+                            foot_row<VEC>(row + SPAN, code & 32, lane, R1);
+                            foot_row<VEC>(row + 2 * SPAN, code & 64, lane, R2);
                         }
+                        fma_row<VEC>(acc[r], e.y, R0);
+                        fma_row<VEC>(acc[r], e.z, R1);
+                        fma_row<VEC>(acc[r], e.w, R2);
                     }
                 }
                 __syncwarp();
@@ -755,21 +793,10 @@ __global__ void __launch_bounds__(kFpThreads, 3)
                         en = E[i + 1];
                         lds_lane<VEC>(S + (__float_as_int(en.x) & 255) * SPAN, lane, vn);
                     }
-                    if (gg >= 2) {
-#pragma unroll
-                        for (int c = 0; c < VEC; c++) acc[gg >= 2 ? gg - 2 : 0][c] =
-                            fmaf(e.y, v[c], acc[gg >= 2 ? gg - 2 : 0][c]);
-                    }
-                    if (gg >= 1 && gg <= BT) {
-#pragma unroll
-                        for (int c = 0; c < VEC; c++) acc[(gg >= 1 && gg <= BT) ? gg - 1 : 0][c] =
-                            fmaf(e.z, v[c], acc[(gg >= 1 && gg <= BT) ? gg - 1 : 0][c]);
-                    }
-                    if (gg <= BT - 1) {
-#pragma unroll
-                        for (int c = 0; c < VEC; c++) acc[gg <= BT - 1 ? gg : 0][c] =
-                            fmaf(e.w, v[c], acc[gg <= BT - 1 ? gg : 0][c]);
-                    }
+                    if (gg >= 2) fma_row<VEC>(acc[gg >= 2 ? gg - 2 : 0], e.y, v);
+                    if (gg >= 1 && gg <= BT)
+                        fma_row<VEC>(acc[(gg >= 1 && gg <= BT) ? gg - 1 : 0], e.z, v);
+                    if (gg <= BT - 1) fma_row<VEC>(acc[gg <= BT - 1 ? gg : 0], e.w, v);
                     e = en;
 #pragma unroll
                     for (int c = 0; c < VEC; c++) v[c] = vn[c];

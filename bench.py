@@ -331,11 +331,21 @@ def kernels_only(args):
     x[:, args.slices:] = 0
     q = torch.zeros(plan.nangles, plan.nx, plan.ys, device="cuda")
     n2 = torch.zeros(1, dtype=torch.float64, device="cuda")
+    tuned = None
+    if args.tune:
+        plan.autotune(x, q)
+        tuned = plan.shapes()
+        x.uniform_(generator=g)
+        x[:, args.slices:] = 0
+    plan.timing(1)
     for _ in range(args.launches):
         plan.project(x, q, norm2=n2)
         plan.backproject(q, x, norm2=n2)
     torch.cuda.synchronize()
+    fp_ms, fp_n, bp_ms, bp_n = plan.timing(0)
     print(json.dumps({"kernels_only": True, "slices": args.slices, "launches": args.launches,
+                      "fp_ms": fp_ms / max(fp_n, 1), "bp_ms": bp_ms / max(bp_n, 1),
+                      "autotuned": tuned,
                       "norm2": float(n2.item())}))
 
 
@@ -355,6 +365,7 @@ def main():
                     help="run only the forward and back projectors (for profiling)")
     ap.add_argument("--slices", type=int, default=NY, help="slices for --kernels-only")
     ap.add_argument("--launches", type=int, default=3, help="launches for --kernels-only")
+    ap.add_argument("--tune", action="store_true", help="--kernels-only: autotune first")
     ap.add_argument("--angles", type=int, default=NA, help="angles for --kernels-only")
     ap.add_argument("--plain", action="store_true", help="plain CGLS only (no warm start)")
     ap.add_argument("--config", type=int, default=0, choices=[0, 1, 3, 5],
@@ -398,7 +409,8 @@ def main():
     lam = ws.sirt_lambda(plan)
     # launch shapes from the library's autotuner (scratch buffers, before any timing)
     q_tmp = torch.zeros(plan.nangles, plan.nx, plan.ys, dtype=torch.float32, device="cuda")
-    tuned = plan.autotune(x, q_tmp, stream=stream)
+    plan.autotune(x, q_tmp, stream=stream)
+    tuned = plan.shapes()
     del q_tmp
     x.zero_()
 
@@ -565,7 +577,8 @@ def main():
     if rank == 0:
         cfg = dict(CONFIG, iterations=n_it, rel_final=rel_final,
                    parallelism="replicas" if world > 1 else "single",
-                   autotuned={"fp_band_lines": tuned[0], "bp_slice_chunks": tuned[1]})
+                   autotuned={"fp_band_lines": tuned[0], "bp_vec": tuned[1],
+                              "bp_slice_chunks": tuned[2]})
         if net is not None:
             cfg.update(warm_start=True, sirt_iters=sirt_iters,
                        workload="learned warm start: SIRT-%d -> BF16 U-Net -> CGLS to "
