@@ -84,7 +84,7 @@ def lib():
                                                      C.POINTER(C.c_int), C.POINTER(C.c_double), vp]
         L.arecgb_ncc_filtered.argtypes = [vp, vp, C.c_int, C.c_int, C.c_int, vp, vp]
         L.arecgb_take_log.argtypes = [vp, C.c_size_t, vp]
-        L.arecgb_plan_shapes.argtypes = [vp, ip, ip, ip]
+        L.arecgb_plan_shapes.argtypes = [vp, ip, ip, ip, ip]
         L.arecgb_profile_shifts.argtypes = [vp, C.c_int, C.c_int, C.c_int, C.c_int, dp, dp, vp]
         L.arecgb_periodic_decomposition.argtypes = [vp, C.c_int, C.c_int, C.c_int, vp, vp]
         ip_ = C.POINTER(C.c_int)
@@ -284,11 +284,12 @@ class Plan:
         return band.value, nsc.value
 
     def shapes(self):
-        """(forward band height, back-projection VEC, slice chunks per block)."""
-        band, vec, nsc = C.c_int(), C.c_int(), C.c_int()
-        _check(lib().arecgb_plan_shapes(self._h, C.byref(band), C.byref(vec), C.byref(nsc)),
-               "arecgb_plan_shapes")
-        return band.value, vec.value, nsc.value
+        """(forward band height, forward VEC, back-projection VEC, slice chunks
+        per block)."""
+        band, fvec, vec, nsc = C.c_int(), C.c_int(), C.c_int(), C.c_int()
+        _check(lib().arecgb_plan_shapes(self._h, C.byref(band), C.byref(fvec), C.byref(vec),
+                                        C.byref(nsc)), "arecgb_plan_shapes")
+        return band.value, fvec.value, vec.value, nsc.value
 
     def timing(self, mode):
         """Projector timing (mode 1 start, 2 report, 0 report and stop):

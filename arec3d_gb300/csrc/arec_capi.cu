@@ -202,13 +202,15 @@ int arecgb_plan_autotune(arecgb_plan *plan, float *d_x, float *d_q, int *fp_band
     return rc;
 }
 
-int arecgb_plan_shapes(const arecgb_plan *plan, int *fp_band, int *bp_vec, int *bp_nsc) {
+int arecgb_plan_shapes(const arecgb_plan *plan, int *fp_band, int *fp_vec, int *bp_vec,
+                       int *bp_nsc) {
     if (!plan) {
         set_error("arecgb_plan_shapes: null plan");
         return ARECGB_ERR_ARG;
     }
     const Plan *p = reinterpret_cast<const Plan *>(plan);
     if (fp_band) *fp_band = p->fp_band;
+    if (fp_vec) *fp_vec = p->fp_vec ? p->fp_vec : p->vec;
     if (bp_vec) *bp_vec = p->bp_vec ? p->bp_vec : p->vec;
     if (bp_nsc) *bp_nsc = p->bp_nsc;
     return 0;

@@ -64,6 +64,7 @@ struct Plan {
     int fp_band = 64;             // forward projection: lines per band launch
     int bp_nsc = 0;               // back projection: slice chunks per block (0 = by size)
     int bp_vec = 0;               // back projection: floats per lane (0 = vec)
+    int fp_vec = 0;               // forward projection (SQ, KB): floats per lane (0 = vec)
     int tuned = 0;                // launch shapes chosen by plan_autotune
     int2 *d_tiles = nullptr;      // back-projection ray tiles: (ix0, iz0) of 8x4-pixel tiles
     int ntiles = 0;

@@ -53,7 +53,13 @@ static int slice_blocks(const Plan *p) {
 
 constexpr int kNormBlocks = 1024;
 
-static int fp_slice_blocks(const Plan *p) { return (p->ys + 32 * p->vec - 1) / (32 * p->vec); }
+// Forward projection (banded kernels): floats per lane.
+static int fp_vec(const Plan *p) { return p->fp_vec ? p->fp_vec : p->vec; }
+
+static int fp_slice_blocks(const Plan *p) {
+    const int v = fp_vec(p);
+    return (p->ys + 32 * v - 1) / (32 * v);
+}
 
 // The forward projector's FP64 norm is a separate pass over q (1024 partials).
 int fp_grid_blocks(const Plan *) { return kNormBlocks; }
@@ -143,8 +149,8 @@ int forward_project(const Plan *p, const float *d_x, float *d_q, double *d_norm2
             for (int lo = 0; lo < p->nx && !rc; lo += p->fp_band) {
                 const int hi = std::min(p->nx, lo + p->fp_band);
                 rc = p->weighting == ARECGB_KB
-                         ? launch_fpb_kb(A, p->vec, grid, d_x, d_q, g0, ngo, lo, hi, st)
-                         : launch_fpb_sq(A, p->vec, grid, d_x, d_q, g0, ngo, lo, hi, st);
+                         ? launch_fpb_kb(A, fp_vec(p), grid, d_x, d_q, g0, ngo, lo, hi, st)
+                         : launch_fpb_sq(A, fp_vec(p), grid, d_x, d_q, g0, ngo, lo, hi, st);
                 count_launches(1);
             }
         }
@@ -212,20 +218,28 @@ int plan_autotune(Plan *p, float *d_x, float *d_q, cudaStream_t st) {
     int rc = 0;
     const bool was_timing = p->timing;
     p->timing = false;
-    int best_band = p->fp_band;
+    // forward projection: band height x floats per lane (the plan's or half)
+    int best_band = p->fp_band, best_fvec = 0;
     float best = 1e30f;
-    for (int band : {32, 64, 128}) {
-        if (band > 2 * p->nx && band != 32) continue;
-        p->fp_band = band;
-        float ms;
-        if ((rc = best_of([&] { return forward_project(p, d_x, d_q, nullptr, nullptr, st); }, &ms)))
-            break;
-        if (ms < best) {
-            best = ms;
-            best_band = band;
+    for (int fv : {p->vec, p->vec / 2}) {
+        if (fv < 1 || rc) continue;
+        p->fp_vec = fv;
+        for (int band : {32, 64, 128}) {
+            if (band > 2 * p->nx && band != 32) continue;
+            p->fp_band = band;
+            float ms;
+            if ((rc = best_of([&] { return forward_project(p, d_x, d_q, nullptr, nullptr, st); },
+                              &ms)))
+                break;
+            if (ms < best) {
+                best = ms;
+                best_band = band;
+                best_fvec = fv;
+            }
         }
     }
     p->fp_band = best_band;
+    p->fp_vec = best_fvec;
     // back projection: (floats per lane, slice chunks per block) in
     // {(vec, 1), (vec, 2), (vec / 2, 1)}: half the vector width halves the
     // accumulators and the staged rows (more blocks per SM)

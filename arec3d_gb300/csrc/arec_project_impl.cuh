@@ -774,33 +774,26 @@ __global__ void __launch_bounds__(kFpThreads, 3)
         }
         __syncwarp();
         // Phase C: entries in bucket order; the bucket index is a compile-time
-        // constant.  The next entry's slices are loaded before this entry's FMAs.
+        // constant.  Each entry's slices are loaded as it is reached (the
+        // other warps cover the load latency; a prefetch into a second
+        // register set cost more in register moves than it saved).
         if (cnt) {
             const float *S = stg + (size_t)buf * US * SPAN;
             const float4 *E = list + ai * 32;
-            float4 e = E[0];
-            float v[VEC];
-            lds_lane<VEC>(S + (__float_as_int(e.x) & 255) * SPAN, lane, v);
             int i = 0;
+            float4 e = E[0];
 #pragma unroll
             for (int gg = 0; gg < NG; gg++) {
                 while (i < cnt && (__float_as_int(e.x) >> 8) == gg) {
-                    float4 en = e;
-                    float vn[VEC];
-#pragma unroll
-                    for (int c = 0; c < VEC; c++) vn[c] = 0.f;
-                    if (i + 1 < cnt) {
-                        en = E[i + 1];
-                        lds_lane<VEC>(S + (__float_as_int(en.x) & 255) * SPAN, lane, vn);
-                    }
-                    if (gg >= 2) fma_row<VEC>(acc[gg >= 2 ? gg - 2 : 0], e.y, v);
-                    if (gg >= 1 && gg <= BT)
-                        fma_row<VEC>(acc[(gg >= 1 && gg <= BT) ? gg - 1 : 0], e.z, v);
-                    if (gg <= BT - 1) fma_row<VEC>(acc[gg <= BT - 1 ? gg : 0], e.w, v);
-                    e = en;
-#pragma unroll
-                    for (int c = 0; c < VEC; c++) v[c] = vn[c];
+                    float v[VEC];
+                    lds_lane<VEC>(S + (__float_as_int(e.x) & 255) * SPAN, lane, v);
+                    const float4 ec = e;
                     i++;
+                    if (i < cnt) e = E[i];
+                    if (gg >= 2) fma_row<VEC>(acc[gg >= 2 ? gg - 2 : 0], ec.y, v);
+                    if (gg >= 1 && gg <= BT)
+                        fma_row<VEC>(acc[(gg >= 1 && gg <= BT) ? gg - 1 : 0], ec.z, v);
+                    if (gg <= BT - 1) fma_row<VEC>(acc[gg <= BT - 1 ? gg : 0], ec.w, v);
                 }
             }
         }

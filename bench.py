@@ -577,8 +577,8 @@ def main():
     if rank == 0:
         cfg = dict(CONFIG, iterations=n_it, rel_final=rel_final,
                    parallelism="replicas" if world > 1 else "single",
-                   autotuned={"fp_band_lines": tuned[0], "bp_vec": tuned[1],
-                              "bp_slice_chunks": tuned[2]})
+                   autotuned={"fp_band_lines": tuned[0], "fp_vec": tuned[1], "bp_vec": tuned[2],
+                              "bp_slice_chunks": tuned[3]})
         if net is not None:
             cfg.update(warm_start=True, sirt_iters=sirt_iters,
                        workload="learned warm start: SIRT-%d -> BF16 U-Net -> CGLS to "

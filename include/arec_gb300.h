@@ -124,20 +124,21 @@ int arecgb_plan_timing(arecgb_plan *plan, int mode, double *fp_ms, long long *fp
                        double *bp_ms, long long *bp_calls);
 
 /* Autotuner: times the projectors of this plan for the forward projector's
- * band height (32, 64, 128 lines) and the back projector's shape (VEC floats
- * per lane and one or two chunks of 32*VEC slices per block, VEC the plan's
- * or half of it) on the caller's buffers d_x (a volume) and d_q (a sinogram),
+ * band height (32, 64, 128 lines) and floats per lane (the plan's VEC or half
+ * of it) and the back projector's shape (VEC or VEC/2 floats per lane, one or
+ * two chunks of 32*VEC slices per block) on the caller's buffers d_x (a volume) and d_q (a sinogram),
  * which it overwrites, and keeps the fastest; reports the band and the chunks
- * (either pointer may be NULL; arecgb_plan_shapes reports all three).  Results
+ * (either pointer may be NULL; arecgb_plan_shapes reports all four).  Results
  * do not depend on the choice beyond float summation order across bands.  No
  * counterpart in the reference. */
 int arecgb_plan_autotune(arecgb_plan *plan, float *d_x, float *d_q, int *fp_band, int *bp_nsc,
                          void *stream);
 
-/* Launch shapes in use: forward band height, back-projection floats per lane
- * and slice chunks per block (0: chosen by size).  No counterpart in the
- * reference. */
-int arecgb_plan_shapes(const arecgb_plan *plan, int *fp_band, int *bp_vec, int *bp_nsc);
+/* Launch shapes in use: forward band height and floats per lane,
+ * back-projection floats per lane and slice chunks per block (0: chosen by
+ * size).  No counterpart in the reference. */
+int arecgb_plan_shapes(const arecgb_plan *plan, int *fp_band, int *fp_vec, int *bp_vec,
+                       int *bp_nsc);
 
 /* Kernel launches issued by this library so far (all threads, approximate
  * only in that concurrent callers interleave). */
