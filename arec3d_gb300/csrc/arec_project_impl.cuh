@@ -310,7 +310,7 @@ __global__ void __launch_bounds__(128 * NSC + 32)
             // by at most one bin between neighbouring pixels), and rotate the
             // weights to the slots.  code: bits 0-1 action (0 skip, 1 same
             // bins, 2 one row enters slot bits 2-3, 3 three rows), bits 4-6
-            // bins on the detector, bits 8+ footprint row.
+            // bins on the detector, bits 8+ footprint row offset (rows x SPAN).
             const bool use = b != INT_MIN / 2 && b - lo <= FW - 3;
             const int gbase = lane & ~7;
             int cb = INT_MIN / 4, m = 0, my_code = 0, my_m = 0;
@@ -325,15 +325,15 @@ __global__ void __launch_bounds__(128 * NSC + 32)
                         code = 1;
                     } else if (d == 1) {  // bin cb (slot m) leaves, bin br + 2 enters
                         code = 2 | (m << 2) | ((unsigned)(br + 2) < (unsigned)A.nx ? 16 : 0) |
-                               ((rr + 2) << 8);
+                               (((rr + 2) * SPAN) << 8);
                         m = m == 2 ? 0 : m + 1;
                     } else if (d == -1) {  // bin cb + 2 leaves, bin br enters
                         m = m == 0 ? 2 : m - 1;
-                        code = 2 | (m << 2) | ((unsigned)br < (unsigned)A.nx ? 16 : 0) | (rr << 8);
+                        code = 2 | (m << 2) | ((unsigned)br < (unsigned)A.nx ? 16 : 0) | ((rr * SPAN) << 8);
                     } else {
                         code = 3 | ((unsigned)br < (unsigned)A.nx ? 16 : 0) |
                                ((unsigned)(br + 1) < (unsigned)A.nx ? 32 : 0) |
-                               ((unsigned)(br + 2) < (unsigned)A.nx ? 64 : 0) | (rr << 8);
+                               ((unsigned)(br + 2) < (unsigned)A.nx ? 64 : 0) | ((rr * SPAN) << 8);
                         m = 0;
                     }
                     cb = br;
@@ -364,8 +364,22 @@ __global__ void __launch_bounds__(128 * NSC + 32)
                     if (lane == 0) atomicOr(A.err, 16);
                 }
                 const int bin = fb[ai] + lane;
-                const bool on = ok && lane < fn[ai] && (unsigned)bin < (unsigned)A.nx;
+                const bool in = ok && lane < fn[ai];
+                const bool on = in && (unsigned)bin < (unsigned)A.nx;
                 const unsigned m = __ballot_sync(0xffffffffu, on);
+                // bins of the footprint off the detector (the cylinder's edge):
+                // zero rows, so the accumulating warps load every row they plan
+                unsigned off = __ballot_sync(0xffffffffu, in && !on);
+                if (off) {
+                    for (; off; off &= off - 1) {
+                        float4 *z = reinterpret_cast<float4 *>(
+                            foot + ((size_t)buf * FW + (__ffs(off) - 1)) * SPAN);
+                        for (int c = lane; c < SPAN / 4; c += 32) z[c] = make_float4(0.f, 0.f, 0.f, 0.f);
+                    }
+                    // order these generic stores before later bulk copies into the rows
+                    asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
+                }
+                __syncwarp();  // zero rows written before the arrival (release)
                 if (lane == 0) umma::mbar_arrive_expect_tx(&full[buf], (uint32_t)__popc(m) * row_bytes);
                 __syncwarp();
                 if (on)
@@ -382,28 +396,26 @@ __global__ void __launch_bounds__(128 * NSC + 32)
                 }
                 if (ok && yok) {
                     const float *F = foot + (size_t)buf * FW * SPAN + yw;
-                    float R0[VEC], R1[VEC], R2[VEC];  // the ring (slots 0, 1, 2)
-#pragma unroll
-                    for (int q = 0; q < VEC; q++) R0[q] = R1[q] = R2[q] = 0.f;
+                    // the ring (slots 0, 1, 2); a warp's first used ray loads all three
+                    float R0[VEC], R1[VEC], R2[VEC];
 #pragma unroll
                     for (int r = 0; r < 8; r++) {
                         const float4 e = sw[ai * 32 + rg * 8 + r];
                         const int code = __float_as_int(e.x), act = code & 3;
                         if (act == 0) continue;
-                        const float *row = F + (code >> 8) * SPAN;
+                        const float *row = F + (code >> 8);  // row offset in floats
                         if (act == 2) {
                             const int slot = (code >> 2) & 3;
-                            const bool on = code & 16;
                             if (slot == 0)
-                                foot_row<VEC>(row, on, lane, R0);
+                                lds_lane<VEC>(row, lane, R0);
                             else if (slot == 1)
-                                foot_row<VEC>(row, on, lane, R1);
+                                lds_lane<VEC>(row, lane, R1);
                             else
-                                foot_row<VEC>(row, on, lane, R2);
+                                lds_lane<VEC>(row, lane, R2);
                         } else if (act == 3) {
-                            foot_row<VEC>(row, code & 16, lane, R0);
-                            foot_row<VEC>(row + SPAN, code & 32, lane, R1);
-                            foot_row<VEC>(row + 2 * SPAN, code & 64, lane, R2);
+                            lds_lane<VEC>(row, lane, R0);
+                            lds_lane<VEC>(row + SPAN, lane, R1);
+                            lds_lane<VEC>(row + 2 * SPAN, lane, R2);
                         }
                         fma_row<VEC>(acc[r], e.y, R0);
                         fma_row<VEC>(acc[r], e.z, R1);
