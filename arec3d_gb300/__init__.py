@@ -85,6 +85,8 @@ def lib():
         L.arecgb_ncc_filtered.argtypes = [vp, vp, C.c_int, C.c_int, C.c_int, vp, vp]
         L.arecgb_take_log.argtypes = [vp, C.c_size_t, vp]
         L.arecgb_plan_shapes.argtypes = [vp, ip, ip, ip, ip]
+        L.arecgb_plan_table_bytes.argtypes = [vp]
+        L.arecgb_plan_table_bytes.restype = C.c_longlong
         L.arecgb_profile_shifts.argtypes = [vp, C.c_int, C.c_int, C.c_int, C.c_int, dp, dp, vp]
         L.arecgb_periodic_decomposition.argtypes = [vp, C.c_int, C.c_int, C.c_int, vp, vp]
         ip_ = C.POINTER(C.c_int)
@@ -282,6 +284,10 @@ class Plan:
         _check(lib().arecgb_plan_autotune(self._h, _ptr(x), _ptr(q), C.byref(band), C.byref(nsc),
                                           _stream(stream)), "arecgb_plan_autotune")
         return band.value, nsc.value
+
+    def table_bytes(self):
+        """Device bytes of the plan's projector tables (0: none)."""
+        return lib().arecgb_plan_table_bytes(self._h)
 
     def shapes(self):
         """(forward band height, forward VEC, back-projection VEC, slice chunks

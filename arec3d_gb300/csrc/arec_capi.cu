@@ -202,6 +202,10 @@ int arecgb_plan_autotune(arecgb_plan *plan, float *d_x, float *d_q, int *fp_band
     return rc;
 }
 
+long long arecgb_plan_table_bytes(const arecgb_plan *plan) {
+    return plan ? (long long)reinterpret_cast<const Plan *>(plan)->table_bytes : 0;
+}
+
 int arecgb_plan_shapes(const arecgb_plan *plan, int *fp_band, int *fp_vec, int *bp_vec,
                        int *bp_nsc) {
     if (!plan) {

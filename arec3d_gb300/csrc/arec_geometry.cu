@@ -242,6 +242,10 @@ int plan_create(Plan **out, int weighting, double radius, int ny, int nangles,
         plan_destroy(p);
         return cuda_status(e);
     }
+    if (int rc = plan_build_tables(p)) {
+        plan_destroy(p);
+        return rc;
+    }
     *out = p;
     return ARECGB_OK;
 }
@@ -261,6 +265,9 @@ void plan_destroy(Plan *p) {
     cudaFree(p->d_w);
     cudaFree(p->d_groups);
     cudaFree(p->d_tiles);
+    cudaFree(p->d_taps);
+    cudaFree(p->d_bpw);
+    cudaFree(p->d_bpf);
     cudaFree(p->d_err);
     cudaFree(p->d_partials);
     for (auto &v : p->d_vol) cudaFree(v);

@@ -65,6 +65,15 @@ struct Plan {
     int bp_nsc = 0;               // back projection: slice chunks per block (0 = by size)
     int bp_vec = 0;               // back projection: floats per lane (0 = vec)
     int fp_vec = 0;               // forward projection (SQ, KB): floats per lane (0 = vec)
+
+    // Optional tables (SQ, KB; built at creation when device memory allows,
+    // see plan_build_tables): the taps of every (ray, angle) for the forward
+    // projector and the back projector's per-(tile, angle) ring plans.  The
+    // kernels compute the same values without them.
+    float4 *d_taps = nullptr;     // [ngroups][nrays][4]
+    float4 *d_bpw = nullptr;      // [ntiles][na][32]
+    int2 *d_bpf = nullptr;        // [ntiles][na]
+    size_t table_bytes = 0;
     int tuned = 0;                // launch shapes chosen by plan_autotune
     int2 *d_tiles = nullptr;      // back-projection ray tiles: (ix0, iz0) of 8x4-pixel tiles
     int ntiles = 0;
@@ -121,6 +130,7 @@ int fp_grid_blocks(const Plan *p);
 int plan_timing(const Plan *p, int mode, double *fp_ms, long long *fp_calls, double *bp_ms,
                 long long *bp_calls);
 int plan_autotune(Plan *p, float *d_x, float *d_q, cudaStream_t st);
+int plan_build_tables(Plan *p);
 int bp_grid_blocks(const Plan *p);
 
 // Layout kernels and vector ops (arec_vector.cu)

@@ -1,5 +1,6 @@
 // Projector dispatch: launch shapes, weighting selection and the FP64 norm.
 #include <algorithm>
+#include <cstdlib>
 
 #include "arec_project_impl.cuh"
 
@@ -9,6 +10,8 @@ int launch_bp_lin(const OpArgs &, int, int, dim3, const float *, float *, cudaSt
 int launch_bp_kb(const OpArgs &, int, int, dim3, const float *, float *, cudaStream_t);
 int launch_bp_sq(const OpArgs &, int, int, dim3, const float *, float *, cudaStream_t);
 int launch_fp_lin(const OpArgs &, int, const float *, float *, cudaStream_t);
+int launch_tables_sq(const OpArgs &, int, float4 *, float4 *, int2 *, cudaStream_t);
+int launch_tables_kb(const OpArgs &, int, float4 *, float4 *, int2 *, cudaStream_t);
 int launch_fpb_kb(const OpArgs &, int, dim3, const float *, float *, int, int, int, int,
                   cudaStream_t);
 int launch_fpb_sq(const OpArgs &, int, dim3, const float *, float *, int, int, int, int,
@@ -33,6 +36,9 @@ static OpArgs make_args(const Plan *p, const int *skip) {
     A.partials = p->d_partials;
     A.skip = skip;
     A.err = p->d_err;
+    A.taps = p->d_taps;
+    A.bpw = p->d_bpw;
+    A.bpf = p->d_bpf;
     return A;
 }
 
@@ -189,6 +195,51 @@ int back_project(const Plan *p, const float *d_s, float *d_g, double *d_norm2,
         if (rc) return rc;
     }
     return timing_mark(p, false, true, st);
+}
+
+// Tables for the SQ and KB projectors: the taps of every (angle group, ray)
+// (ngroups x nrays x 4 x 16 B: 15.8 GB at 1024^2 x 1200 angles) and the back
+// projector's ring plans (ntiles x na x 520 B: 16.3 GB).  Built when they take
+// at most 40 % of the free device memory and ARECGB_PLAN_TABLES is not "0";
+// otherwise the kernels compute the same values as they go.  The tables hold
+// exactly what the kernels would compute (the same device functions), so
+// results do not depend on them.
+int plan_build_tables(Plan *p) {
+    if (p->weighting == ARECGB_LIN) return 0;
+    const char *env = getenv("ARECGB_PLAN_TABLES");
+    if (env && env[0] == '0') return 0;
+    const size_t b_taps = sizeof(float4) * (size_t)p->ngroups * p->nrays * 4;
+    const size_t b_bpw = sizeof(float4) * (size_t)p->ntiles * p->na * 32;
+    const size_t b_bpf = sizeof(int2) * (size_t)p->ntiles * p->na;
+    size_t free_b = 0, total_b = 0;
+    if (cudaMemGetInfo(&free_b, &total_b) != cudaSuccess) return 0;
+    if ((double)(b_taps + b_bpw + b_bpf) > 0.4 * (double)free_b) return 0;
+    if (cudaMalloc(&p->d_taps, b_taps) != cudaSuccess || cudaMalloc(&p->d_bpw, b_bpw) != cudaSuccess ||
+        cudaMalloc(&p->d_bpf, b_bpf) != cudaSuccess) {
+        cudaGetLastError();  // an allocation failure is not sticky; run without tables
+        cudaFree(p->d_taps);
+        cudaFree(p->d_bpw);
+        cudaFree(p->d_bpf);
+        p->d_taps = nullptr;
+        p->d_bpw = nullptr;
+        p->d_bpf = nullptr;
+        return 0;
+    }
+    OpArgs A = make_args(p, nullptr);
+    const int rc = p->weighting == ARECGB_KB
+                       ? launch_tables_kb(A, p->ntiles, p->d_taps, p->d_bpw, p->d_bpf, p->stream)
+                       : launch_tables_sq(A, p->ntiles, p->d_taps, p->d_bpw, p->d_bpf, p->stream);
+    count_launches(2);
+    ARECGB_CUDA(cudaGetLastError());
+    ARECGB_CUDA(cudaStreamSynchronize(p->stream));
+    int err = 0;
+    ARECGB_CUDA(cudaMemcpy(&err, p->d_err, sizeof(int), cudaMemcpyDeviceToHost));
+    if (rc || err) {
+        set_error("plan_build_tables: a tile's footprint exceeds the staged width");
+        return ARECGB_ERR_ARG;
+    }
+    p->table_bytes = b_taps + b_bpw + b_bpf;
+    return 0;
 }
 
 // Autotuner: times the forward projector for band heights of 32, 64 and 128

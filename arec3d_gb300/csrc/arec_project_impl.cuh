@@ -48,6 +48,11 @@ struct OpArgs {
     double *partials;
     const int *skip;
     int *err;
+    // optional per-plan tables (null when the plan has none)
+    const float4 *taps;  // [ngroups][nrays][4]: ray_taps of each forward-projection angle
+                         // group's (up to 4) angles per ray: (iqx, w0, w1, w2)
+    const float4 *bpw;   // [ntiles][na][32]: the back projector's plan entries
+    const int2 *bpf;     // [ntiles][na]: footprint (first bin, bins) per tile and angle
 };
 
 template <int VEC>
@@ -226,6 +231,117 @@ constexpr int kBpFoot = 16;    // staged footprint width in bins (an 8x4 tile sp
 
 constexpr int kBpBuf = 3;  // footprint buffers in flight
 
+// The back projector's plan for one angle of one 8x4-pixel tile; lanes = the
+// tile's 32 rays (lane = 8 * row + pixel; has: the lane's pixel is a ray of
+// the cylinder).  The accumulating warp of each row of 8 rays keeps the three
+// bins b .. b+2 of its current ray in a register ring; the plan says, per
+// ray, which ring slot takes which footprint row (the centre bin moves by at
+// most one bin between neighbouring pixels) and rotates the weights to the
+// slots.  Entry (code, wa, wb, wc): code bits 0-1 action (0 skip, 1 same
+// bins, 2 one row enters slot bits 2-3, 3 three rows), bits 8+ footprint row
+// of the (first) row entering; wa, wb, wc the weights of slots 0, 1, 2.
+// Also the tile's footprint: first bin fb and bins spanned fn (<= FW; wide:
+// the taps reach further, an impossible case reported by the caller).
+template <int W, int FW>
+__device__ __forceinline__ float4 bp_plan(const OpArgs &A, const float4 &myray, bool has,
+                                          const AngleParams &ap, int lane, int &fb, int &fn,
+                                          bool &wide) {
+    Taps t{};
+    int b = INT_MIN / 2, lo = INT_MAX, hi = INT_MIN;
+    if (has) {
+        t = ray_taps<W>(myray, ap, A.r_hi, A.r_lo);
+        b = lo = hi = t.iqx - 1;
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+        lo = min(lo, __shfl_xor_sync(0xffffffffu, lo, o));
+        hi = max(hi, __shfl_xor_sync(0xffffffffu, hi, o));
+    }
+    const bool use = b != INT_MIN / 2 && b - lo <= FW - 3;
+    const int gbase = lane & ~7;
+    int cb = INT_MIN / 4, m = 0, my_code = 0, my_m = 0;
+#pragma unroll
+    for (int r = 0; r < 8; r++) {
+        const int br = __shfl_sync(0xffffffffu, b, gbase + r);
+        const int ur = __shfl_sync(0xffffffffu, (int)use, gbase + r);
+        int code = 0;
+        if (ur) {
+            const int d = br - cb, rr = br - lo;
+            if (d == 0) {
+                code = 1;
+            } else if (d == 1) {  // bin cb (slot m) leaves, bin br + 2 enters
+                code = 2 | (m << 2) | ((rr + 2) << 8);
+                m = m == 2 ? 0 : m + 1;
+            } else if (d == -1) {  // bin cb + 2 leaves, bin br enters
+                m = m == 0 ? 2 : m - 1;
+                code = 2 | (m << 2) | (rr << 8);
+            } else {
+                code = 3 | (rr << 8);
+                m = 0;
+            }
+            cb = br;
+        }
+        if ((lane & 7) == r) {
+            my_code = code;
+            my_m = m;
+        }
+    }
+    wide = hi - lo + 3 > FW && lo != INT_MAX;
+    fb = lo == INT_MAX ? 0 : lo;
+    fn = lo == INT_MAX ? 0 : min(FW, hi - lo + 3);
+    // slot s holds bin b + ((s - m) mod 3): its weight is w_{(s - m) mod 3}
+    const float wa = my_m == 0 ? t.w0 : (my_m == 1 ? t.w2 : t.w1);
+    const float wb = my_m == 0 ? t.w1 : (my_m == 1 ? t.w0 : t.w2);
+    const float wc = my_m == 0 ? t.w2 : (my_m == 1 ? t.w1 : t.w0);
+    return make_float4(__int_as_float(my_code), wa, wb, wc);
+}
+
+__device__ __forceinline__ int tile_lane_ray(const OpArgs &A, int2 tile, int lane) {
+    const int ix = tile.x + (lane & (kTileX - 1)), iz = tile.y + lane / kTileX;
+    int k = -1;
+    if (iz < A.nx) {
+        const RowInfo ri = A.rows[iz];
+        if (ix >= ri.lo && ix <= ri.hi) k = ri.start + ix - ri.lo;
+    }
+    return k;
+}
+
+// Plan tables: the back projector's entries for every (tile, angle) (one warp
+// each) and the taps of every (angle group, ray, angle of the group); a
+// group's 4 slots of one ray are one 64-byte copy for the forward projector's
+// staging warp, and the rays of a line are contiguous.
+static_assert(kGroupAngles == 4, "the taps table holds 4 angles per group");
+template <int W, int FW>
+__global__ void __launch_bounds__(128) k_bp_table(OpArgs A, float4 *bpw, int2 *bpf) {
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int tile = blockIdx.x, a = blockIdx.y * 4 + warp;
+    if (a >= A.na) return;  // whole warp
+    const int k = tile_lane_ray(A, A.tiles[tile], lane);
+    const float4 myray = k >= 0 ? A.ray[k] : make_float4(0.f, 0.f, 0.f, 0.f);
+    int f0, f1;
+    bool wide;
+    bpw[((size_t)tile * A.na + a) * 32 + lane] = bp_plan<W, FW>(A, myray, k >= 0, A.ang[a], lane, f0, f1, wide);
+    if (lane == 0) {
+        bpf[(size_t)tile * A.na + a] = make_int2(f0, f1);
+        if (wide) atomicOr(A.err, 2);
+    }
+}
+
+template <int W>
+__global__ void __launch_bounds__(256) k_fp_taps(OpArgs A, float4 *taps) {
+    const size_t t = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= (size_t)A.ngroups * A.nrays * 4) return;
+    const int j = (int)(t & 3);
+    const size_t gk = t >> 2;
+    const int grp = (int)(gk / A.nrays), k = (int)(gk % A.nrays);
+    const int4 G = A.groups[grp];
+    float4 e = make_float4(0.f, 0.f, 0.f, 0.f);
+    if (j < G.y) {
+        const Taps tp = ray_taps<W>(A.ray[k], A.ang[G.x + j], A.r_hi, A.r_lo);
+        e = make_float4(__int_as_float(tp.iqx), tp.w0, tp.w1, tp.w2);
+    }
+    taps[t] = e;
+}
+
 template <int VEC, int NSC>
 constexpr size_t bp_smem_bytes() {
     return sizeof(float) * kBpBuf * kBpFoot * (NSC * 32 * VEC) + sizeof(float4) * kBpAngles * 32 +
@@ -259,14 +375,8 @@ __global__ void __launch_bounds__(128 * NSC + 32)
     if (A.skip && *A.skip) return;
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const bool stager = warp == NCW;
-    const int2 tile = A.tiles[blockIdx.x];
-    const int ix = tile.x + (lane & (kTileX - 1)), iz = tile.y + lane / kTileX;
-    int k = -1;
-    if (iz < A.nx) {
-        RowInfo ri = A.rows[iz];
-        if (ix >= ri.lo && ix <= ri.hi) k = ri.start + ix - ri.lo;
-    }
-    const float4 myray = k >= 0 ? A.ray[k] : make_float4(0.f, 0.f, 0.f, 0.f);
+    const int k = tile_lane_ray(A, A.tiles[blockIdx.x], lane);
+    const float4 myray = k >= 0 && !A.bpw ? A.ray[k] : make_float4(0.f, 0.f, 0.f, 0.f);
     const int rg = warp & 3, sc = warp >> 2;
     const int yb = blockIdx.y * SPAN;                  // first slice of the block
     const int yw = sc * 32 * VEC;                        // this warp's slices within the block
@@ -292,66 +402,30 @@ __global__ void __launch_bounds__(128 * NSC + 32)
     int t0 = 0;  // angles staged before this chunk (buffer t % NB, use t / NB)
     for (int a0 = 0; a0 < A.na; a0 += AC) {
         const int nac = min(AC, A.na - a0);
-        for (int ai = warp; ai < AC; ai += NCW + 1) {
-            const int a = a0 + ai;
-            Taps t{};
-            int b = INT_MIN / 2, lo = INT_MAX, hi = INT_MIN;
-            if (a < A.na && k >= 0) {
-                t = ray_taps<W>(myray, A.ang[a], A.r_hi, A.r_lo);
-                b = lo = hi = t.iqx - 1;
+        if (A.bpw) {
+            // the plan's precomputed entries for this tile and chunk
+            const float4 *src = A.bpw + ((size_t)blockIdx.x * A.na + a0) * 32;
+            for (int i = threadIdx.x; i < nac * 32; i += blockDim.x) cp_async16(sw + i, src + i, true);
+            cp_async_commit();
+            for (int i = threadIdx.x; i < nac; i += blockDim.x) {
+                const int2 f = A.bpf[(size_t)blockIdx.x * A.na + a0 + i];
+                fb[i] = f.x;
+                fn[i] = f.y;
             }
-            for (int o = 16; o > 0; o >>= 1) {
-                lo = min(lo, __shfl_xor_sync(0xffffffffu, lo, o));
-                hi = max(hi, __shfl_xor_sync(0xffffffffu, hi, o));
-            }
-            // The accumulating warp of each row of 8 rays keeps the three bins
-            // b .. b+2 of its current ray in a register ring; plan, per ray,
-            // which ring slot takes which footprint row (the centre bin moves
-            // by at most one bin between neighbouring pixels), and rotate the
-            // weights to the slots.  code: bits 0-1 action (0 skip, 1 same
-            // bins, 2 one row enters slot bits 2-3, 3 three rows), bits 4-6
-            // bins on the detector, bits 8+ footprint row offset (rows x SPAN).
-            const bool use = b != INT_MIN / 2 && b - lo <= FW - 3;
-            const int gbase = lane & ~7;
-            int cb = INT_MIN / 4, m = 0, my_code = 0, my_m = 0;
-#pragma unroll
-            for (int r = 0; r < 8; r++) {
-                const int br = __shfl_sync(0xffffffffu, b, gbase + r);
-                const int ur = __shfl_sync(0xffffffffu, (int)use, gbase + r);
-                int code = 0;
-                if (ur) {
-                    const int d = br - cb, rr = br - lo;
-                    if (d == 0) {
-                        code = 1;
-                    } else if (d == 1) {  // bin cb (slot m) leaves, bin br + 2 enters
-                        code = 2 | (m << 2) | ((unsigned)(br + 2) < (unsigned)A.nx ? 16 : 0) |
-                               (((rr + 2) * SPAN) << 8);
-                        m = m == 2 ? 0 : m + 1;
-                    } else if (d == -1) {  // bin cb + 2 leaves, bin br enters
-                        m = m == 0 ? 2 : m - 1;
-                        code = 2 | (m << 2) | ((unsigned)br < (unsigned)A.nx ? 16 : 0) | ((rr * SPAN) << 8);
-                    } else {
-                        code = 3 | ((unsigned)br < (unsigned)A.nx ? 16 : 0) |
-                               ((unsigned)(br + 1) < (unsigned)A.nx ? 32 : 0) |
-                               ((unsigned)(br + 2) < (unsigned)A.nx ? 64 : 0) | ((rr * SPAN) << 8);
-                        m = 0;
-                    }
-                    cb = br;
+            cp_async_wait<0>();
+        } else {
+            for (int ai = warp; ai < AC; ai += NCW + 1) {
+                const int a = a0 + ai;
+                int f0, f1;
+                bool wide;
+                sw[ai * 32 + lane] =
+                    bp_plan<W, FW>(A, myray, a < A.na && k >= 0, A.ang[min(a, A.na - 1)], lane,
+                                   f0, f1, wide);
+                if (lane == 0) {
+                    if (wide) atomicOr(A.err, 2);
+                    fb[ai] = f0;
+                    fn[ai] = f1;
                 }
-                if ((lane & 7) == r) {
-                    my_code = code;
-                    my_m = m;
-                }
-            }
-            // slot s holds bin b + ((s - m) mod 3): its weight is w_{(s - m) mod 3}
-            const float wa = my_m == 0 ? t.w0 : (my_m == 1 ? t.w2 : t.w1);
-            const float wb = my_m == 0 ? t.w1 : (my_m == 1 ? t.w0 : t.w2);
-            const float wc = my_m == 0 ? t.w2 : (my_m == 1 ? t.w1 : t.w0);
-            sw[ai * 32 + lane] = make_float4(__int_as_float(my_code), wa, wb, wc);
-            if (lane == 0) {
-                if (hi - lo + 3 > FW && lo != INT_MAX) atomicOr(A.err, 2);
-                fb[ai] = lo == INT_MAX ? 0 : lo;
-                fn[ai] = lo == INT_MAX ? 0 : min(FW, hi - lo + 3);
             }
         }
         __syncthreads();  // weights and footprint bases of this chunk (barriers initialised)
@@ -403,7 +477,7 @@ __global__ void __launch_bounds__(128 * NSC + 32)
                         const float4 e = sw[ai * 32 + rg * 8 + r];
                         const int code = __float_as_int(e.x), act = code & 3;
                         if (act == 0) continue;
-                        const float *row = F + (code >> 8);  // row offset in floats
+                        const float *row = F + (code >> 8) * SPAN;
                         if (act == 2) {
                             const int slot = (code >> 2) & 3;
                             if (slot == 0)
@@ -461,14 +535,8 @@ __global__ void __launch_bounds__(128 * NSC)
     __shared__ double red[NWARP];
     if (A.skip && *A.skip) return;
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const int2 tile = A.tiles[blockIdx.x];
-    const int ix = tile.x + (lane & (kTileX - 1)), iz = tile.y + lane / kTileX;
-    int k = -1;
-    if (iz < A.nx) {
-        RowInfo ri = A.rows[iz];
-        if (ix >= ri.lo && ix <= ri.hi) k = ri.start + ix - ri.lo;
-    }
-    const float4 myray = k >= 0 ? A.ray[k] : make_float4(0.f, 0.f, 0.f, 0.f);
+    const int k = tile_lane_ray(A, A.tiles[blockIdx.x], lane);
+    const float4 myray = k >= 0 && !A.bpw ? A.ray[k] : make_float4(0.f, 0.f, 0.f, 0.f);
     const int rg = warp & 3, sc = warp >> 2;
     const int y0 = (blockIdx.y * NSC + sc) * 32 * VEC + lane * VEC;
     const bool yok = y0 < A.ys;
@@ -615,7 +683,7 @@ __device__ __forceinline__ int line_pixel_ray(const OpArgs &A, int orient, int l
 template <int VEC>
 constexpr size_t fpb_smem_bytes() {
     return sizeof(float) * 2 * kFpStage * (32 * VEC) + sizeof(float4) * kGroupAngles * 32 +
-           sizeof(float4) * 2 * kFpStage + sizeof(int) * (2 * kGroupAngles + 4);
+           sizeof(float4) * 2 * kFpStage * kGroupAngles + sizeof(int) * (2 * kGroupAngles + 4);
 }
 
 constexpr int kFpThreads = 32 * (kGroupAngles + 1);
@@ -629,8 +697,10 @@ __global__ void __launch_bounds__(kFpThreads, 3)
     __shared__ __align__(8) uint64_t full[2], empty[2];
     float *stg = reinterpret_cast<float *>(smem_raw);                // [2][US][SPAN]
     float4 *list = reinterpret_cast<float4 *>(stg + 2 * US * SPAN);  // [NA][32]
-    float4 *rayb = list + NA * 32;                                   // [2][US] ray of each row
-    int *lrange = reinterpret_cast<int *>(rayb + 2 * US);            // [NA][2]
+    // [2][US][NA]: per staged row its ray-table entry (slot 0), or with the
+    // plan's taps table the taps of the group's NA angles
+    float4 *rayb = list + NA * 32;
+    int *lrange = reinterpret_cast<int *>(rayb + 2 * US * NA);       // [NA][2]
     int *uinfo = lrange + 2 * NA;                                    // [2][2] (first pixel, rows)
     if (A.skip && *A.skip) return;
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -725,13 +795,18 @@ __global__ void __launch_bounds__(kFpThreads, 3)
                 uinfo[2 * buf] = ulo;
                 uinfo[2 * buf + 1] = n;
                 __threadfence_block();  // counts before the arrival
-                umma::mbar_arrive_expect_tx(&full[buf], (uint32_t)n * (row_bytes + 16u));
+                umma::mbar_arrive_expect_tx(&full[buf],
+                                            (uint32_t)n * (row_bytes + (A.taps ? 16u * NA : 16u)));
             }
             __syncwarp();
             if (lane < n) {
                 umma::bulk_g2s(stg + ((size_t)buf * US + lane) * SPAN, x + (size_t)k * ys + yb,
                                row_bytes, &full[buf]);
-                umma::bulk_g2s(rayb + buf * US + lane, A.ray + k, 16u, &full[buf]);
+                if (A.taps)
+                    umma::bulk_g2s(rayb + (buf * US + lane) * NA,
+                                   A.taps + ((size_t)grp * A.nrays + k) * NA, 16u * NA, &full[buf]);
+                else
+                    umma::bulk_g2s(rayb + (buf * US + lane) * NA, A.ray + k, 16u, &full[buf]);
             }
         }
         return;
@@ -757,7 +832,16 @@ __global__ void __launch_bounds__(kFpThreads, 3)
         float4 ent = make_float4(0.f, 0.f, 0.f, 0.f);
         if (angle_ok && lane < un && li >= my_lo && li <= my_hi) {
             const int row = ca > 0.f ? lane : un - 1 - lane;
-            const Taps t = ray_taps<W>(rayb[buf * US + row], ap, A.r_hi, A.r_lo);
+            Taps t;
+            if (A.taps) {
+                const float4 tt = rayb[(buf * US + row) * NA + ai];
+                t.iqx = __float_as_int(tt.x);
+                t.w0 = tt.y;
+                t.w1 = tt.z;
+                t.w2 = tt.w;
+            } else {
+                t = ray_taps<W>(rayb[(buf * US + row) * NA], ap, A.r_hi, A.r_lo);
+            }
             gk = t.iqx - b0 + 1;
             valid = gk >= 0 && gk <= BT + 1;
             ent = make_float4(__int_as_float(row | (gk << 8)), t.w0, t.w1, t.w2);
@@ -891,6 +975,16 @@ int launch_bp(const OpArgs &A, int vec, int nsc, dim3 grid, const float *s, floa
     ARECGB_BP(1, 2) ARECGB_BP(2, 2) ARECGB_BP(4, 2) ARECGB_BP(8, 2)
 #undef ARECGB_BP
     return -1;
+}
+
+// The plan's tables for weighting W (one launch each).
+template <int W>
+int launch_tables(const OpArgs &A, int ntiles, float4 *taps, float4 *bpw, int2 *bpf,
+                  cudaStream_t st) {
+    const size_t n = (size_t)A.ngroups * A.nrays * 4;
+    k_fp_taps<W><<<(unsigned)((n + 255) / 256), 256, 0, st>>>(A, taps);
+    k_bp_table<W, kBpFoot><<<dim3(ntiles, (A.na + 3) / 4), 128, 0, st>>>(A, bpw, bpf);
+    return 0;
 }
 
 template <int W, int V, int BT>

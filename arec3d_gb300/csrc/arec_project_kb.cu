@@ -13,4 +13,9 @@ int launch_fpb_kb(const OpArgs &A, int vec, dim3 grid, const float *x, float *q,
     return launch_fpb<ARECGB_KB, kFpBins>(A, vec, grid, x, q, g0, ngo, lo, hi, st);
 }
 
+int launch_tables_kb(const OpArgs &A, int ntiles, float4 *taps, float4 *bpw, int2 *bpf,
+                    cudaStream_t st) {
+    return launch_tables<ARECGB_KB>(A, ntiles, taps, bpw, bpf, st);
+}
+
 }  // namespace arecgb

@@ -130,7 +130,9 @@ def make_problem(gb, seed, device="cuda"):
     from arec3d_gb300 import synthetic as syn
 
     angles = syn.uniform_angles(NA)
+    t0 = time.perf_counter()
     plan = gb.Plan(gb.SQ, 0.5 * (NX - 1), NY, angles)
+    plan.create_ms = (time.perf_counter() - t0) * 1e3  # geometry tables + projector tables
     ph = syn.sphere_cylinder_phantom(seed, NX, NY)
     b = syn.sphere_sinogram(ph, NX, NY, angles, ys=plan.ys, device=device)
     syn.poisson_log(b, PHOTONS, seed + 1, NY, device=device)
@@ -578,7 +580,10 @@ def main():
         cfg = dict(CONFIG, iterations=n_it, rel_final=rel_final,
                    parallelism="replicas" if world > 1 else "single",
                    autotuned={"fp_band_lines": tuned[0], "fp_vec": tuned[1], "bp_vec": tuned[2],
-                              "bp_slice_chunks": tuned[3]})
+                              "bp_slice_chunks": tuned[3]},
+                   plan={"projector_tables_gb": plan.table_bytes() / 1e9,
+                         "create_ms": getattr(plan, "create_ms", None),
+                         "note": "created once per geometry, outside the timed region"})
         if net is not None:
             cfg.update(warm_start=True, sirt_iters=sirt_iters,
                        workload="learned warm start: SIRT-%d -> BF16 U-Net -> CGLS to "

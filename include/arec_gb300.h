@@ -134,6 +134,14 @@ int arecgb_plan_timing(arecgb_plan *plan, int mode, double *fp_ms, long long *fp
 int arecgb_plan_autotune(arecgb_plan *plan, float *d_x, float *d_q, int *fp_band, int *bp_nsc,
                          void *stream);
 
+/* Device bytes of the plan's projector tables (0: none).  A plan for the
+ * square-pixel or Kaiser-Bessel weighting stores the taps of every (ray,
+ * angle) and the back projector's per-tile ring plans when they take at most
+ * 40 % of the free device memory and the environment variable
+ * ARECGB_PLAN_TABLES is not "0" at creation; the projectors compute the same
+ * values without them (identical results).  No counterpart in the reference. */
+long long arecgb_plan_table_bytes(const arecgb_plan *plan);
+
 /* Launch shapes in use: forward band height and floats per lane,
  * back-projection floats per lane and slice chunks per block (0: chosen by
  * size).  No counterpart in the reference. */

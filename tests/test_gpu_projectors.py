@@ -170,6 +170,8 @@ def test_autotuned_shapes_keep_parity(gb, oc, w):
     plan = gb.Plan(w, radius, ny, ang)
     band, nsc = plan.autotune(empty_vol(plan), empty_sino(plan))
     assert band in (32, 64, 128) and nsc in (1, 2)
+    _, fvec, bvec, _ = plan.shapes()
+    assert fvec in (4, 8) and bvec in (4, 8)
     rng = np.random.default_rng(w)
     x = rng.standard_normal((plan.nrays, ny)).astype(np.float32)
     q_ref = oc.project(w, radius, x, ang)
@@ -182,3 +184,28 @@ def test_autotuned_shapes_keep_parity(gb, oc, w):
     assert rel_l2(vol_from_dev(plan, gd), g_ref) < TOL
     assert plan.check() == 0
     print("autotune w=%d: band %d, back-projection chunks %d" % (w, band, nsc))
+
+
+@pytest.mark.parametrize("w", [2, 3])
+@pytest.mark.parametrize("gi", [2, 4, 5, 6])
+def test_plan_tables_change_nothing(gb, w, gi, monkeypatch):
+    """A plan with the projector tables (the taps of every ray and angle, the
+    back projector's ring plans) and one without give bit-identical
+    projections: the tables hold exactly what the kernels compute."""
+    radius, ny, ang = GEOMS[gi]
+    with_t = gb.Plan(w, radius, ny, ang)
+    monkeypatch.setenv("ARECGB_PLAN_TABLES", "0")
+    without = gb.Plan(w, radius, ny, ang)
+    assert with_t.table_bytes() > 0 and without.table_bytes() == 0
+    rng = np.random.default_rng(gi * 10 + w)
+    x = rng.standard_normal((with_t.nrays, ny)).astype(np.float32)
+    s = rng.standard_normal((len(ang), ny, with_t.nx)).astype(np.float32)
+    out = []
+    for plan in (with_t, without):
+        qd, gd = empty_sino(plan), empty_vol(plan)
+        plan.project(vol_to_dev(plan, x), qd)
+        plan.backproject(sino_to_dev(plan, s), gd)
+        out.append((sino_from_dev(plan, qd), vol_from_dev(plan, gd)))
+        assert plan.check() == 0
+    assert np.array_equal(out[0][0], out[1][0])
+    assert np.array_equal(out[0][1], out[1][1])
