@@ -85,6 +85,7 @@ def lib():
         L.arecgb_ncc_filtered.argtypes = [vp, vp, C.c_int, C.c_int, C.c_int, vp, vp]
         L.arecgb_take_log.argtypes = [vp, C.c_size_t, vp]
         L.arecgb_plan_shapes.argtypes = [vp, ip, ip, ip, ip]
+        L.arecgb_plan_set_shapes.argtypes = [vp, C.c_int, C.c_int, C.c_int, C.c_int]
         L.arecgb_plan_table_bytes.argtypes = [vp]
         L.arecgb_plan_table_bytes.restype = C.c_longlong
         L.arecgb_profile_shifts.argtypes = [vp, C.c_int, C.c_int, C.c_int, C.c_int, dp, dp, vp]
@@ -284,6 +285,11 @@ class Plan:
         _check(lib().arecgb_plan_autotune(self._h, _ptr(x), _ptr(q), C.byref(band), C.byref(nsc),
                                           _stream(stream)), "arecgb_plan_autotune")
         return band.value, nsc.value
+
+    def set_shapes(self, fp_band, fp_vec, bp_vec, bp_nsc):
+        """Launch shapes as (forward band, forward VEC, back VEC, chunks)."""
+        _check(lib().arecgb_plan_set_shapes(self._h, fp_band, fp_vec, bp_vec, bp_nsc),
+               "arecgb_plan_set_shapes")
 
     def table_bytes(self):
         """Device bytes of the plan's projector tables (0: none)."""

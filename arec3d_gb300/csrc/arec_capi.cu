@@ -202,6 +202,27 @@ int arecgb_plan_autotune(arecgb_plan *plan, float *d_x, float *d_q, int *fp_band
     return rc;
 }
 
+int arecgb_plan_set_shapes(arecgb_plan *plan, int fp_band, int fp_vec, int bp_vec, int bp_nsc) {
+    if (!plan) {
+        set_error("arecgb_plan_set_shapes: null plan");
+        return ARECGB_ERR_ARG;
+    }
+    Plan *p = reinterpret_cast<Plan *>(plan);
+    auto vec_ok = [&](int v) { return v == p->vec || (v == p->vec / 2 && v >= 1); };
+    if ((fp_band != 32 && fp_band != 64 && fp_band != 128) || !vec_ok(fp_vec) || !vec_ok(bp_vec) ||
+        (bp_nsc != 1 && bp_nsc != 2)) {
+        set_error("arecgb_plan_set_shapes: band must be 32, 64 or 128, vectors the plan's VEC or "
+                  "half of it, chunks 1 or 2");
+        return ARECGB_ERR_ARG;
+    }
+    p->fp_band = fp_band;
+    p->fp_vec = fp_vec;
+    p->bp_vec = bp_vec;
+    p->bp_nsc = bp_nsc;
+    p->tuned = 1;
+    return 0;
+}
+
 long long arecgb_plan_table_bytes(const arecgb_plan *plan) {
     return plan ? (long long)reinterpret_cast<const Plan *>(plan)->table_bytes : 0;
 }

@@ -134,6 +134,11 @@ int arecgb_plan_timing(arecgb_plan *plan, int mode, double *fp_ms, long long *fp
 int arecgb_plan_autotune(arecgb_plan *plan, float *d_x, float *d_q, int *fp_band, int *bp_nsc,
                          void *stream);
 
+/* Set the launch shapes directly (e.g. ones arecgb_plan_autotune chose for
+ * another plan of the same geometry): band 32, 64 or 128; vectors the plan's
+ * VEC or half of it; chunks 1 or 2.  No counterpart in the reference. */
+int arecgb_plan_set_shapes(arecgb_plan *plan, int fp_band, int fp_vec, int bp_vec, int bp_nsc);
+
 /* Device bytes of the plan's projector tables (0: none).  A plan for the
  * square-pixel or Kaiser-Bessel weighting stores the taps of every (ray,
  * angle) and the back projector's per-tile ring plans when they take at most
