@@ -25,22 +25,46 @@ static int blocks_for(size_t n) {
     for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < (n); i += (size_t)gridDim.x * blockDim.x)
 
 // ---- first layer: 1 -> C channels, 3x3, bias, ReLU (CUDA cores: 9 MACs per output) ---------
-__global__ void k_conv_in(const float *__restrict__ x, const float *__restrict__ w,
-                          const float *__restrict__ b, __nv_bfloat16 *__restrict__ y, int N, int H,
-                          int W, int C) {
+// One thread per pixel and all C channels: the 9 inputs are read once, the
+// outputs leave as 16-byte vectors; per output the FMAs run in tap order from
+// the bias (taps outside the image skipped).
+template <int C>
+__global__ void __launch_bounds__(256)
+    k_conv_in(const float *__restrict__ x, const float *__restrict__ w,
+              const float *__restrict__ b, __nv_bfloat16 *__restrict__ y, int N, int H, int W) {
+    __shared__ float sw[C * 9], sb[C];
+    for (int i = threadIdx.x; i < C * 9; i += blockDim.x) sw[i] = w[i];
+    for (int i = threadIdx.x; i < C; i += blockDim.x) sb[i] = b[i];
+    __syncthreads();
     const size_t P = (size_t)N * H * W;
-    GRID_STRIDE(i, P * C) {
-        const size_t p = i / C;
-        const int c = (int)(i % C);
-        const int n = (int)(p / ((size_t)H * W)), h = (int)((p / W) % H), wx = (int)(p % W);
-        float s = b[c];
+    GRID_STRIDE(p, P) {
+        const int wx = (int)(p % W);
+        const size_t nh = p / W;
+        const int h = (int)(nh % H);
+        const size_t row0 = nh - h;  // first row of this image
+        float v[9];
+        bool in[9];
 #pragma unroll
         for (int t = 0; t < 9; t++) {
             const int hh = h + t / 3 - 1, ww = wx + t % 3 - 1;
-            if (hh >= 0 && hh < H && ww >= 0 && ww < W)
-                s = fmaf(w[c * 9 + t], x[((size_t)n * H + hh) * W + ww], s);
+            in[t] = hh >= 0 && hh < H && ww >= 0 && ww < W;
+            v[t] = in[t] ? x[(row0 + hh) * W + ww] : 0.f;
         }
-        y[i] = tobf(fmaxf(s, 0.f));
+        uint4 *yp = reinterpret_cast<uint4 *>(y + p * C);
+#pragma unroll
+        for (int q = 0; q < C / 8; q++) {
+            __align__(16) __nv_bfloat16 o[8];
+#pragma unroll
+            for (int j = 0; j < 8; j++) {
+                const int c = q * 8 + j;
+                float s = sb[c];
+#pragma unroll
+                for (int t = 0; t < 9; t++)
+                    if (in[t]) s = fmaf(sw[c * 9 + t], v[t], s);
+                o[j] = tobf(fmaxf(s, 0.f));
+            }
+            yp[q] = *reinterpret_cast<const uint4 *>(o);
+        }
     }
 }
 
@@ -82,12 +106,24 @@ __global__ void k_conv_in_wgrad(const float *__restrict__ x, const __nv_bfloat16
 }
 
 // ---- last layer: 1x1, C -> 1, plus the residual input --------------------------------------
-__global__ void k_conv_out(const __nv_bfloat16 *__restrict__ h, const float *__restrict__ w,
-                           const float *__restrict__ b, const float *__restrict__ x0,
-                           float *__restrict__ y, size_t P, int C) {
+template <int C>
+__global__ void __launch_bounds__(256)
+    k_conv_out(const __nv_bfloat16 *__restrict__ h, const float *__restrict__ w,
+               const float *__restrict__ b, const float *__restrict__ x0,
+               float *__restrict__ y, size_t P) {
+    __shared__ float sw[C];
+    for (int i = threadIdx.x; i < C; i += blockDim.x) sw[i] = w[i];
+    __syncthreads();
     GRID_STRIDE(p, P) {
         float s = b[0] + x0[p];
-        for (int c = 0; c < C; c++) s = fmaf(w[c], bf(h[p * C + c]), s);
+        const uint4 *hp = reinterpret_cast<const uint4 *>(h + p * C);
+#pragma unroll
+        for (int q = 0; q < C / 8; q++) {
+            const uint4 hv = hp[q];
+            const __nv_bfloat16 *hb = reinterpret_cast<const __nv_bfloat16 *>(&hv);
+#pragma unroll
+            for (int j = 0; j < 8; j++) s = fmaf(sw[q * 8 + j], bf(hb[j]), s);
+        }
         y[p] = s;
     }
 }
@@ -133,27 +169,44 @@ __global__ void __launch_bounds__(128)
 }
 
 // ---- pooling / upsampling / concat -----------------------------------------------------------
+// 2x2 max pooling with the arg max (0..3, first of equals) per output; one
+// thread per output pixel and 8 channels (16-byte vectors; C % 8 == 0).
 __global__ void k_maxpool(const __nv_bfloat16 *__restrict__ x, __nv_bfloat16 *__restrict__ y,
                           uint8_t *__restrict__ arg, int N, int H, int W, int C) {
-    const int Ho = H / 2, Wo = W / 2;
-    const size_t n_out = (size_t)N * Ho * Wo * C;
+    const int Ho = H / 2, Wo = W / 2, C8 = C / 8;
+    const size_t n_out = (size_t)N * Ho * Wo * C8;
     GRID_STRIDE(i, n_out) {
-        const int c = (int)(i % C);
-        const size_t po = i / C;
-        const int n = (int)(po / ((size_t)Ho * Wo)), ho = (int)((po / Wo) % Ho), wo = (int)(po % Wo);
-        float best = -3.4e38f;
-        int bi = 0;
+        const int g = (int)(i % C8);
+        const size_t po = i / C8;
+        const int wo = (int)(po % Wo);
+        const size_t nho = po / Wo;  // n * Ho + ho
+        const size_t top = (2 * nho) * W + 2 * wo;  // (n * H + 2 ho) * W + 2 wo
+        float best[8];
+        uint8_t bi[8];
 #pragma unroll
         for (int t = 0; t < 4; t++) {
-            const int h = 2 * ho + (t >> 1), w = 2 * wo + (t & 1);
-            const float v = bf(x[(((size_t)n * H + h) * W + w) * C + c]);
-            if (v > best) {
-                best = v;
-                bi = t;
+            const size_t pix = top + (size_t)(t >> 1) * W + (t & 1);
+            const uint4 xv = *reinterpret_cast<const uint4 *>(x + pix * C + g * 8);
+            const __nv_bfloat16 *xb = reinterpret_cast<const __nv_bfloat16 *>(&xv);
+#pragma unroll
+            for (int j = 0; j < 8; j++) {
+                const float v = bf(xb[j]);
+                if (t == 0 || v > best[j]) {
+                    best[j] = v;
+                    bi[j] = (uint8_t)t;
+                }
             }
         }
-        y[i] = tobf(best);
-        arg[i] = (uint8_t)bi;
+        __align__(16) __nv_bfloat16 o[8];
+#pragma unroll
+        for (int j = 0; j < 8; j++) o[j] = tobf(best[j]);
+        *reinterpret_cast<uint4 *>(y + po * C + g * 8) = *reinterpret_cast<const uint4 *>(o);
+        if (arg) {
+            uint2 a;
+            a.x = bi[0] | (bi[1] << 8) | (bi[2] << 16) | ((uint32_t)bi[3] << 24);
+            a.y = bi[4] | (bi[5] << 8) | (bi[6] << 16) | ((uint32_t)bi[7] << 24);
+            *reinterpret_cast<uint2 *>(arg + po * C + g * 8) = a;
+        }
     }
 }
 
@@ -173,15 +226,23 @@ __global__ void k_maxpool_bwd(const __nv_bfloat16 *__restrict__ dy, const uint8_
 }
 
 // nearest 2x upsampling of x [N][H][W][C] into channels [0, C) of y [N][2H][2W][Cy]
+// One thread per input pixel and 8 channels: one 16-byte load, four stores
+// (C, Cy multiples of 8).
 __global__ void k_upsample(const __nv_bfloat16 *__restrict__ x, __nv_bfloat16 *__restrict__ y,
                            int N, int H, int W, int C, int Cy) {
-    const size_t n_out = (size_t)N * 4 * H * W * C;
-    GRID_STRIDE(i, n_out) {
-        const int c = (int)(i % C);
-        const size_t po = i / C;
-        const int n = (int)(po / ((size_t)4 * H * W)), h = (int)((po / (2 * W)) % (2 * H)),
-                  w = (int)(po % (2 * W));
-        y[po * Cy + c] = x[(((size_t)n * H + h / 2) * W + w / 2) * C + c];
+    const int C8 = C / 8;
+    const size_t n_in = (size_t)N * H * W * C8;
+    GRID_STRIDE(i, n_in) {
+        const int g = (int)(i % C8);
+        const size_t p = i / C8;
+        const int w = (int)(p % W);
+        const size_t nh = p / W;  // n * H + h
+        const uint4 v = *reinterpret_cast<const uint4 *>(x + p * C + g * 8);
+        const size_t o0 = ((2 * nh) * (2 * W) + 2 * w) * Cy + g * 8;  // row 2h, column 2w
+        *reinterpret_cast<uint4 *>(y + o0) = v;
+        *reinterpret_cast<uint4 *>(y + o0 + Cy) = v;
+        *reinterpret_cast<uint4 *>(y + o0 + (size_t)2 * W * Cy) = v;
+        *reinterpret_cast<uint4 *>(y + o0 + (size_t)2 * W * Cy + Cy) = v;
     }
 }
 
@@ -206,7 +267,13 @@ __global__ void k_upsample_bwd(const __nv_bfloat16 *__restrict__ dy, __nv_bfloat
 // copy x [P][C] into channels [off, off+C) of y [P][Cy]
 __global__ void k_chan_copy(const __nv_bfloat16 *__restrict__ x, __nv_bfloat16 *__restrict__ y,
                             size_t P, int C, int Cy, int off) {
-    GRID_STRIDE(i, P * C) { y[(i / C) * Cy + off + (i % C)] = x[i]; }
+    const int C8 = C / 8;  // 16-byte vectors (C, Cy, off multiples of 8)
+    GRID_STRIDE(i, P * C8) {
+        const size_t p = i / C8;
+        const int g = (int)(i % C8);
+        *reinterpret_cast<uint4 *>(y + p * Cy + off + g * 8) =
+            *reinterpret_cast<const uint4 *>(x + p * C + g * 8);
+    }
 }
 
 // dst[P][C] (fp32 accumulator) += channels [off, off+C) of src [P][Cs]
@@ -390,7 +457,8 @@ __global__ void k_sumsq_partial(const float *__restrict__ a, size_t n, double *_
 // ---- host launchers -----------------------------------------------------------------------
 void conv_in(const float *x, const float *w, const float *b, __nv_bfloat16 *y, int N, int H, int W,
              int C, cudaStream_t st) {
-    k_conv_in<<<blocks_for((size_t)N * H * W * C), 256, 0, st>>>(x, w, b, y, N, H, W, C);
+    if (C != 32) return;  // the network's first layer (32 channels)
+    k_conv_in<32><<<blocks_for((size_t)N * H * W), 256, 0, st>>>(x, w, b, y, N, H, W);
 }
 void conv_in_wgrad(const float *x, const __nv_bfloat16 *dpre, float *gw, float *gb, int N, int H,
                    int W, int C, cudaStream_t st) {
@@ -400,7 +468,8 @@ void conv_in_wgrad(const float *x, const __nv_bfloat16 *dpre, float *gw, float *
 }
 void conv_out(const __nv_bfloat16 *h, const float *w, const float *b, const float *x0, float *y,
               size_t P, int C, cudaStream_t st) {
-    k_conv_out<<<blocks_for(P), 256, 0, st>>>(h, w, b, x0, y, P, C);
+    if (C != kOutC) return;
+    k_conv_out<kOutC><<<blocks_for(P), 256, 0, st>>>(h, w, b, x0, y, P);
 }
 void conv_out_bwd(const __nv_bfloat16 *h, const float *w, const float *dy, __nv_bfloat16 *dh,
                   float *gw, float *gb, size_t P, int C, cudaStream_t st) {
@@ -410,7 +479,7 @@ void conv_out_bwd(const __nv_bfloat16 *h, const float *w, const float *dy, __nv_
 }
 void maxpool(const __nv_bfloat16 *x, __nv_bfloat16 *y, uint8_t *arg, int N, int H, int W, int C,
              cudaStream_t st) {
-    k_maxpool<<<blocks_for((size_t)N * H * W * C / 4), 256, 0, st>>>(x, y, arg, N, H, W, C);
+    k_maxpool<<<blocks_for((size_t)N * H * W * C / 32), 256, 0, st>>>(x, y, arg, N, H, W, C);
 }
 void maxpool_bwd(const __nv_bfloat16 *dy, const uint8_t *arg, float *dx_acc, int N, int H, int W,
                  int C, cudaStream_t st) {
@@ -418,7 +487,7 @@ void maxpool_bwd(const __nv_bfloat16 *dy, const uint8_t *arg, float *dx_acc, int
 }
 void upsample(const __nv_bfloat16 *x, __nv_bfloat16 *y, int N, int H, int W, int C, int Cy,
               cudaStream_t st) {
-    k_upsample<<<blocks_for((size_t)N * 4 * H * W * C), 256, 0, st>>>(x, y, N, H, W, C, Cy);
+    k_upsample<<<blocks_for((size_t)N * H * W * C / 8), 256, 0, st>>>(x, y, N, H, W, C, Cy);
 }
 void upsample_bwd(const __nv_bfloat16 *dy, __nv_bfloat16 *dx, int N, int H, int W, int C, int Cy,
                   cudaStream_t st) {
@@ -426,7 +495,7 @@ void upsample_bwd(const __nv_bfloat16 *dy, __nv_bfloat16 *dx, int N, int H, int 
 }
 void chan_copy(const __nv_bfloat16 *x, __nv_bfloat16 *y, size_t P, int C, int Cy, int off,
                cudaStream_t st) {
-    k_chan_copy<<<blocks_for(P * C), 256, 0, st>>>(x, y, P, C, Cy, off);
+    k_chan_copy<<<blocks_for(P * C / 8), 256, 0, st>>>(x, y, P, C, Cy, off);
 }
 void chan_add(const __nv_bfloat16 *src, float *dst, size_t P, int C, int Cs, int off,
               cudaStream_t st) {
