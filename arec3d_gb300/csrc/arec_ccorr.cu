@@ -77,6 +77,12 @@ __device__ __forceinline__ void dft_reg(float2 *v) {
     }
 }
 
+// Shared-memory lines are padded by one element per 16 (index i at
+// pz(i) = i + i/16, line length plen(N)): the Stockham passes write with
+// strides of 16 elements, which would otherwise fall in one bank.
+__device__ __host__ __forceinline__ int pz(int i) { return i + (i >> 4); }
+__device__ __host__ __forceinline__ int plen(int n) { return n + (n >> 4); }
+
 template <int R>
 __device__ __forceinline__ void stockham_pass(float2 *L, int N, int Ns, int b, bool active,
                                               const float2 *__restrict__ tw) {
@@ -91,7 +97,7 @@ __device__ __forceinline__ void stockham_pass(float2 *L, int N, int Ns, int b, b
             const int step = N / (Ns * R);
 #pragma unroll
             for (int r = 0; r < R; r++) {
-                const float2 x = L[j + r * NR];
+                const float2 x = L[pz(j + r * NR)];
                 const float2 w = __ldg(&tw[(r * k * step) & (N - 1)]);
                 v[i * R + r] = cmul(x, w);
             }
@@ -106,14 +112,14 @@ __device__ __forceinline__ void stockham_pass(float2 *L, int N, int Ns, int b, b
             const int k = j % Ns;
             const int d = (j / Ns) * Ns * R + k;
 #pragma unroll
-            for (int r = 0; r < R; r++) L[d + r * Ns] = v[i * R + r];
+            for (int r = 0; r < R; r++) L[pz(d + r * Ns)] = v[i * R + r];
         }
     }
     __syncthreads();
 }
 
 // In-place forward FFT of G lines of length N (power of two, 16..4096) held in
-// shared memory at buf + l*lstride.  N/16 threads per line; all threads of the
+// shared memory at buf + l*lstride (padded lines: element i at pz(i)).  N/16 threads per line; all threads of the
 // block must call it.
 __device__ void fft_lines(float2 *buf, int N, int lstride, int G, const float2 *tw) {
     const int tpl = N / 16;
@@ -153,15 +159,15 @@ __global__ void __launch_bounds__(256) k_cc_rows_fwd(const float *__restrict__ x
         const int l = i / nx, c = i % nx, row = row0 + l;
         float2 z = make_float2(0.f, 0.f);
         if (row < ny) z = make_float2(x[img + (size_t)row * nx + c], y[img + (size_t)row * nx + c]);
-        sm[l * nx + c] = z;
+        sm[l * plen(nx) + pz(c)] = z;
     }
     __syncthreads();
-    fft_lines(sm, nx, nx, G, tw);
+    fft_lines(sm, nx, plen(nx), G, tw);
     const size_t half = (size_t)pair * ny * H;
     for (int i = threadIdx.x; i < G * H; i += blockDim.x) {
         const int l = i / H, k = i % H, row = row0 + l;
         if (row >= ny) continue;
-        const float2 Z = sm[l * nx + k], Zm = sm[l * nx + ((nx - k) & (nx - 1))];
+        const float2 Z = sm[l * plen(nx) + pz(k)], Zm = sm[l * plen(nx) + pz((nx - k) & (nx - 1))];
         Xh[half + (size_t)row * H + k] = make_float2(0.5f * (Z.x + Zm.x), 0.5f * (Z.y - Zm.y));
         Yh[half + (size_t)row * H + k] = make_float2(0.5f * (Z.y + Zm.y), -0.5f * (Z.x - Zm.x));
     }
@@ -180,7 +186,8 @@ __global__ void __launch_bounds__(256) k_cc_cols(float2 *__restrict__ Xh,
     const int c0 = blockIdx.x * ct, pair = blockIdx.y;
     const int nc = min(ct, H - c0);
     const size_t half = (size_t)pair * ny * H;
-    float2 *sx = sm, *sy = sm + ct * ny;
+    const int PN = plen(ny);
+    float2 *sx = sm, *sy = sm + ct * PN;
     for (int i = threadIdx.x; i < ct * ny; i += blockDim.x) {
         const int row = i / ct, c = i % ct;
         float2 a = make_float2(0.f, 0.f), b = a;
@@ -188,26 +195,27 @@ __global__ void __launch_bounds__(256) k_cc_cols(float2 *__restrict__ Xh,
             a = Xh[half + (size_t)row * H + c0 + c];
             b = Yh[half + (size_t)row * H + c0 + c];
         }
-        sx[c * ny + row] = a;
-        sy[c * ny + row] = b;
+        sx[c * PN + pz(row)] = a;
+        sy[c * PN + pz(row)] = b;
     }
     __syncthreads();
     const int G = max(1, 256 / (ny / 16));
     for (int l0 = 0; l0 < 2 * ct; l0 += G)
-        fft_lines(sm + (size_t)l0 * ny, ny, ny, min(G, 2 * ct - l0), tw);
+        fft_lines(sm + (size_t)l0 * PN, ny, PN, min(G, 2 * ct - l0), tw);
     // conj(X)*Y, conjugated again for the inverse transform (IDFT = conj DFT conj)
     for (int i = threadIdx.x; i < ct * ny; i += blockDim.x) {
-        const float2 a = sx[i], b = sy[i];
+        const int c = i / ny, row = i % ny, o = c * PN + pz(row);
+        const float2 a = sx[o], b = sy[o];
         const float2 cc = make_float2(a.x * b.x + a.y * b.y, a.x * b.y - a.y * b.x);
-        sx[i] = make_float2(cc.x, -cc.y);
+        sx[o] = make_float2(cc.x, -cc.y);
     }
     __syncthreads();
     for (int l0 = 0; l0 < ct; l0 += G)
-        fft_lines(sm + (size_t)l0 * ny, ny, ny, min(G, ct - l0), tw);
+        fft_lines(sm + (size_t)l0 * PN, ny, PN, min(G, ct - l0), tw);
     for (int i = threadIdx.x; i < ct * ny; i += blockDim.x) {
         const int row = i / ct, c = i % ct;
         if (c < nc) {
-            const float2 w = sx[c * ny + row];
+            const float2 w = sx[c * PN + pz(row)];
             Xh[half + (size_t)row * H + c0 + c] = make_float2(w.x, -w.y);
         }
     }
@@ -244,10 +252,10 @@ __global__ void __launch_bounds__(256) k_cc_rows_inv(const float2 *__restrict__ 
                 w = Wh[half + (size_t)row * H + (nx - k)];  // conj(conj(W[nx-k]))
             }
         }
-        sm[l * nx + k] = w;
+        sm[l * plen(nx) + pz(k)] = w;
     }
     __syncthreads();
-    fft_lines(sm, nx, nx, G, tw);
+    fft_lines(sm, nx, plen(nx), G, tw);
     // one warp per row for the statistics
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const size_t img = (size_t)pair * nx * ny;
@@ -256,7 +264,7 @@ __global__ void __launch_bounds__(256) k_cc_rows_inv(const float2 *__restrict__ 
         if (row >= ny) continue;
         RowStat s{-1.0f, INT_MAX, -1, 0};
         for (int i = lane; i < nx; i += 32) {
-            const float v = sm[l * nx + i].x;
+            const float v = sm[l * plen(nx) + pz(i)].x;
             if (c) c[img + (size_t)row * nx + i] = v;
             const float a = fabsf(v);
             RowStat t{a, v == a && a == a ? i : INT_MAX, v == -a && v != a ? i : -1, 0};
@@ -432,13 +440,13 @@ __global__ void __launch_bounds__(256) k_fs_rows(const float *__restrict__ in,
     const size_t img = (size_t)blockIdx.y * nx * ny;
     for (int i = threadIdx.x; i < G * nx; i += blockDim.x) {
         const int l = i / nx, c = i % nx, row = row0 + l;
-        sm[l * nx + c] = make_float2(row < ny ? in[img + (size_t)row * nx + c] : 0.f, 0.f);
+        sm[l * plen(nx) + pz(c)] = make_float2(row < ny ? in[img + (size_t)row * nx + c] : 0.f, 0.f);
     }
     __syncthreads();
-    fft_lines(sm, nx, nx, G, tw);
+    fft_lines(sm, nx, plen(nx), G, tw);
     for (int i = threadIdx.x; i < G * nx; i += blockDim.x) {
         const int l = i / nx, c = i % nx, row = row0 + l;
-        if (row < ny) C[img + (size_t)row * nx + c] = sm[l * nx + c];
+        if (row < ny) C[img + (size_t)row * nx + c] = sm[l * plen(nx) + pz(c)];
     }
 }
 
@@ -457,31 +465,32 @@ __global__ void __launch_bounds__(256) k_fs_cols(float2 *__restrict__ C, int nx,
     const size_t img = (size_t)blockIdx.y * nx * ny;
     const float sx = sxs[blockIdx.y], sy = sys[blockIdx.y];
     const double two_pi = 2.0 * 3.14159265358979323846;
+    const int PN = plen(ny);
     for (int i = threadIdx.x; i < kColTile * ny; i += blockDim.x) {
         const int row = i / kColTile, c = i % kColTile;
-        sm[c * ny + row] = C[img + (size_t)row * nx + c0 + c];
+        sm[c * PN + pz(row)] = C[img + (size_t)row * nx + c0 + c];
     }
     __syncthreads();
     const int G = max(1, 256 / (ny / 16));
     for (int l0 = 0; l0 < kColTile; l0 += G)
-        fft_lines(sm + (size_t)l0 * ny, ny, ny, min(G, kColTile - l0), tw);
+        fft_lines(sm + (size_t)l0 * PN, ny, PN, min(G, kColTile - l0), tw);
     for (int i = threadIdx.x; i < kColTile * ny; i += blockDim.x) {
-        const int c = i / ny, row = i % ny;
+        const int c = i / ny, row = i % ny, o = c * PN + pz(row);
         const float t = __fadd_rn(__fmul_rn(sx, fs_freq(c0 + c, nx)), __fmul_rn(sy, fs_freq(row, ny)));
         const float ph = (float)(-two_pi * (double)t);
         float sn, cs;
         sincosf(ph, &sn, &cs);
-        const float2 f = sm[i];
+        const float2 f = sm[o];
         const float re = __fsub_rn(__fmul_rn(f.x, cs), __fmul_rn(f.y, sn));
         const float im = __fadd_rn(__fmul_rn(f.x, sn), __fmul_rn(f.y, cs));
-        sm[i] = make_float2(re, -im);  // conjugated: IDFT = conj(DFT(conj))
+        sm[o] = make_float2(re, -im);  // conjugated: IDFT = conj(DFT(conj))
     }
     __syncthreads();
     for (int l0 = 0; l0 < kColTile; l0 += G)
-        fft_lines(sm + (size_t)l0 * ny, ny, ny, min(G, kColTile - l0), tw);
+        fft_lines(sm + (size_t)l0 * PN, ny, PN, min(G, kColTile - l0), tw);
     for (int i = threadIdx.x; i < kColTile * ny; i += blockDim.x) {
         const int row = i / kColTile, c = i % kColTile;
-        const float2 w = sm[c * ny + row];
+        const float2 w = sm[c * PN + pz(row)];
         C[img + (size_t)row * nx + c0 + c] = make_float2(w.x, -w.y);
     }
 }
@@ -501,14 +510,14 @@ __global__ void __launch_bounds__(256) k_fs_rows_inv(const float2 *__restrict__ 
             z = C[img + (size_t)row * nx + c];
             z.y = -z.y;
         }
-        sm[l * nx + c] = z;
+        sm[l * plen(nx) + pz(c)] = z;
     }
     __syncthreads();
-    fft_lines(sm, nx, nx, G, tw);
+    fft_lines(sm, nx, plen(nx), G, tw);
     const float scale = (float)(nx * ny);
     for (int i = threadIdx.x; i < G * nx; i += blockDim.x) {
         const int l = i / nx, c = i % nx, row = row0 + l;
-        if (row < ny) out[img + (size_t)row * nx + c] = sm[l * nx + c].x / scale;
+        if (row < ny) out[img + (size_t)row * nx + c] = sm[l * plen(nx) + pz(c)].x / scale;
     }
 }
 
@@ -559,8 +568,8 @@ static int correlate_batch(const float *d1, const float *d2, int np, int ny, int
     if (rc) return rc;
     const int G = rows_per_block(nx);
     const int ct = col_tile(ny);
-    const size_t row_smem = sizeof(float2) * (size_t)G * nx;
-    const size_t col_smem = sizeof(float2) * 2 * ct * (size_t)ny;
+    const size_t row_smem = sizeof(float2) * (size_t)G * plen(nx);
+    const size_t col_smem = sizeof(float2) * 2 * ct * (size_t)plen(ny);
     if ((rc = set_smem((const void *)k_cc_rows_fwd, row_smem))) return rc;
     if ((rc = set_smem((const void *)k_cc_rows_inv, row_smem))) return rc;
     if ((rc = set_smem((const void *)k_cc_cols, col_smem))) return rc;
@@ -649,8 +658,8 @@ int fshift_stack(const float *d_in, float *d_out, int nz, int ny, int nx, const 
     if (!rc) rc = twiddles(ny, &twy);
     if (rc) return rc;
     const int G = rows_per_block(nx);
-    const size_t row_smem = sizeof(float2) * (size_t)G * nx;
-    const size_t col_smem = sizeof(float2) * kColTile * (size_t)ny;
+    const size_t row_smem = sizeof(float2) * (size_t)G * plen(nx);
+    const size_t col_smem = sizeof(float2) * kColTile * (size_t)plen(ny);
     if ((rc = set_smem((const void *)k_fs_rows, row_smem))) return rc;
     if ((rc = set_smem((const void *)k_fs_rows_inv, row_smem))) return rc;
     if ((rc = set_smem((const void *)k_fs_cols, col_smem))) return rc;
@@ -813,8 +822,8 @@ int cc_shifts_static(const float *d1, const float *d2, int nz, int ny, int nx, f
     // column block.  The limits are set on every call: cc_shifts sets them to
     // its own (possibly smaller) sizes.
     const int G = rows_per_block(nx);
-    const size_t row_smem = sizeof(float2) * (size_t)G * nx;
-    const size_t col_smem = sizeof(float2) * 2 * kColTile * (size_t)ny;
+    const size_t row_smem = sizeof(float2) * (size_t)G * plen(nx);
+    const size_t col_smem = sizeof(float2) * 2 * kColTile * (size_t)plen(ny);
     if ((rc = set_smem((const void *)k_cc_rows_fwd, row_smem))) return rc;
     if ((rc = set_smem((const void *)k_cc_rows_inv, row_smem))) return rc;
     if ((rc = set_smem((const void *)k_cc_cols, col_smem))) return rc;
