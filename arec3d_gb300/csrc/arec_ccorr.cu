@@ -144,6 +144,10 @@ struct RowStat {
     int pad;
 };
 
+// Global loads per thread issued together before their shared-memory stores
+// (a block stages 4096 elements: 16 per thread in one batch).
+constexpr int kLoadBatch = 16;
+
 // Pass 1: rows of z = x + i*y -> half spectra of x and y.
 __global__ void __launch_bounds__(256) k_cc_rows_fwd(const float *__restrict__ x,
                                                      const float *__restrict__ y,
@@ -155,11 +159,21 @@ __global__ void __launch_bounds__(256) k_cc_rows_fwd(const float *__restrict__ x
     const int row0 = blockIdx.x * G, pair = blockIdx.y;
     const int H = nx / 2 + 1;
     const size_t img = (size_t)pair * nx * ny;
-    for (int i = threadIdx.x; i < G * nx; i += blockDim.x) {
-        const int l = i / nx, c = i % nx, row = row0 + l;
-        float2 z = make_float2(0.f, 0.f);
-        if (row < ny) z = make_float2(x[img + (size_t)row * nx + c], y[img + (size_t)row * nx + c]);
-        sm[l * plen(nx) + pz(c)] = z;
+    // all of a thread's loads issued before any store (G * nx = 4096: 16 each)
+    for (int i0 = 0; i0 < G * nx; i0 += kLoadBatch * 256) {
+        float2 z[kLoadBatch];
+#pragma unroll
+        for (int e = 0; e < kLoadBatch; e++) {
+            const int i = i0 + e * 256 + threadIdx.x, l = i / nx, c = i % nx, row = row0 + l;
+            z[e] = make_float2(0.f, 0.f);
+            if (i < G * nx && row < ny)
+                z[e] = make_float2(x[img + (size_t)row * nx + c], y[img + (size_t)row * nx + c]);
+        }
+#pragma unroll
+        for (int e = 0; e < kLoadBatch; e++) {
+            const int i = i0 + e * 256 + threadIdx.x, l = i / nx, c = i % nx;
+            if (i < G * nx) sm[l * plen(nx) + pz(c)] = z[e];
+        }
     }
     __syncthreads();
     fft_lines(sm, nx, plen(nx), G, tw);
@@ -188,15 +202,25 @@ __global__ void __launch_bounds__(256) k_cc_cols(float2 *__restrict__ Xh,
     const size_t half = (size_t)pair * ny * H;
     const int PN = plen(ny);
     float2 *sx = sm, *sy = sm + ct * PN;
-    for (int i = threadIdx.x; i < ct * ny; i += blockDim.x) {
-        const int row = i / ct, c = i % ct;
-        float2 a = make_float2(0.f, 0.f), b = a;
-        if (c < nc) {
-            a = Xh[half + (size_t)row * H + c0 + c];
-            b = Yh[half + (size_t)row * H + c0 + c];
+    for (int i0 = 0; i0 < ct * ny; i0 += kLoadBatch * 256) {
+        float2 a[kLoadBatch], b[kLoadBatch];
+#pragma unroll
+        for (int e = 0; e < kLoadBatch; e++) {
+            const int i = i0 + e * 256 + threadIdx.x, row = i / ct, c = i % ct;
+            a[e] = b[e] = make_float2(0.f, 0.f);
+            if (i < ct * ny && c < nc) {
+                a[e] = Xh[half + (size_t)row * H + c0 + c];
+                b[e] = Yh[half + (size_t)row * H + c0 + c];
+            }
         }
-        sx[c * PN + pz(row)] = a;
-        sy[c * PN + pz(row)] = b;
+#pragma unroll
+        for (int e = 0; e < kLoadBatch; e++) {
+            const int i = i0 + e * 256 + threadIdx.x, row = i / ct, c = i % ct;
+            if (i < ct * ny) {
+                sx[c * PN + pz(row)] = a[e];
+                sy[c * PN + pz(row)] = b[e];
+            }
+        }
     }
     __syncthreads();
     const int G = max(1, 256 / (ny / 16));
@@ -241,18 +265,26 @@ __global__ void __launch_bounds__(256) k_cc_rows_inv(const float2 *__restrict__ 
     const int row0 = blockIdx.x * G, pair = blockIdx.y;
     const int H = nx / 2 + 1;
     const size_t half = (size_t)pair * ny * H;
-    for (int i = threadIdx.x; i < G * nx; i += blockDim.x) {
-        const int l = i / nx, k = i % nx, row = row0 + l;
-        float2 w = make_float2(0.f, 0.f);
-        if (row < ny) {
-            if (k < H) {
-                w = Wh[half + (size_t)row * H + k];
-                w.y = -w.y;  // conj for the inverse
-            } else {
-                w = Wh[half + (size_t)row * H + (nx - k)];  // conj(conj(W[nx-k]))
+    for (int i0 = 0; i0 < G * nx; i0 += kLoadBatch * 256) {
+        float2 w[kLoadBatch];
+#pragma unroll
+        for (int e = 0; e < kLoadBatch; e++) {
+            const int i = i0 + e * 256 + threadIdx.x, l = i / nx, k = i % nx, row = row0 + l;
+            w[e] = make_float2(0.f, 0.f);
+            if (i < G * nx && row < ny) {
+                if (k < H) {
+                    w[e] = Wh[half + (size_t)row * H + k];
+                    w[e].y = -w[e].y;  // conj for the inverse
+                } else {
+                    w[e] = Wh[half + (size_t)row * H + (nx - k)];  // conj(conj(W[nx-k]))
+                }
             }
         }
-        sm[l * plen(nx) + pz(k)] = w;
+#pragma unroll
+        for (int e = 0; e < kLoadBatch; e++) {
+            const int i = i0 + e * 256 + threadIdx.x, l = i / nx, k = i % nx;
+            if (i < G * nx) sm[l * plen(nx) + pz(k)] = w[e];
+        }
     }
     __syncthreads();
     fft_lines(sm, nx, plen(nx), G, tw);
