@@ -145,11 +145,13 @@ struct RowStat {
 };
 
 // Global loads per thread issued together before their shared-memory stores
-// (a block stages 4096 elements: 16 per thread in one batch).
+// (a block stages 4096 elements: 16 per thread in one batch).  The three
+// passes are capped at 128 registers (two blocks per SM): the radix-16
+// butterflies spill a little, which costs less than running one block per SM.
 constexpr int kLoadBatch = 16;
 
 // Pass 1: rows of z = x + i*y -> half spectra of x and y.
-__global__ void __launch_bounds__(256) k_cc_rows_fwd(const float *__restrict__ x,
+__global__ void __launch_bounds__(256, 2) k_cc_rows_fwd(const float *__restrict__ x,
                                                      const float *__restrict__ y,
                                                      float2 *__restrict__ Xh,
                                                      float2 *__restrict__ Yh, int nx, int ny,
@@ -192,7 +194,7 @@ __global__ void __launch_bounds__(256) k_cc_rows_fwd(const float *__restrict__ x
 // share an SM); W = IDFT_col(conj(X)*Y) overwrites Xh.
 constexpr int kColTile = 4;
 static inline int col_tile(int ny) { return ny <= 1024 ? 4 : (ny <= 2048 ? 2 : 1); }
-__global__ void __launch_bounds__(256) k_cc_cols(float2 *__restrict__ Xh,
+__global__ void __launch_bounds__(256, 2) k_cc_cols(float2 *__restrict__ Xh,
                                                  const float2 *__restrict__ Yh, int nx, int ny,
                                                  const float2 *__restrict__ tw, int ct) {
     extern __shared__ float2 sm[];
@@ -256,7 +258,7 @@ __device__ __forceinline__ RowStat stat_merge(RowStat a, RowStat b) {
 }
 
 // Pass 3: inverse row transforms -> c rows, with per-row peak statistics.
-__global__ void __launch_bounds__(256) k_cc_rows_inv(const float2 *__restrict__ Wh,
+__global__ void __launch_bounds__(256, 2) k_cc_rows_inv(const float2 *__restrict__ Wh,
                                                      float *__restrict__ c, RowStat *stats,
                                                      int nx, int ny,
                                                      const float2 *__restrict__ tw) {
