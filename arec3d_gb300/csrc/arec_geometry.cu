@@ -128,7 +128,7 @@ int plan_create(Plan **out, int weighting, double radius, int ny, int nangles,
     std::vector<ColInfo> cols(nx);
     for (int i = 0; i < nx; i++) {
         rows[i] = RowInfo{0, nx, -1, 0};
-        cols[i] = ColInfo{nx, -1};
+        cols[i] = ColInfo{nx, -1, 0, 0};
     }
     for (int k = nr - 1; k >= 0; k--) {
         int ix = cord[2 * k], iz = cord[2 * k + 1];
@@ -137,6 +137,20 @@ int plan_create(Plan **out, int weighting, double radius, int ny, int nangles,
         rows[iz].hi = std::max(rows[iz].hi, ix);
         cols[ix].lo = std::min(cols[ix].lo, iz);
         cols[ix].hi = std::max(cols[ix].hi, iz);
+    }
+    // column-major ray order (the forward projector's column sweeps read
+    // consecutive pixels of a column as consecutive rays of a gathered copy)
+    std::vector<int> kinv(nr);
+    {
+        int cs = 0;
+        for (int ix = 0; ix < nx; ix++) {
+            cols[ix].start = cs;
+            if (cols[ix].hi >= cols[ix].lo) cs += cols[ix].hi - cols[ix].lo + 1;
+        }
+        for (int k = 0; k < nr; k++) {
+            const int ix = cord[2 * k], iz = cord[2 * k + 1];
+            kinv[cols[ix].start + iz - cols[ix].lo] = k;
+        }
     }
 
     // Per-angle constants.  The reference evaluates the ray position with
@@ -218,6 +232,7 @@ int plan_create(Plan **out, int weighting, double radius, int ny, int nangles,
     if (e == cudaSuccess) e = cudaMalloc(&p->d_ang, sizeof(AngleParams) * nangles);
     if (e == cudaSuccess) e = cudaMalloc(&p->d_rows, sizeof(RowInfo) * nx);
     if (e == cudaSuccess) e = cudaMalloc(&p->d_cols, sizeof(ColInfo) * nx);
+    if (e == cudaSuccess) e = cudaMalloc(&p->d_kinv, sizeof(int) * std::max(nr, 1));
     if (e == cudaSuccess)
         e = cudaMemcpy(p->d_ray, ray.data(), sizeof(float4) * nr, cudaMemcpyHostToDevice);
     if (e == cudaSuccess)
@@ -227,6 +242,8 @@ int plan_create(Plan **out, int weighting, double radius, int ny, int nangles,
         e = cudaMemcpy(p->d_rows, rows.data(), sizeof(RowInfo) * nx, cudaMemcpyHostToDevice);
     if (e == cudaSuccess)
         e = cudaMemcpy(p->d_cols, cols.data(), sizeof(ColInfo) * nx, cudaMemcpyHostToDevice);
+    if (e == cudaSuccess && nr)
+        e = cudaMemcpy(p->d_kinv, kinv.data(), sizeof(int) * nr, cudaMemcpyHostToDevice);
     if (e == cudaSuccess) {
         // room for the back projector's grid with one slice chunk per block
         // at half the vector width (the autotuner may choose it):
@@ -266,6 +283,8 @@ void plan_destroy(Plan *p) {
     cudaFree(p->d_groups);
     cudaFree(p->d_tiles);
     cudaFree(p->d_taps);
+    cudaFree(p->d_kinv);
+    cudaFree(p->d_xT);
     cudaFree(p->d_bpw);
     cudaFree(p->d_bpf);
     cudaFree(p->d_err);

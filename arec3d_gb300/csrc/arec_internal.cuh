@@ -43,6 +43,8 @@ struct RowInfo {
 
 struct ColInfo {
     int lo, hi; // first/last iz of column ix inside the cylinder
+    int start;  // index of pixel (lo, ix) in column-major ray order
+    int pad;
 };
 
 struct Plan {
@@ -70,7 +72,9 @@ struct Plan {
     // see plan_build_tables): the taps of every (ray, angle) for the forward
     // projector and the back projector's per-(tile, angle) ring plans.  The
     // kernels compute the same values without them.
-    float4 *d_taps = nullptr;     // [ngroups][nrays][4]
+    float4 *d_taps = nullptr;     // [ngroups][nrays][4], rays in each group's line order
+    int *d_kinv = nullptr;        // column-major ray index -> ray index
+    float *d_xT = nullptr;        // [nrays][ys]: x in column-major ray order (column sweeps)
     float4 *d_bpw = nullptr;      // [ntiles][na][32]
     int2 *d_bpf = nullptr;        // [ntiles][na]
     size_t table_bytes = 0;

@@ -1,6 +1,7 @@
 // Projector dispatch: launch shapes, weighting selection and the FP64 norm.
 #include <algorithm>
 #include <cstdlib>
+#include <cstring>
 
 #include "arec_project_impl.cuh"
 
@@ -13,9 +14,9 @@ int launch_fp_lin(const OpArgs &, int, const float *, float *, cudaStream_t);
 int launch_tables_sq(const OpArgs &, int, float4 *, float4 *, int2 *, cudaStream_t);
 int launch_tables_kb(const OpArgs &, int, float4 *, float4 *, int2 *, cudaStream_t);
 int launch_fpb_kb(const OpArgs &, int, dim3, const float *, float *, int, int, int, int,
-                  cudaStream_t);
+                  const CUtensorMap &, const CUtensorMap &, cudaStream_t);
 int launch_fpb_sq(const OpArgs &, int, dim3, const float *, float *, int, int, int, int,
-                  cudaStream_t);
+                  const CUtensorMap &, const CUtensorMap &, cudaStream_t);
 int sumsq_partials(const float *d_v, size_t n, double *d_partials, int nblocks, cudaStream_t st);
 
 static OpArgs make_args(const Plan *p, const int *skip) {
@@ -39,6 +40,7 @@ static OpArgs make_args(const Plan *p, const int *skip) {
     A.taps = p->d_taps;
     A.bpw = p->d_bpw;
     A.bpf = p->d_bpf;
+    A.kinv = p->d_kinv;
     return A;
 }
 
@@ -147,6 +149,28 @@ int forward_project(const Plan *p, const float *d_x, float *d_q, double *d_norm2
             reinterpret_cast<float4 *>(d_q), nq / 4, d_skip);
         const int ntile = (p->nx + kFpBins - 1) / kFpBins;
         rc = 0;
+        // With the tables: tensor maps over x and over its column-major copy
+        // (gathered here when there are column sweeps), box = 32 rays x SPAN
+        // slices; the kernels stage each line's pixels as one tile.
+        CUtensorMap tmx, tmxT;
+        memset(&tmx, 0, sizeof(tmx));
+        memset(&tmxT, 0, sizeof(tmxT));
+        if (A.taps) {
+            const int span = 32 * fp_vec(p);
+            if (p->ngroups_o[1]) {
+                const int ys4 = p->ys / 4;
+                const size_t n4 = (size_t)p->nrays * ys4;
+                k_ray_gather<<<(unsigned)std::min<size_t>(152 * 16, (n4 + 255) / 256), 256, 0, st>>>(
+                    reinterpret_cast<const float4 *>(d_x), reinterpret_cast<float4 *>(p->d_xT),
+                    p->d_kinv, p->nrays, ys4);
+                count_launches(1);
+            }
+            if (!encode_rows_map(&tmx, d_x, p->ys, p->nrays, span, kFpStage) ||
+                !encode_rows_map(&tmxT, p->d_xT, p->ys, p->nrays, span, kFpStage)) {
+                set_error("forward_project: tensor map encoding failed");
+                return ARECGB_ERR_ARG;
+            }
+        }
         for (int o = 0; o < 2 && !rc; o++) {
             const int ngo = p->ngroups_o[o];
             if (!ngo) continue;
@@ -155,8 +179,8 @@ int forward_project(const Plan *p, const float *d_x, float *d_q, double *d_norm2
             for (int lo = 0; lo < p->nx && !rc; lo += p->fp_band) {
                 const int hi = std::min(p->nx, lo + p->fp_band);
                 rc = p->weighting == ARECGB_KB
-                         ? launch_fpb_kb(A, fp_vec(p), grid, d_x, d_q, g0, ngo, lo, hi, st)
-                         : launch_fpb_sq(A, fp_vec(p), grid, d_x, d_q, g0, ngo, lo, hi, st);
+                         ? launch_fpb_kb(A, fp_vec(p), grid, d_x, d_q, g0, ngo, lo, hi, tmx, tmxT, st)
+                         : launch_fpb_sq(A, fp_vec(p), grid, d_x, d_q, g0, ngo, lo, hi, tmx, tmxT, st);
                 count_launches(1);
             }
         }
@@ -208,19 +232,23 @@ int plan_build_tables(Plan *p) {
     if (p->weighting == ARECGB_LIN) return 0;
     const char *env = getenv("ARECGB_PLAN_TABLES");
     if (env && env[0] == '0') return 0;
-    const size_t b_taps = sizeof(float4) * (size_t)p->ngroups * p->nrays * 4;
+    const size_t b_taps = sizeof(float4) * (size_t)p->ngroups * p->nrays * 4 +
+                          sizeof(float) * (size_t)p->nrays * p->ys;  // + x's column-major copy
     const size_t b_bpw = sizeof(float4) * (size_t)p->ntiles * p->na * 32;
     const size_t b_bpf = sizeof(int2) * (size_t)p->ntiles * p->na;
     size_t free_b = 0, total_b = 0;
     if (cudaMemGetInfo(&free_b, &total_b) != cudaSuccess) return 0;
     if ((double)(b_taps + b_bpw + b_bpf) > 0.4 * (double)free_b) return 0;
-    if (cudaMalloc(&p->d_taps, b_taps) != cudaSuccess || cudaMalloc(&p->d_bpw, b_bpw) != cudaSuccess ||
-        cudaMalloc(&p->d_bpf, b_bpf) != cudaSuccess) {
+    if (cudaMalloc(&p->d_taps, sizeof(float4) * (size_t)p->ngroups * p->nrays * 4) != cudaSuccess ||
+        cudaMalloc(&p->d_xT, sizeof(float) * (size_t)p->nrays * p->ys) != cudaSuccess ||
+        cudaMalloc(&p->d_bpw, b_bpw) != cudaSuccess || cudaMalloc(&p->d_bpf, b_bpf) != cudaSuccess) {
         cudaGetLastError();  // an allocation failure is not sticky; run without tables
         cudaFree(p->d_taps);
+        cudaFree(p->d_xT);
         cudaFree(p->d_bpw);
         cudaFree(p->d_bpf);
         p->d_taps = nullptr;
+        p->d_xT = nullptr;
         p->d_bpw = nullptr;
         p->d_bpf = nullptr;
         return 0;

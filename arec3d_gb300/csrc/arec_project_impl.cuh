@@ -29,6 +29,8 @@
 // the forward projector's is a separate pass over q.
 #pragma once
 
+#include <cuda.h>  // CUtensorMap (the forward projector's row tiles)
+
 #include <climits>
 
 #include "arec_umma.cuh"
@@ -53,7 +55,13 @@ struct OpArgs {
                          // group's (up to 4) angles per ray: (iqx, w0, w1, w2)
     const float4 *bpw;   // [ntiles][na][32]: the back projector's plan entries
     const int2 *bpf;     // [ntiles][na]: footprint (first bin, bins) per tile and angle
+    const int *kinv;     // column-major ray index -> ray index
 };
+
+// A 2-D tensor map over rows of ys floats (x or its column-major copy): box =
+// box_cols slices x box_rows rays; false if the driver refuses it.
+bool encode_rows_map(CUtensorMap *m, const float *base, int ys, int nrows, int box_cols,
+                     int box_rows);
 
 template <int VEC>
 __device__ __forceinline__ void ldv(const float *__restrict__ p, float (&v)[VEC]) {
@@ -306,9 +314,9 @@ __device__ __forceinline__ int tile_lane_ray(const OpArgs &A, int2 tile, int lan
 }
 
 // Plan tables: the back projector's entries for every (tile, angle) (one warp
-// each) and the taps of every (angle group, ray, angle of the group); a
-// group's 4 slots of one ray are one 64-byte copy for the forward projector's
-// staging warp, and the rays of a line are contiguous.
+// each) and the taps of every (angle group, ray, angle of the group), the rays
+// in the group's line order (row-major for row sweeps, column-major for
+// column sweeps): the staged pixels of a line are one contiguous record.
 static_assert(kGroupAngles == 4, "the taps table holds 4 angles per group");
 template <int W, int FW>
 __global__ void __launch_bounds__(128) k_bp_table(OpArgs A, float4 *bpw, int2 *bpf) {
@@ -336,7 +344,10 @@ __global__ void __launch_bounds__(256) k_fp_taps(OpArgs A, float4 *taps) {
     const int4 G = A.groups[grp];
     float4 e = make_float4(0.f, 0.f, 0.f, 0.f);
     if (j < G.y) {
-        const Taps tp = ray_taps<W>(A.ray[k], A.ang[G.x + j], A.r_hi, A.r_lo);
+        // the group's line order: row-major rays for row sweeps, column-major
+        // for column sweeps (k here indexes that order)
+        const int kr = G.z ? A.kinv[k] : k;
+        const Taps tp = ray_taps<W>(A.ray[kr], A.ang[G.x + j], A.r_hi, A.r_lo);
         e = make_float4(__int_as_float(tp.iqx), tp.w0, tp.w1, tp.w2);
     }
     taps[t] = e;
@@ -691,7 +702,8 @@ constexpr int kFpThreads = 32 * (kGroupAngles + 1);
 template <int W, int VEC, int BT>
 __global__ void __launch_bounds__(kFpThreads, 3)
     fp_band_kernel(OpArgs A, const float *__restrict__ x, float *__restrict__ q, int g0, int ngo,
-                   int band_lo, int band_hi) {
+                   int band_lo, int band_hi, const __grid_constant__ CUtensorMap tmx,
+                   const __grid_constant__ CUtensorMap tmxT) {
     constexpr int NA = kGroupAngles, NG = BT + 2, SPAN = 32 * VEC, US = kFpStage;
     extern __shared__ __align__(128) unsigned char smem_raw[];
     __shared__ __align__(8) uint64_t full[2], empty[2];
@@ -790,23 +802,48 @@ __global__ void __launch_bounds__(kFpThreads, 3)
                 n = US;
             }
             if (!ok) n = 0;  // a wait gave up: stage nothing more
+            if (A.taps) {
+                // With the plan's tables the staged pixels of a line are
+                // consecutive rays in the line's order: one tile of US rays x
+                // SPAN slices from x (row sweeps) or its column-major copy
+                // (column sweeps), and one contiguous taps record.
+                if (lane == 0) {
+                    uinfo[2 * buf] = ulo;
+                    uinfo[2 * buf + 1] = n;
+                    __threadfence_block();  // counts before the arrival
+                    umma::mbar_arrive_expect_tx(
+                        &full[buf], n ? (uint32_t)(US * SPAN * 4 + n * 16 * NA) : 0u);
+                    if (n) {
+                        int j0;
+                        if (orient == 0) {
+                            const RowInfo ri = A.rows[li];
+                            j0 = ri.start + ulo - ri.lo;
+                        } else {
+                            const ColInfo ci = A.cols[li];
+                            j0 = ci.start + ulo - ci.lo;
+                        }
+                        umma::tma_load_2d(stg + (size_t)buf * US * SPAN, orient ? &tmxT : &tmx, yb, j0,
+                                          &full[buf]);
+                        umma::bulk_g2s(rayb + buf * US * NA,
+                                       A.taps + ((size_t)grp * A.nrays + j0) * NA,
+                                       (uint32_t)n * 16u * NA, &full[buf]);
+                    }
+                }
+                __syncwarp();
+                continue;
+            }
             const int k = lane < n ? line_pixel_ray(A, orient, li, ulo + lane) : 0;
             if (lane == 0) {
                 uinfo[2 * buf] = ulo;
                 uinfo[2 * buf + 1] = n;
                 __threadfence_block();  // counts before the arrival
-                umma::mbar_arrive_expect_tx(&full[buf],
-                                            (uint32_t)n * (row_bytes + (A.taps ? 16u * NA : 16u)));
+                umma::mbar_arrive_expect_tx(&full[buf], (uint32_t)n * (row_bytes + 16u));
             }
             __syncwarp();
             if (lane < n) {
                 umma::bulk_g2s(stg + ((size_t)buf * US + lane) * SPAN, x + (size_t)k * ys + yb,
                                row_bytes, &full[buf]);
-                if (A.taps)
-                    umma::bulk_g2s(rayb + (buf * US + lane) * NA,
-                                   A.taps + ((size_t)grp * A.nrays + k) * NA, 16u * NA, &full[buf]);
-                else
-                    umma::bulk_g2s(rayb + (buf * US + lane) * NA, A.ray + k, 16u, &full[buf]);
+                umma::bulk_g2s(rayb + (buf * US + lane) * NA, A.ray + k, 16u, &full[buf]);
             }
         }
         return;
@@ -977,6 +1014,20 @@ int launch_bp(const OpArgs &A, int vec, int nsc, dim3 grid, const float *s, floa
     return -1;
 }
 
+// x in column-major ray order: xT[j] = x[kinv[j]] (rows of ys floats).
+static __global__ void __launch_bounds__(256) k_ray_gather(const float4 *__restrict__ x,
+                                                    float4 *__restrict__ xT,
+                                                    const int *__restrict__ kinv, int nrays,
+                                                    int ys4) {
+    const size_t n = (size_t)nrays * ys4;
+    for (size_t t = (size_t)blockIdx.x * blockDim.x + threadIdx.x; t < n;
+         t += (size_t)gridDim.x * blockDim.x) {
+        const size_t j = t / ys4;
+        const int c = (int)(t - j * ys4);
+        xT[t] = x[(size_t)kinv[j] * ys4 + c];
+    }
+}
+
 // The plan's tables for weighting W (one launch each).
 template <int W>
 int launch_tables(const OpArgs &A, int ntiles, float4 *taps, float4 *bpw, int2 *bpf,
@@ -989,7 +1040,7 @@ int launch_tables(const OpArgs &A, int ntiles, float4 *taps, float4 *bpw, int2 *
 
 template <int W, int V, int BT>
 int launch_fpb_one(const OpArgs &A, dim3 grid, const float *x, float *q, int g0, int ngo, int lo,
-                   int hi, cudaStream_t st) {
+                   int hi, const CUtensorMap &tmx, const CUtensorMap &tmxT, cudaStream_t st) {
     constexpr size_t smem = fpb_smem_bytes<V>();
     static bool configured = false;  // per instantiation, once per process
     if (!configured) {
@@ -998,17 +1049,17 @@ int launch_fpb_one(const OpArgs &A, dim3 grid, const float *x, float *q, int g0,
             return -2;
         configured = true;
     }
-    fp_band_kernel<W, V, BT><<<grid, kFpThreads, smem, st>>>(A, x, q, g0, ngo, lo, hi);
+    fp_band_kernel<W, V, BT><<<grid, kFpThreads, smem, st>>>(A, x, q, g0, ngo, lo, hi, tmx, tmxT);
     return 0;
 }
 
 template <int W, int BT>
 int launch_fpb(const OpArgs &A, int vec, dim3 grid, const float *x, float *q, int g0, int ngo,
-               int lo, int hi, cudaStream_t st) {
-    if (vec == 1) return launch_fpb_one<W, 1, BT>(A, grid, x, q, g0, ngo, lo, hi, st);
-    if (vec == 2) return launch_fpb_one<W, 2, BT>(A, grid, x, q, g0, ngo, lo, hi, st);
-    if (vec == 4) return launch_fpb_one<W, 4, BT>(A, grid, x, q, g0, ngo, lo, hi, st);
-    return launch_fpb_one<W, 8, BT>(A, grid, x, q, g0, ngo, lo, hi, st);
+               int lo, int hi, const CUtensorMap &tmx, const CUtensorMap &tmxT, cudaStream_t st) {
+    if (vec == 1) return launch_fpb_one<W, 1, BT>(A, grid, x, q, g0, ngo, lo, hi, tmx, tmxT, st);
+    if (vec == 2) return launch_fpb_one<W, 2, BT>(A, grid, x, q, g0, ngo, lo, hi, tmx, tmxT, st);
+    if (vec == 4) return launch_fpb_one<W, 4, BT>(A, grid, x, q, g0, ngo, lo, hi, tmx, tmxT, st);
+    return launch_fpb_one<W, 8, BT>(A, grid, x, q, g0, ngo, lo, hi, tmx, tmxT, st);
 }
 
 // Linear weighting (scatter).

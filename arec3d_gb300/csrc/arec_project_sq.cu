@@ -9,8 +9,8 @@ int launch_bp_sq(const OpArgs &A, int vec, int nsc, dim3 grid, const float *s, f
 }
 
 int launch_fpb_sq(const OpArgs &A, int vec, dim3 grid, const float *x, float *q, int g0, int ngo,
-                int lo, int hi, cudaStream_t st) {
-    return launch_fpb<ARECGB_SQ, kFpBins>(A, vec, grid, x, q, g0, ngo, lo, hi, st);
+                int lo, int hi, const CUtensorMap &tmx, const CUtensorMap &tmxT, cudaStream_t st) {
+    return launch_fpb<ARECGB_SQ, kFpBins>(A, vec, grid, x, q, g0, ngo, lo, hi, tmx, tmxT, st);
 }
 
 int launch_tables_sq(const OpArgs &A, int ntiles, float4 *taps, float4 *bpw, int2 *bpf,

@@ -161,6 +161,14 @@ __device__ __forceinline__ void bulk_g2s(void *dst, const void *src, uint32_t by
 }
 
 // Tiled TMA loads (cp.async.bulk.tensor), completing on `mbar`.
+__device__ __forceinline__ void tma_load_2d(void *dst, const void *tmap, int c0, int c1,
+                                            uint64_t *mbar) {
+    asm volatile(
+        "cp.async.bulk.tensor.2d.shared::cluster.global.tile.mbarrier::complete_tx::bytes "
+        "[%0], [%1, {%2, %3}], [%4];\n" ::"r"(smem_addr(dst)),
+        "l"(tmap), "r"(c0), "r"(c1), "r"(smem_addr(mbar))
+        : "memory");
+}
 __device__ __forceinline__ void tma_load_3d(void *dst, const void *tmap, int c0, int c1, int c2,
                                             uint64_t *mbar) {
     asm volatile(
