@@ -7,9 +7,12 @@
 
 namespace arecgb {
 
-int launch_bp_lin(const OpArgs &, int, int, dim3, const float *, float *, cudaStream_t);
-int launch_bp_kb(const OpArgs &, int, int, dim3, const float *, float *, cudaStream_t);
-int launch_bp_sq(const OpArgs &, int, int, dim3, const float *, float *, cudaStream_t);
+int launch_bp_lin(const OpArgs &, int, int, dim3, const float *, float *, const CUtensorMap &,
+                 int, cudaStream_t);
+int launch_bp_kb(const OpArgs &, int, int, dim3, const float *, float *, const CUtensorMap &,
+                 int, cudaStream_t);
+int launch_bp_sq(const OpArgs &, int, int, dim3, const float *, float *, const CUtensorMap &,
+                 int, cudaStream_t);
 int launch_fp_lin(const OpArgs &, int, const float *, float *, cudaStream_t);
 int launch_tables_sq(const OpArgs &, int, float4 *, float4 *, int2 *, cudaStream_t);
 int launch_tables_kb(const OpArgs &, int, float4 *, float4 *, int2 *, cudaStream_t);
@@ -203,15 +206,26 @@ int back_project(const Plan *p, const float *d_s, float *d_g, double *d_norm2,
     const OpArgs A = make_args(p, d_skip);
     const int nsc = slice_chunks(p);
     dim3 grid(p->ntiles, slice_blocks(p));
+    // the footprint of an angle as one TMA tile (16 bins x the block's slices,
+    // at most 256: one slice chunk per block up to VEC 8)
+    CUtensorMap tms;
+    memset(&tms, 0, sizeof(tms));
+    const int span = 32 * bp_vec(p) * nsc;
+    int use_tma = p->weighting != ARECGB_LIN && span <= 256 &&
+                  encode_sino_map(&tms, d_s, p->ys, p->nx, p->na, span, kBpFoot);
+    {
+        const char *env = getenv("ARECGB_BP_TMA");
+        if (env && env[0] == '0') use_tma = 0;
+    }
     int rc = timing_mark(p, false, false, st);
     if (rc) return rc;
     count_launches(d_norm2 ? 2 : 1);
     if (p->weighting == ARECGB_LIN)
-        rc = launch_bp_lin(A, bp_vec(p), nsc, grid, d_s, d_g, st);
+        rc = launch_bp_lin(A, bp_vec(p), nsc, grid, d_s, d_g, tms, use_tma, st);
     else if (p->weighting == ARECGB_KB)
-        rc = launch_bp_kb(A, bp_vec(p), nsc, grid, d_s, d_g, st);
+        rc = launch_bp_kb(A, bp_vec(p), nsc, grid, d_s, d_g, tms, use_tma, st);
     else
-        rc = launch_bp_sq(A, bp_vec(p), nsc, grid, d_s, d_g, st);
+        rc = launch_bp_sq(A, bp_vec(p), nsc, grid, d_s, d_g, tms, use_tma, st);
     ARECGB_CUDA(cudaGetLastError());
     if (rc) return ARECGB_ERR_ARG;
     if (d_norm2) {

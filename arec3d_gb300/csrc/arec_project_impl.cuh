@@ -62,6 +62,10 @@ struct OpArgs {
 // box_cols slices x box_rows rays; false if the driver refuses it.
 bool encode_rows_map(CUtensorMap *m, const float *base, int ys, int nrows, int box_cols,
                      int box_rows);
+// A 3-D tensor map over a sinogram [na][nx][ys] (device layout): box =
+// box_cols slices x box_bins bins x 1 angle; false if the driver refuses it.
+bool encode_sino_map(CUtensorMap *m, const float *base, int ys, int nx, int na, int box_cols,
+                     int box_bins);
 
 template <int VEC>
 __device__ __forceinline__ void ldv(const float *__restrict__ p, float (&v)[VEC]) {
@@ -373,7 +377,8 @@ constexpr size_t bp_smem_bytes() {
 // the reference skips them.
 template <int W, int VEC, int NSC>
 __global__ void __launch_bounds__(128 * NSC + 32)
-    bp_kernel(OpArgs A, const float *__restrict__ s, float *__restrict__ g) {
+    bp_kernel(OpArgs A, const float *__restrict__ s, float *__restrict__ g,
+              const __grid_constant__ CUtensorMap tms, int use_tma) {
     constexpr int NCW = 4 * NSC, AC = kBpAngles, FW = kBpFoot, NB = kBpBuf;
     constexpr int SPAN = NSC * 32 * VEC;  // slices per block
     extern __shared__ __align__(128) unsigned char smem_raw[];
@@ -447,6 +452,19 @@ __global__ void __launch_bounds__(128 * NSC + 32)
                     !umma::mbar_wait(&empty[buf], (uint32_t)(t / NB - 1) & 1u, kFpWait)) {
                     ok = false;
                     if (lane == 0) atomicOr(A.err, 16);
+                }
+                if (use_tma) {
+                    // the footprint as one tile of FW bins x SPAN slices; bins
+                    // off the detector are outside the tensor and read as zero
+                    if (lane == 0) {
+                        const bool any = ok && fn[ai] > 0;
+                        umma::mbar_arrive_expect_tx(&full[buf], any ? (uint32_t)(FW * SPAN * 4) : 0u);
+                        if (any)
+                            umma::tma_load_3d(foot + (size_t)buf * FW * SPAN, &tms, yb, fb[ai],
+                                              a0 + ai, &full[buf]);
+                    }
+                    __syncwarp();
+                    continue;
                 }
                 const int bin = fb[ai] + lane;
                 const bool in = ok && lane < fn[ai];
@@ -986,7 +1004,8 @@ namespace arecgb {
 
 // Launch helpers, instantiated once per weighting in arec_project_{lin,kb,sq}.cu.
 template <int W, int V, int N>
-int launch_bp_one(const OpArgs &A, dim3 grid, const float *s, float *g, cudaStream_t st) {
+int launch_bp_one(const OpArgs &A, dim3 grid, const float *s, float *g, const CUtensorMap &tms,
+                  int use_tma, cudaStream_t st) {
     if constexpr (W == ARECGB_LIN) {
         bp_lin_kernel<V, N><<<grid, 128 * N, 0, st>>>(A, s, g);
     } else {
@@ -998,16 +1017,16 @@ int launch_bp_one(const OpArgs &A, dim3 grid, const float *s, float *g, cudaStre
                 return -2;
             configured = true;
         }
-        bp_kernel<W, V, N><<<grid, 128 * N + 32, smem, st>>>(A, s, g);
+        bp_kernel<W, V, N><<<grid, 128 * N + 32, smem, st>>>(A, s, g, tms, use_tma);
     }
     return 0;
 }
 
 template <int W>
 int launch_bp(const OpArgs &A, int vec, int nsc, dim3 grid, const float *s, float *g,
-              cudaStream_t st) {
+              const CUtensorMap &tms, int use_tma, cudaStream_t st) {
 #define ARECGB_BP(V, N) \
-    if (vec == V && nsc == N) return launch_bp_one<W, V, N>(A, grid, s, g, st);
+    if (vec == V && nsc == N) return launch_bp_one<W, V, N>(A, grid, s, g, tms, use_tma, st);
     ARECGB_BP(1, 1) ARECGB_BP(2, 1) ARECGB_BP(4, 1) ARECGB_BP(8, 1)
     ARECGB_BP(1, 2) ARECGB_BP(2, 2) ARECGB_BP(4, 2) ARECGB_BP(8, 2)
 #undef ARECGB_BP

@@ -4,8 +4,8 @@
 namespace arecgb {
 
 int launch_bp_sq(const OpArgs &A, int vec, int nsc, dim3 grid, const float *s, float *g,
-               cudaStream_t st) {
-    return launch_bp<ARECGB_SQ>(A, vec, nsc, grid, s, g, st);
+               const CUtensorMap &tms, int use_tma, cudaStream_t st) {
+    return launch_bp<ARECGB_SQ>(A, vec, nsc, grid, s, g, tms, use_tma, st);
 }
 
 int launch_fpb_sq(const OpArgs &A, int vec, dim3 grid, const float *x, float *q, int g0, int ngo,

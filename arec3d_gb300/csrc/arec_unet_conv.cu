@@ -323,6 +323,19 @@ bool encode_rows_map(CUtensorMap *m, const float *base, int ys, int nrows, int b
                CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
 }
 
+bool encode_sino_map(CUtensorMap *m, const float *base, int ys, int nx, int na, int box_cols,
+                     int box_bins) {
+    EncodeTiledFn enc = encode_tiled();
+    if (!enc) return false;
+    const cuuint64_t d[3] = {(cuuint64_t)ys, (cuuint64_t)nx, (cuuint64_t)na};
+    const cuuint64_t st[2] = {(cuuint64_t)ys * 4, (cuuint64_t)nx * ys * 4};
+    const cuuint32_t b[3] = {(cuuint32_t)box_cols, (cuuint32_t)box_bins, 1};
+    const cuuint32_t one[3] = {1, 1, 1};
+    return enc(m, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 3, (void *)base, d, st, b, one,
+               CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+               CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+}
+
 // Tensor maps of one convolution; false if the driver refuses them (the
 // caller then uses the gather kernel).
 static bool conv_tensor_maps(const __nv_bfloat16 *x, const __nv_bfloat16 *w, int N, int H, int Wd,
