@@ -717,12 +717,27 @@ constexpr size_t fpb_smem_bytes() {
 
 constexpr int kFpThreads = 32 * (kGroupAngles + 1);
 
+// One staged pixel's contribution to the tile: bucket GG (centre bin b0+GG-1)
+// adds w0, w1, w2 times the pixel's slices to bins GG-2, GG-1, GG of the tile.
+// GG is a constant once the caller's bucket loop is unrolled, so the
+// accumulator rows stay in registers.
+template <int VEC, int BT>
+__device__ __forceinline__ void fp_entry(float (&acc)[BT][VEC], const int GG, const float4 e,
+                                         const float *S, int lane) {
+    float v[VEC];
+    lds_lane<VEC>(S + (__float_as_int(e.x) & 255) * (32 * VEC), lane, v);
+    if (GG >= 2) fma_row<VEC>(acc[GG >= 2 ? GG - 2 : 0], e.y, v);
+    if (GG >= 1 && GG <= BT) fma_row<VEC>(acc[(GG >= 1 && GG <= BT) ? GG - 1 : 0], e.z, v);
+    if (GG <= BT - 1) fma_row<VEC>(acc[GG <= BT - 1 ? GG : 0], e.w, v);
+}
+
 template <int W, int VEC, int BT>
 __global__ void __launch_bounds__(kFpThreads, 3)
     fp_band_kernel(OpArgs A, const float *__restrict__ x, float *__restrict__ q, int g0, int ngo,
                    int band_lo, int band_hi, const __grid_constant__ CUtensorMap tmx,
                    const __grid_constant__ CUtensorMap tmxT) {
     constexpr int NA = kGroupAngles, NG = BT + 2, SPAN = 32 * VEC, US = kFpStage;
+    static_assert(NG <= 16, "two slot rows of 16 buckets per warp list");
     extern __shared__ __align__(128) unsigned char smem_raw[];
     __shared__ __align__(8) uint64_t full[2], empty[2];
     float *stg = reinterpret_cast<float *>(smem_raw);                // [2][US][SPAN]
@@ -794,11 +809,8 @@ __global__ void __launch_bounds__(kFpThreads, 3)
         }
         for (int li = L0; li <= L1; li++) {
             const int it = li - L0, buf = it & 1;
-            if (it >= 2 && ok &&
-                !umma::mbar_wait(&empty[buf], (uint32_t)((it - 2) >> 1) & 1u, kFpWait)) {
-                ok = false;
-                if (lane == 0) atomicOr(A.err, 16);
-            }
+            // The line's candidates and first ray do not depend on the
+            // buffer: they are worked out before the wait for it.
             int clo = INT_MAX, chi = INT_MIN;
             if (lane < NA && li >= q_lo && li <= q_hi) {
                 line_candidates(A, orient, cq, lq, T1, T2, r, li, clo, chi);
@@ -819,6 +831,21 @@ __global__ void __launch_bounds__(kFpThreads, 3)
                 if (lane == 0) atomicOr(A.err, 1);
                 n = US;
             }
+            int j0 = 0;
+            if (A.taps && lane == 0 && n) {
+                if (orient == 0) {
+                    const RowInfo ri = A.rows[li];
+                    j0 = ri.start + ulo - ri.lo;
+                } else {
+                    const ColInfo ci = A.cols[li];
+                    j0 = ci.start + ulo - ci.lo;
+                }
+            }
+            if (it >= 2 && ok &&
+                !umma::mbar_wait(&empty[buf], (uint32_t)((it - 2) >> 1) & 1u, kFpWait)) {
+                ok = false;
+                if (lane == 0) atomicOr(A.err, 16);
+            }
             if (!ok) n = 0;  // a wait gave up: stage nothing more
             if (A.taps) {
                 // With the plan's tables the staged pixels of a line are
@@ -832,14 +859,6 @@ __global__ void __launch_bounds__(kFpThreads, 3)
                     umma::mbar_arrive_expect_tx(
                         &full[buf], n ? (uint32_t)(US * SPAN * 4 + n * 16 * NA) : 0u);
                     if (n) {
-                        int j0;
-                        if (orient == 0) {
-                            const RowInfo ri = A.rows[li];
-                            j0 = ri.start + ulo - ri.lo;
-                        } else {
-                            const ColInfo ci = A.cols[li];
-                            j0 = ci.start + ulo - ci.lo;
-                        }
                         umma::tma_load_2d(stg + (size_t)buf * US * SPAN, orient ? &tmxT : &tmx, yb, j0,
                                           &full[buf]);
                         umma::bulk_g2s(rayb + buf * US * NA,
@@ -909,7 +928,20 @@ __global__ void __launch_bounds__(kFpThreads, 3)
         const int gprev = __shfl_up_sync(0xffffffffu, gk, 1);
         const bool run = vm == 0 || (vm >> f) == (cnt == 32 ? 0xffffffffu : (1u << cnt) - 1u);
         const bool sorted = run && !__any_sync(0xffffffffu, valid && lane > f && gk < gprev);
-        if (sorted) {
+        // Slots: with the entries in bucket order and at most two per bucket
+        // (the rule whenever pixels on a line step by >= 0.5 bin; sweep
+        // orientations keep |step| >= 0.707), entry k of bucket g goes to slot
+        // [k][g] of the warp's list, so the accumulation below walks a fixed
+        // bucket sequence without a data-dependent loop.
+        const unsigned firsts =
+            __ballot_sync(0xffffffffu, valid && (lane == f || gk != gprev));
+        const int rank = lane - (31 - __clz(firsts & ((2u << lane) - 1u)));
+        const bool slots = sorted && !__any_sync(0xffffffffu, valid && rank > 1);
+        const unsigned maskA = __reduce_or_sync(0xffffffffu, valid && rank == 0 ? 1u << gk : 0u);
+        const unsigned maskB = __reduce_or_sync(0xffffffffu, valid && rank == 1 ? 1u << gk : 0u);
+        if (slots) {
+            if (valid) list[ai * 32 + rank * 16 + gk] = ent;
+        } else if (sorted) {
             if (valid) list[ai * 32 + lane - f] = ent;
         } else {
             const unsigned key = valid ? (unsigned)gk : 64u + lane;
@@ -925,10 +957,28 @@ __global__ void __launch_bounds__(kFpThreads, 3)
         }
         __syncwarp();
         // Phase C: entries in bucket order; the bucket index is a compile-time
-        // constant.  Each entry's slices are loaded as it is reached (the
-        // other warps cover the load latency; a prefetch into a second
-        // register set cost more in register moves than it saved).
-        if (cnt) {
+        // constant.  In the slot layout a line that fills every bucket (the
+        // usual case: the strip crosses the whole line) runs as straight-line
+        // code, so the loads of later buckets overlap the FMAs of earlier ones.
+        if (slots) {
+            const float *S = stg + (size_t)buf * US * SPAN;
+            const float4 *E = list + ai * 32;
+            if (maskA == (1u << NG) - 1u) {
+#pragma unroll
+                for (int gg = 0; gg < NG; gg++) fp_entry<VEC, BT>(acc, gg, E[gg], S, lane);
+            } else {
+#pragma unroll
+                for (int gg = 0; gg < NG; gg++)
+                    if (maskA >> gg & 1u) fp_entry<VEC, BT>(acc, gg, E[gg], S, lane);
+            }
+            if (maskB) {
+#pragma unroll
+                for (int gg = 0; gg < NG; gg++)
+                    if (maskB >> gg & 1u) fp_entry<VEC, BT>(acc, gg, E[16 + gg], S, lane);
+            }
+        } else if (cnt) {
+            // Each entry's slices are loaded as it is reached (a prefetch into
+            // a second register set cost more in register moves than it saved).
             const float *S = stg + (size_t)buf * US * SPAN;
             const float4 *E = list + ai * 32;
             int i = 0;
