@@ -709,10 +709,13 @@ __device__ __forceinline__ int line_pixel_ray(const OpArgs &A, int orient, int l
 // bucket index known at compile time, and arrives on the buffer's "empty"
 // mbarrier.  No block-wide barrier inside the line loop; every wait is
 // bounded and a timeout sets an error flag.
+constexpr int kFpMaxBand = 128;  // lines per band launch at most (the staging info per line)
+
 template <int VEC>
 constexpr size_t fpb_smem_bytes() {
     return sizeof(float) * 2 * kFpStage * (32 * VEC) + sizeof(float4) * kGroupAngles * 32 +
-           sizeof(float4) * 2 * kFpStage * kGroupAngles + sizeof(int) * (2 * kGroupAngles + 4);
+           sizeof(float4) * 2 * kFpStage * kGroupAngles + sizeof(int) * (2 * kGroupAngles + 4) +
+           sizeof(int2) * kFpMaxBand;
 }
 
 constexpr int kFpThreads = 32 * (kGroupAngles + 1);
@@ -747,7 +750,12 @@ __global__ void __launch_bounds__(kFpThreads, 3)
     float4 *rayb = list + NA * 32;
     int *lrange = reinterpret_cast<int *>(rayb + 2 * US * NA);       // [NA][2]
     int *uinfo = lrange + 2 * NA;                                    // [2][2] (first pixel, rows)
+    int2 *linfo = reinterpret_cast<int2 *>(uinfo + 4);               // [band lines] (first ray, rows)
     if (A.skip && *A.skip) return;
+    if (band_hi - band_lo > kFpMaxBand) {  // the host keeps bands within kFpMaxBand lines
+        if (threadIdx.x == 0) atomicOr(A.err, 1);
+        return;
+    }
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const bool stager = warp == NA;
     const int ai = stager ? 0 : warp;
@@ -807,10 +815,89 @@ __global__ void __launch_bounds__(kFpThreads, 3)
             q_lo = lrange[2 * lane];
             q_hi = lrange[2 * lane + 1];
         }
+        if (A.taps) {
+            // With the plan's tables every line's staging (first ray of the
+            // union of the group's candidates, rows) is worked out up front,
+            // lanes = lines, so the per-line loop below carries no dependent
+            // chain of loads, divisions and shuffles.
+            float ck[NA], lk[NA];
+            int klo[NA], khi[NA];
+#pragma unroll
+            for (int i = 0; i < NA; i++) {
+                ck[i] = 1.f;
+                lk[i] = 0.f;
+                klo[i] = INT_MAX;
+                khi[i] = INT_MIN;
+                if (i < G.y) {
+                    const AngleParams aq = A.ang[G.x + i];
+                    ck[i] = orient ? aq.s : aq.c;
+                    lk[i] = orient ? aq.c : aq.s;
+                    klo[i] = lrange[2 * i];
+                    khi[i] = lrange[2 * i + 1];
+                }
+            }
+            for (int li = L0 + lane; li <= L1; li += 32) {
+                int clo = INT_MAX, chi = INT_MIN;
+#pragma unroll
+                for (int i = 0; i < NA; i++) {
+                    if (li < klo[i] || li > khi[i]) continue;
+                    int c0, c1;
+                    line_candidates(A, orient, ck[i], lk[i], T1, T2, r, li, c0, c1);
+                    if (c0 <= c1) {
+                        clo = min(clo, c0);
+                        chi = max(chi, c1);
+                    }
+                }
+                int n = chi >= clo ? chi - clo + 1 : 0;
+                if (n > US) {
+                    atomicOr(A.err, 1);
+                    n = US;
+                }
+                int j0 = 0;
+                if (n) {
+                    if (orient == 0) {
+                        const RowInfo ri = A.rows[li];
+                        j0 = ri.start + clo - ri.lo;
+                    } else {
+                        const ColInfo ci = A.cols[li];
+                        j0 = ci.start + clo - ci.lo;
+                    }
+                }
+                linfo[li - L0] = make_int2(j0, n);
+            }
+            __syncwarp();
+            for (int li = L0; li <= L1; li++) {
+                const int it = li - L0, buf = it & 1;
+                const int2 lf = linfo[it];
+                if (it >= 2 && ok &&
+                    !umma::mbar_wait(&empty[buf], (uint32_t)((it - 2) >> 1) & 1u, kFpWait)) {
+                    ok = false;
+                    if (lane == 0) atomicOr(A.err, 16);
+                }
+                // the staged pixels of a line are consecutive rays in the
+                // line's order: one tile of US rays x SPAN slices from x (row
+                // sweeps) or its column-major copy (column sweeps), and one
+                // contiguous taps record
+                const int n = ok ? lf.y : 0;  // a wait gave up: stage nothing more
+                if (lane == 0) {
+                    uinfo[2 * buf + 1] = n;
+                    __threadfence_block();  // counts before the arrival
+                    umma::mbar_arrive_expect_tx(
+                        &full[buf], n ? (uint32_t)(US * SPAN * 4 + n * 16 * NA) : 0u);
+                    if (n) {
+                        umma::tma_load_2d(stg + (size_t)buf * US * SPAN, orient ? &tmxT : &tmx, yb,
+                                          lf.x, &full[buf]);
+                        umma::bulk_g2s(rayb + buf * US * NA,
+                                       A.taps + ((size_t)grp * A.nrays + lf.x) * NA,
+                                       (uint32_t)n * 16u * NA, &full[buf]);
+                    }
+                }
+                __syncwarp();
+            }
+            return;
+        }
         for (int li = L0; li <= L1; li++) {
             const int it = li - L0, buf = it & 1;
-            // The line's candidates and first ray do not depend on the
-            // buffer: they are worked out before the wait for it.
             int clo = INT_MAX, chi = INT_MIN;
             if (lane < NA && li >= q_lo && li <= q_hi) {
                 line_candidates(A, orient, cq, lq, T1, T2, r, li, clo, chi);
@@ -831,44 +918,12 @@ __global__ void __launch_bounds__(kFpThreads, 3)
                 if (lane == 0) atomicOr(A.err, 1);
                 n = US;
             }
-            int j0 = 0;
-            if (A.taps && lane == 0 && n) {
-                if (orient == 0) {
-                    const RowInfo ri = A.rows[li];
-                    j0 = ri.start + ulo - ri.lo;
-                } else {
-                    const ColInfo ci = A.cols[li];
-                    j0 = ci.start + ulo - ci.lo;
-                }
-            }
             if (it >= 2 && ok &&
                 !umma::mbar_wait(&empty[buf], (uint32_t)((it - 2) >> 1) & 1u, kFpWait)) {
                 ok = false;
                 if (lane == 0) atomicOr(A.err, 16);
             }
             if (!ok) n = 0;  // a wait gave up: stage nothing more
-            if (A.taps) {
-                // With the plan's tables the staged pixels of a line are
-                // consecutive rays in the line's order: one tile of US rays x
-                // SPAN slices from x (row sweeps) or its column-major copy
-                // (column sweeps), and one contiguous taps record.
-                if (lane == 0) {
-                    uinfo[2 * buf] = ulo;
-                    uinfo[2 * buf + 1] = n;
-                    __threadfence_block();  // counts before the arrival
-                    umma::mbar_arrive_expect_tx(
-                        &full[buf], n ? (uint32_t)(US * SPAN * 4 + n * 16 * NA) : 0u);
-                    if (n) {
-                        umma::tma_load_2d(stg + (size_t)buf * US * SPAN, orient ? &tmxT : &tmx, yb, j0,
-                                          &full[buf]);
-                        umma::bulk_g2s(rayb + buf * US * NA,
-                                       A.taps + ((size_t)grp * A.nrays + j0) * NA,
-                                       (uint32_t)n * 16u * NA, &full[buf]);
-                    }
-                }
-                __syncwarp();
-                continue;
-            }
             const int k = lane < n ? line_pixel_ray(A, orient, li, ulo + lane) : 0;
             if (lane == 0) {
                 uinfo[2 * buf] = ulo;
