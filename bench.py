@@ -326,7 +326,7 @@ def kernels_only(args):
 
     gb.build()
     angles = syn.uniform_angles(args.angles)
-    plan = gb.Plan(gb.SQ, 0.5 * (NX - 1), args.slices, angles)
+    plan = gb.Plan(gb.SQ, 0.5 * (args.nx - 1), args.slices, angles)
     g = torch.Generator(device="cuda")
     g.manual_seed(0)
     x = torch.rand(plan.nrays, plan.ys, device="cuda", generator=g)
@@ -376,6 +376,7 @@ def main():
     ap.add_argument("--tune", action="store_true", help="--kernels-only: autotune first")
     ap.add_argument("--shapes", default="", help="--kernels-only: band,fp_vec,bp_vec,chunks")
     ap.add_argument("--angles", type=int, default=NA, help="angles for --kernels-only")
+    ap.add_argument("--nx", type=int, default=NX, help="detector bins for --kernels-only")
     ap.add_argument("--plain", action="store_true", help="plain CGLS only (no warm start)")
     ap.add_argument("--config", type=int, default=0, choices=[0, 1, 3, 5],
                     help="measure another benchmark configuration instead of the headline")
