@@ -206,7 +206,7 @@ int back_project(const Plan *p, const float *d_s, float *d_g, double *d_norm2,
     const OpArgs A = make_args(p, d_skip);
     const int nsc = slice_chunks(p);
     dim3 grid(p->ntiles, slice_blocks(p));
-    // the footprint of an angle as one TMA tile (16 bins x the block's slices,
+    // the footprint of an angle as one TMA tile (kBpFoot bins x the block's slices,
     // at most 256: one slice chunk per block up to VEC 8)
     CUtensorMap tms;
     memset(&tms, 0, sizeof(tms));

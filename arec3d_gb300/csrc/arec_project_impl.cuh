@@ -239,7 +239,7 @@ __device__ __forceinline__ void fma_row(float (&acc)[VEC], float w, const float 
 }
 
 constexpr int kBpAngles = 32;  // angles per weight chunk
-constexpr int kBpFoot = 16;    // staged footprint width in bins (an 8x4 tile spans <= 12)
+constexpr int kBpFoot = 12;    // staged footprint width in bins (an 8x4 tile spans <= 11)
 
 constexpr int kBpBuf = 3;  // footprint buffers in flight
 
@@ -360,50 +360,93 @@ __global__ void __launch_bounds__(256) k_fp_taps(OpArgs A, float4 *taps) {
 template <int VEC, int NSC>
 constexpr size_t bp_smem_bytes() {
     return sizeof(float) * kBpBuf * kBpFoot * (NSC * 32 * VEC) + sizeof(float4) * kBpAngles * 32 +
-           sizeof(int) * 2 * kBpAngles + sizeof(double) * (4 * NSC + 1);
+           sizeof(int) * 2 * kBpAngles + sizeof(double) * (4 * NSC);
+}
+
+// Stage angle ai of the chunk (footprint first bin fb, bins fn) into buffer
+// buf, completing on `full`; one whole warp calls it.  TMA: the footprint as
+// one tile of FW bins x SPAN slices (bins off the detector are outside the
+// tensor and read as zero).  Otherwise one bulk copy per bin, bins off the
+// detector zero-filled, so the accumulating warps load every row they plan.
+// `ok` false: arrive without copying (a wait gave up; nothing waits forever).
+template <int FW, int SPAN>
+__device__ __forceinline__ void bp_stage(const OpArgs &A, const float *__restrict__ s, float *dst,
+                                         uint64_t *full, const CUtensorMap *tms, bool use_tma,
+                                         int angle, int fb, int fn, int yb, uint32_t row_bytes,
+                                         bool ok, int lane) {
+    // order this block's earlier generic reads of the buffer before the copy
+    asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
+    if (use_tma) {
+        if (lane == 0) {
+            const bool any = ok && fn > 0;
+            umma::mbar_arrive_expect_tx(full, any ? (uint32_t)(FW * SPAN * 4) : 0u);
+            if (any) umma::tma_load_3d(dst, tms, yb, fb, angle, full);
+        }
+        __syncwarp();
+        return;
+    }
+    const size_t ys = (size_t)A.ys;
+    const int bin = fb + lane;
+    const bool in = ok && lane < fn;
+    const bool on = in && (unsigned)bin < (unsigned)A.nx;
+    const unsigned m = __ballot_sync(0xffffffffu, on);
+    unsigned off = __ballot_sync(0xffffffffu, in && !on);
+    if (off) {
+        for (; off; off &= off - 1) {
+            float4 *z = reinterpret_cast<float4 *>(dst + (size_t)(__ffs(off) - 1) * SPAN);
+            for (int c = lane; c < SPAN / 4; c += 32) z[c] = make_float4(0.f, 0.f, 0.f, 0.f);
+        }
+        // order these generic stores before later bulk copies into the rows
+        asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
+    }
+    __syncwarp();  // zero rows written before the arrival (release)
+    if (lane == 0) umma::mbar_arrive_expect_tx(full, (uint32_t)__popc(m) * row_bytes);
+    __syncwarp();
+    if (on)
+        umma::bulk_g2s(dst + (size_t)lane * SPAN, s + ((size_t)angle * A.nx + bin) * ys + yb,
+                       row_bytes, full);
 }
 
 // Square-pixel and Kaiser-Bessel weightings.  Block = 4*NSC accumulating warps
-// (8 rays x 32*VEC slices each) + 1 staging warp.  Per chunk of 32 angles the
-// weights of the tile's 32 rays are computed once (lanes = rays) into shared
-// memory; then the staging warp copies the footprint of each angle (the bins
-// the tile's taps reach, <= 16, each a contiguous row of the block's slices)
-// with one bulk copy per bin (cp.async.bulk) into one of three buffers, two
-// angles ahead, completing on the buffer's "full" mbarrier, and the
-// accumulating warps release buffers on its "empty" mbarrier: no block-wide
-// barrier per angle.  Each accumulating warp walks its 8 rays through a
+// (8 rays x 32*VEC slices each).  Per chunk of 32 angles the tile's ray plans
+// (lanes = rays) are copied from the plan table (or computed) into shared
+// memory; the footprint of each angle (the bins the tile's taps reach, <= 12,
+// each a row of the block's slices) is staged into one of three buffers:
+// warp 0 primes the first three angles of the chunk, and the warp that
+// releases a buffer last (a shared counter per buffer) refills it with the
+// angle three ahead, completing on the buffer's "full" mbarrier.  No staging
+// warp, so 4 blocks fit per SM.  Each warp walks its 8 rays through a
 // three-row register ring (one shared-memory row read per ray instead of
-// three).  Bins off the detector are not copied and their taps add nothing, as
-// the reference skips them.
+// three).  Bins off the detector add nothing, as the reference skips them.
 template <int W, int VEC, int NSC>
-__global__ void __launch_bounds__(128 * NSC + 32)
+__global__ void __launch_bounds__(128 * NSC, NSC == 1 ? 4 : 1)
     bp_kernel(OpArgs A, const float *__restrict__ s, float *__restrict__ g,
               const __grid_constant__ CUtensorMap tms, int use_tma) {
     constexpr int NCW = 4 * NSC, AC = kBpAngles, FW = kBpFoot, NB = kBpBuf;
     constexpr int SPAN = NSC * 32 * VEC;  // slices per block
     extern __shared__ __align__(128) unsigned char smem_raw[];
-    __shared__ __align__(8) uint64_t full[NB], empty[NB];
+    __shared__ __align__(8) uint64_t full[NB];
+    __shared__ int released[NB];  // warps done with the buffer, cumulative
     float *foot = reinterpret_cast<float *>(smem_raw);               // [NB][FW][SPAN]
     float4 *sw = reinterpret_cast<float4 *>(foot + NB * FW * SPAN);  // [AC][32]
     int *fb = reinterpret_cast<int *>(sw + AC * 32);                 // [AC] first bin
     int *fn = fb + AC;                                               // [AC] bins spanned
-    double *red = reinterpret_cast<double *>(fn + AC);               // [NCW + 1]
+    double *red = reinterpret_cast<double *>(fn + AC);               // [NCW]
     if (A.skip && *A.skip) return;
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const bool stager = warp == NCW;
     const int k = tile_lane_ray(A, A.tiles[blockIdx.x], lane);
     const float4 myray = k >= 0 && !A.bpw ? A.ray[k] : make_float4(0.f, 0.f, 0.f, 0.f);
     const int rg = warp & 3, sc = warp >> 2;
     const int yb = blockIdx.y * SPAN;                  // first slice of the block
     const int yw = sc * 32 * VEC;                        // this warp's slices within the block
-    const bool yok = !stager && yb + yw + lane_piece<VEC>(lane, 0) < A.ys;
+    const bool yok = yb + yw + lane_piece<VEC>(lane, 0) < A.ys;
     const size_t ys = (size_t)A.ys;
     const uint32_t row_bytes = (uint32_t)min(SPAN, A.ys - yb) * 4u;
     if (threadIdx.x == 0) {
 #pragma unroll
         for (int b = 0; b < NB; b++) {
             umma::mbar_init(&full[b], 1);
-            umma::mbar_init(&empty[b], NCW);
+            released[b] = 0;
         }
         umma::mbar_fence_init();
     }
@@ -430,7 +473,7 @@ __global__ void __launch_bounds__(128 * NSC + 32)
             }
             cp_async_wait<0>();
         } else {
-            for (int ai = warp; ai < AC; ai += NCW + 1) {
+            for (int ai = warp; ai < AC; ai += NCW) {
                 const int a = a0 + ai;
                 int f0, f1;
                 bool wide;
@@ -444,113 +487,78 @@ __global__ void __launch_bounds__(128 * NSC + 32)
                 }
             }
         }
-        __syncthreads();  // weights and footprint bases of this chunk (barriers initialised)
-        if (stager) {
-            for (int ai = 0; ai < nac; ai++) {
-                const int t = t0 + ai, buf = t % NB;
-                if (t >= NB && ok &&
-                    !umma::mbar_wait(&empty[buf], (uint32_t)(t / NB - 1) & 1u, kFpWait)) {
-                    ok = false;
-                    if (lane == 0) atomicOr(A.err, 16);
-                }
-                if (use_tma) {
-                    // the footprint as one tile of FW bins x SPAN slices; bins
-                    // off the detector are outside the tensor and read as zero
-                    if (lane == 0) {
-                        const bool any = ok && fn[ai] > 0;
-                        umma::mbar_arrive_expect_tx(&full[buf], any ? (uint32_t)(FW * SPAN * 4) : 0u);
-                        if (any)
-                            umma::tma_load_3d(foot + (size_t)buf * FW * SPAN, &tms, yb, fb[ai],
-                                              a0 + ai, &full[buf]);
-                    }
-                    __syncwarp();
-                    continue;
-                }
-                const int bin = fb[ai] + lane;
-                const bool in = ok && lane < fn[ai];
-                const bool on = in && (unsigned)bin < (unsigned)A.nx;
-                const unsigned m = __ballot_sync(0xffffffffu, on);
-                // bins of the footprint off the detector (the cylinder's edge):
-                // zero rows, so the accumulating warps load every row they plan
-                unsigned off = __ballot_sync(0xffffffffu, in && !on);
-                if (off) {
-                    for (; off; off &= off - 1) {
-                        float4 *z = reinterpret_cast<float4 *>(
-                            foot + ((size_t)buf * FW + (__ffs(off) - 1)) * SPAN);
-                        for (int c = lane; c < SPAN / 4; c += 32) z[c] = make_float4(0.f, 0.f, 0.f, 0.f);
-                    }
-                    // order these generic stores before later bulk copies into the rows
-                    asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
-                }
-                __syncwarp();  // zero rows written before the arrival (release)
-                if (lane == 0) umma::mbar_arrive_expect_tx(&full[buf], (uint32_t)__popc(m) * row_bytes);
-                __syncwarp();
-                if (on)
-                    umma::bulk_g2s(foot + ((size_t)buf * FW + lane) * SPAN,
-                                   s + ((size_t)(a0 + ai) * A.nx + bin) * ys + yb, row_bytes,
-                                   &full[buf]);
-            }
-        } else {
-            for (int ai = 0; ai < nac; ai++) {
-                const int t = t0 + ai, buf = t % NB;
-                if (ok && !umma::mbar_wait(&full[buf], (uint32_t)(t / NB) & 1u, kFpWait)) {
-                    ok = false;
-                    if (lane == 0) atomicOr(A.err, 16);
-                }
-                if (ok && yok) {
-                    const float *F = foot + (size_t)buf * FW * SPAN + yw;
-                    // the ring (slots 0, 1, 2); a warp's first used ray loads all three
-                    float R0[VEC], R1[VEC], R2[VEC];
-#pragma unroll
-                    for (int r = 0; r < 8; r++) {
-                        const float4 e = sw[ai * 32 + rg * 8 + r];
-                        const int code = __float_as_int(e.x), act = code & 3;
-                        if (act == 0) continue;
-                        const float *row = F + (code >> 8) * SPAN;
-                        if (act == 2) {
-                            const int slot = (code >> 2) & 3;
-                            if (slot == 0)
-                                lds_lane<VEC>(row, lane, R0);
-                            else if (slot == 1)
-                                lds_lane<VEC>(row, lane, R1);
-                            else
-                                lds_lane<VEC>(row, lane, R2);
-                        } else if (act == 3) {
-                            lds_lane<VEC>(row, lane, R0);
-                            lds_lane<VEC>(row + SPAN, lane, R1);
-                            lds_lane<VEC>(row + 2 * SPAN, lane, R2);
-                        }
-                        fma_row<VEC>(acc[r], e.y, R0);
-                        fma_row<VEC>(acc[r], e.z, R1);
-                        fma_row<VEC>(acc[r], e.w, R2);
-                    }
-                }
-                __syncwarp();
-                if (lane == 0) umma::mbar_arrive(&empty[buf]);
+        __syncthreads();  // plans and footprint bases of this chunk (barriers initialised)
+        if (warp == 0) {
+            for (int ai = 0; ai < min(NB, nac); ai++) {
+                const int buf = (t0 + ai) % NB;
+                bp_stage<FW, SPAN>(A, s, foot + (size_t)buf * FW * SPAN, &full[buf], &tms,
+                                   use_tma != 0, a0 + ai, fb[ai], fn[ai], yb, row_bytes, ok, lane);
             }
         }
+        for (int ai = 0; ai < nac; ai++) {
+            const int t = t0 + ai, buf = t % NB;
+            if (ok && !umma::mbar_wait(&full[buf], (uint32_t)(t / NB) & 1u, kFpWait)) {
+                ok = false;
+                if (lane == 0) atomicOr(A.err, 16);
+            }
+            if (ok && yok) {
+                const float *F = foot + (size_t)buf * FW * SPAN + yw;
+                // the ring (slots 0, 1, 2); a warp's first used ray loads all three
+                float R0[VEC], R1[VEC], R2[VEC];
+#pragma unroll
+                for (int r = 0; r < 8; r++) {
+                    const float4 e = sw[ai * 32 + rg * 8 + r];
+                    const int code = __float_as_int(e.x), act = code & 3;
+                    if (act == 0) continue;
+                    const float *row = F + (code >> 8) * SPAN;
+                    if (act == 2) {
+                        const int slot = (code >> 2) & 3;
+                        if (slot == 0)
+                            lds_lane<VEC>(row, lane, R0);
+                        else if (slot == 1)
+                            lds_lane<VEC>(row, lane, R1);
+                        else
+                            lds_lane<VEC>(row, lane, R2);
+                    } else if (act == 3) {
+                        lds_lane<VEC>(row, lane, R0);
+                        lds_lane<VEC>(row + SPAN, lane, R1);
+                        lds_lane<VEC>(row + 2 * SPAN, lane, R2);
+                    }
+                    fma_row<VEC>(acc[r], e.y, R0);
+                    fma_row<VEC>(acc[r], e.z, R1);
+                    fma_row<VEC>(acc[r], e.w, R2);
+                }
+            }
+            __syncwarp();  // this warp's reads of the buffer are done
+            // the last of the NCW warps to release the buffer refills it
+            int last = 0;
+            if (lane == 0) last = (atomicAdd(&released[buf], 1) + 1) % NCW == 0;
+            last = __shfl_sync(0xffffffffu, last, 0);
+            if (last && ai + NB < nac)
+                bp_stage<FW, SPAN>(A, s, foot + (size_t)buf * FW * SPAN, &full[buf], &tms,
+                                   use_tma != 0, a0 + ai + NB, fb[ai + NB], fn[ai + NB], yb,
+                                   row_bytes, ok, lane);
+        }
         t0 += nac;
-        __syncthreads();  // the chunk's weights are no longer read
+        __syncthreads();  // the chunk's plans are no longer read
     }
-    if (!ok && !stager) {
+    if (!ok) {
         // a wait gave up: let the copies still in flight land before the block exits
         for (int t = max(0, t0 - NB); t < t0; t++)
             umma::mbar_wait(&full[t % NB], (uint32_t)(t / NB) & 1u, kFpWait);
     }
 
     double s2 = 0.0;
-    if (!stager) {
 #pragma unroll
-        for (int r = 0; r < 8; r++) {
-            const int kr = __shfl_sync(0xffffffffu, k, rg * 8 + r);
-            if (kr >= 0 && yok) {
-                stg_lane<VEC>(g + (size_t)kr * ys + yb + yw, lane, acc[r], A.ys - (yb + yw));
+    for (int r = 0; r < 8; r++) {
+        const int kr = __shfl_sync(0xffffffffu, k, rg * 8 + r);
+        if (kr >= 0 && yok) {
+            stg_lane<VEC>(g + (size_t)kr * ys + yb + yw, lane, acc[r], A.ys - (yb + yw));
 #pragma unroll
-                for (int q = 0; q < VEC; q++) s2 += (double)__fmul_rn(acc[r][q], acc[r][q]);
-            }
+            for (int q = 0; q < VEC; q++) s2 += (double)__fmul_rn(acc[r][q], acc[r][q]);
         }
     }
-    block_sum_to<NCW + 1>(s2, red, A.partials + (size_t)blockIdx.y * gridDim.x + blockIdx.x);
+    block_sum_to<NCW>(s2, red, A.partials + (size_t)blockIdx.y * gridDim.x + blockIdx.x);
 }
 
 // Linear weighting: its ray coordinates are the reference's shifted table
@@ -1122,7 +1130,7 @@ int launch_bp_one(const OpArgs &A, dim3 grid, const float *s, float *g, const CU
                 return -2;
             configured = true;
         }
-        bp_kernel<W, V, N><<<grid, 128 * N + 32, smem, st>>>(A, s, g, tms, use_tma);
+        bp_kernel<W, V, N><<<grid, 128 * N, smem, st>>>(A, s, g, tms, use_tma);
     }
     return 0;
 }
