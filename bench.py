@@ -545,8 +545,13 @@ def main():
         b_dev = torch.empty_like(b)
         x_dev = torch.zeros_like(x)
 
+        ev = [torch.cuda.Event(enable_timing=True) for _ in range(4)]
+        copy_ms = [0.0, 0.0]
+
         def e2e_step():
+            ev[0].record(stream)
             b_ref.copy_(b_host, non_blocking=True)
+            ev[1].record(stream)
             plan.sino_from_reference(b_ref, b_dev, stream=stream)
             if net is not None:
                 _, sinfo = plan.sirt(b_dev, x_dev, lam, sirt_iters, 0.0, stream=stream)
@@ -555,10 +560,15 @@ def main():
                           stream=stream)
             else:
                 plan.cgls(b_dev, x_dev, MAXIT, TOL, stream=stream)
+            ev[2].record(stream)
             x_host.copy_(x_dev, non_blocking=True)
+            ev[3].record(stream)
             torch.cuda.synchronize()
+            copy_ms[0] += ev[0].elapsed_time(ev[1])
+            copy_ms[1] += ev[2].elapsed_time(ev[3])
 
         e2e_step()
+        copy_ms[0] = copy_ms[1] = 0.0
         n_e2e = max(1, min(args.steps, 2))
         torch.cuda.synchronize()
         t0 = time.perf_counter()
@@ -568,6 +578,7 @@ def main():
         e2e = {"value": world * NY / dt, "unit": "slices/s",
                "h2d_bytes_per_step": NA * NY * NX * 4,
                "d2h_bytes_per_step": plan.nrays * plan.ys * 4, "ms_per_step": dt * 1e3,
+               "h2d_ms": copy_ms[0] / n_e2e, "d2h_ms": copy_ms[1] / n_e2e,
                "path": "pinned host sinogram [angle][slice][bin] -> arecgb_sino_from_reference "
                        "-> " + ("arecgb_sirt -> arecgb_warm_start -> arecgb_cgls" if net is not None
                                 else "arecgb_cgls") + " -> pinned host volume"}
