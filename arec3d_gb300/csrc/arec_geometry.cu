@@ -294,6 +294,15 @@ void plan_destroy(Plan *p) {
     cudaFree(p->d_stage);
     if (p->h_pinned) cudaFreeHost(p->h_pinned);
     if (p->stream) cudaStreamDestroy(p->stream);
+    if (p->solve_stream) cudaStreamSynchronize(p->solve_stream);
+    for (cudaStream_t x : p->solve_bs) cudaStreamDestroy(x);
+    if (p->solve_stream) cudaStreamDestroy(p->solve_stream);
+    for (cudaEvent_t x : p->solve_ev) cudaEventDestroy(x);
+    cudaFree(p->d_sred);
+    if (p->h_sred) cudaFreeHost(p->h_sred);
+    cudaFree(p->d_cstate);
+    if (p->h_cstate) cudaFreeHost(p->h_cstate);
+    cudaFree(p->d_chist);
     if (cur != p->device) cudaSetDevice(cur);
     delete p;
 }

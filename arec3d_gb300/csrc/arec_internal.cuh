@@ -103,6 +103,20 @@ struct Plan {
 
     cudaStream_t stream = nullptr; // plan-owned stream for the compatible entry points
 
+    // solver scratch, allocated on first use and kept (no allocation or
+    // free, and so no device synchronisation, per solve): SIRT's reduction
+    // partials and its two pinned results; the CGLS driver's per-problem
+    // state (device and pinned copy), residual history, stream, events and
+    // branch streams (a batch keeps them in its first plan)
+    double *d_sred = nullptr, *h_sred = nullptr;
+    void *d_cstate = nullptr, *h_cstate = nullptr;
+    size_t cstate_bytes = 0;
+    double *d_chist = nullptr;
+    size_t chist_bytes = 0;
+    cudaStream_t solve_stream = nullptr;
+    std::vector<cudaEvent_t> solve_ev;
+    std::vector<cudaStream_t> solve_bs;
+
     // optional projector timing: CUDA events around every forward / back
     // projection (arecgb_plan_timing); pairs are reused across calls
     mutable bool timing = false;

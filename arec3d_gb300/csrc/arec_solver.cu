@@ -476,21 +476,49 @@ int cgls_batch(Plan *const *plans, const float *const *d_b, float *const *d_x, c
         return cgls_iteration(p, S + i, hist + (size_t)i * cap, d_x[i], p->d_sin[0], p->d_sin[1],
                               p->d_vol[0], p->d_vol[1], p->d_vol[2], d_w ? d_w[i] : nullptr, s_);
     };
-    cudaError_t e = cudaMalloc(&S, sizeof(SolveState) * n);
-    if (e == cudaSuccess) e = cudaMalloc(&hist, sizeof(double) * n * (size_t)cap);
-    if (e == cudaSuccess) e = cudaMallocHost(&H, sizeof(SolveState) * n);
-    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking);
-    for (int i = 0; e == cudaSuccess && i < n + 2; i++) {
+    // state, history, stream and events from the first plan's solver
+    // scratch, grown when this batch needs more
+    Plan *q0 = plans[0];
+    cudaError_t e = cudaSuccess;
+    const size_t s_bytes = sizeof(SolveState) * n, h_bytes = sizeof(double) * n * (size_t)cap;
+    if (q0->cstate_bytes < s_bytes) {
+        cudaFree(q0->d_cstate);
+        if (q0->h_cstate) cudaFreeHost(q0->h_cstate);
+        q0->d_cstate = q0->h_cstate = nullptr;
+        q0->cstate_bytes = 0;
+        e = cudaMalloc(&q0->d_cstate, s_bytes);
+        if (e == cudaSuccess) e = cudaMallocHost(&q0->h_cstate, s_bytes);
+        if (e == cudaSuccess) q0->cstate_bytes = s_bytes;
+    }
+    if (e == cudaSuccess && q0->chist_bytes < h_bytes) {
+        cudaFree(q0->d_chist);
+        q0->d_chist = nullptr;
+        q0->chist_bytes = 0;
+        e = cudaMalloc(&q0->d_chist, h_bytes);
+        if (e == cudaSuccess) q0->chist_bytes = h_bytes;
+    }
+    if (e == cudaSuccess && !q0->solve_stream)
+        e = cudaStreamCreateWithFlags(&q0->solve_stream, cudaStreamNonBlocking);
+    while (e == cudaSuccess && (int)q0->solve_ev.size() < n + 2) {
         cudaEvent_t x;
         e = cudaEventCreateWithFlags(&x, cudaEventDisableTiming);
-        if (e == cudaSuccess) ev.push_back(x);
+        if (e == cudaSuccess) q0->solve_ev.push_back(x);
     }
-    for (int i = 0; e == cudaSuccess && n > 1 && i < n; i++) {
+    while (e == cudaSuccess && n > 1 && (int)q0->solve_bs.size() < n) {
         cudaStream_t x;
         e = cudaStreamCreateWithFlags(&x, cudaStreamNonBlocking);
-        if (e == cudaSuccess) bs.push_back(x);
+        if (e == cudaSuccess) q0->solve_bs.push_back(x);
     }
-    if (e != cudaSuccess) fail(e, "setup");
+    if (e == cudaSuccess) {
+        S = static_cast<SolveState *>(q0->d_cstate);
+        H = static_cast<SolveState *>(q0->h_cstate);
+        hist = q0->d_chist;
+        cs = q0->solve_stream;
+        ev.assign(q0->solve_ev.begin(), q0->solve_ev.begin() + (n + 2));
+        if (n > 1) bs.assign(q0->solve_bs.begin(), q0->solve_bs.begin() + n);
+    } else {
+        fail(e, "setup");
+    }
     // the solve runs on cs, ordered after the caller's stream
     if (!rc) {
         e = cudaEventRecord(ev[0], st);
@@ -619,13 +647,7 @@ int cgls_batch(Plan *const *plans, const float *const *d_b, float *const *d_x, c
     }
     if (exec) cudaGraphExecDestroy(exec);
     if (graph) cudaGraphDestroy(graph);
-    cudaStreamSynchronize(cs);
-    for (cudaStream_t x : bs) cudaStreamDestroy(x);
-    if (cs) cudaStreamDestroy(cs);
-    for (cudaEvent_t x : ev) cudaEventDestroy(x);
-    cudaFree(S);
-    cudaFree(hist);
-    if (H) cudaFreeHost(H);
+    if (cs) cudaStreamSynchronize(cs);  // the scratch is reused by the next solve
     return rc;
 }
 
@@ -674,13 +696,13 @@ int sirt(Plan *p, const float *d_b, float *d_x, float lam, int maxit, float tol,
     if (rc) return rc;
     const size_t nv = vol_floats(p);
     float *bvol = p->d_vol[0], *pvol = p->d_vol[1], *grad = p->d_vol[2], *proj = p->d_sin[0];
-    double *red = nullptr, *h_red = nullptr;
-    ARECGB_CUDA(cudaMalloc(&red, sizeof(double) * (2 * kRedBlocks + 2)));
-    if (cudaMallocHost(&h_red, sizeof(double) * 2) != cudaSuccess) {
-        cudaFree(red);
+    if (!p->d_sred) ARECGB_CUDA(cudaMalloc(&p->d_sred, sizeof(double) * (2 * kRedBlocks + 2)));
+    if (!p->h_sred && cudaMallocHost(&p->h_sred, sizeof(double) * 2) != cudaSuccess) {
+        p->h_sred = nullptr;
         set_error("sirt: pinned allocation failed");
         return ARECGB_ERR_NOMEM;
     }
+    double *red = p->d_sred, *h_red = p->h_sred;
     double relnrm0 = 1.00001, bnorm2 = 0.0, bnorm = 0.0, atb_norm = 0.0, rel_last = 0.0;
     int restarts = 0, iter = 1, count = 0;
     const int nblk = std::min(kRedBlocks, grid_for(nv, 8));
@@ -768,8 +790,6 @@ int sirt(Plan *p, const float *d_b, float *d_x, float lam, int maxit, float tol,
         info->rnorm0 = atb_norm;  // ||A^T b||: the CGLS denominator for a warm start
         info->rel_final = rel_last;
     }
-    cudaFree(red);
-    cudaFreeHost(h_red);
     return rc;
 }
 
