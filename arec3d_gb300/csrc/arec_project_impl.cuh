@@ -707,16 +707,20 @@ __device__ __forceinline__ int line_pixel_ray(const OpArgs &A, int orient, int l
 // depend on timing.
 //
 // Block = 4 angle warps + 1 staging warp.  The staging warp runs up to two
-// lines ahead: per line it forms the union of the group's candidate pixels,
-// looks up their rays and stages their x rows and ray-table entries with one
-// bulk copy each (cp.async.bulk) into one of two buffers, completing on that
-// buffer's "full" mbarrier.  Each angle warp computes its weights for the staged rows (lanes =
-// rows, ordered by increasing centre bin), compacts the rows whose centre bin
-// falls in the tile (a contiguous run: the centre bin is monotonic along a
-// line; a counting sort covers any exception), accumulates them with the
-// bucket index known at compile time, and arrives on the buffer's "empty"
-// mbarrier.  No block-wide barrier inside the line loop; every wait is
-// bounded and a timeout sets an error flag.
+// lines ahead: per line it stages the union of the group's candidate pixels
+// into one of two buffers, completing on that buffer's "full" mbarrier.  With
+// the plan's tables the pixels of a line are consecutive rays in the line's
+// order, so the line is one 2-D TMA tile of x (or of its column-major copy)
+// plus one bulk copy of their taps, and every line's staging is worked out
+// before the line loop (lanes = lines); without tables, one bulk copy per
+// pixel row and ray-table entry.  Each angle warp takes the taps of the
+// staged rows (lanes = rows, ordered by increasing centre bin), compacts the
+// rows whose centre bin falls in the tile (a contiguous run: the centre bin
+// is monotonic along a line; a counting sort covers any exception) into
+// per-bucket slots, accumulates them with the bucket index known at compile
+// time (straight-line code when every bucket holds an entry), and arrives on
+// the buffer's "empty" mbarrier.  No block-wide barrier inside the line loop;
+// every wait is bounded and a timeout sets an error flag.
 constexpr int kFpMaxBand = 128;  // lines per band launch at most (the staging info per line)
 
 template <int VEC>
