@@ -125,3 +125,30 @@ def test_no_cpu_fallback(tmp_path, monkeypatch):
     monkeypatch.setattr(arec3d_gb300, "_lib", None)
     with pytest.raises(RuntimeError):
         arec3d_gb300.lib()
+
+
+def test_argument_errors_before_any_device_call(lib):
+    """Invalid arguments come back as ARECGB_ERR_ARG with a message, checked
+    before the library touches a device (so this runs without a GPU)."""
+    L = lib.lib()
+    ERR_ARG = -90
+    vp, fp = C.c_void_p, C.POINTER(C.c_float)
+    ang = np.zeros(4, np.float32)
+    angp = ang.ctypes.data_as(fp)
+    plan = vp()
+    for w, radius, ny, na, a in ((0, 10.0, 4, 4, angp), (4, 10.0, 4, 4, angp),
+                                 (3, -1.0, 4, 4, angp), (3, 9000.0, 4, 4, angp),
+                                 (3, 10.0, 0, 4, angp), (3, 10.0, 4, 0, angp),
+                                 (3, 10.0, 4, 4, None)):
+        assert L.arecgb_plan_create(C.byref(plan), w, radius, ny, na, a) == ERR_ARG
+        assert not plan.value
+        assert L.arecgb_last_error().decode().startswith("plan_create:")
+    assert L.arecgb_plan_create(None, 3, 10.0, 4, 4, angp) == ERR_ARG
+    ip = C.POINTER(C.c_int)
+    n = C.c_int()
+    assert L.arecgb_plan_info(None, C.byref(n), C.byref(n), C.byref(n)) == ERR_ARG
+    assert L.arecgb_plan_shapes(None, None, None, None, None) == ERR_ARG
+    assert L.arecgb_plan_set_shapes(None, 64, 8, 8, 1) == ERR_ARG
+    assert L.arecgb_plan_table_bytes(None) == 0
+    L.arecgb_cgls_batch.argtypes = [vp, vp, vp, ip, C.c_int, C.c_int, C.c_float, vp, vp, vp]
+    assert L.arecgb_cgls_batch(None, None, None, None, 0, 10, 1e-3, None, None, None) == ERR_ARG
