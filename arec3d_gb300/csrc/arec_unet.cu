@@ -1,8 +1,8 @@
 // Learned warm start: a BF16 4-level U-Net (32 base channels, FP32
 // accumulation and master weights) mapping an early reconstruction of a slice
 // (few-iteration SIRT) to an initial guess for CGLS.  The reference has no
-// counterpart; plain CGLS continuing from the guess is unchanged and remains
-// the judge of the result.
+// counterpart; plain CGLS continuing from the guess is unchanged and still
+// decides the result.
 //
 // Architecture (NHWC, bf16 activations, every 3x3 conv with bias + ReLU):
 //   level 0 (H x W):    c1a 1->32 (CUDA cores), c1b 32->32               = e1

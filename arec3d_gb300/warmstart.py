@@ -7,8 +7,8 @@ a few SIRT iterations (the network input, cheap) and many CGLS iterations (the
 target).  Images are the cylinder's slices on a zero-padded square grid,
 normalised by the RMS of the SIRT volume over the cylinder, the normalisation
 arecgb_warm_start applies at inference.  Plain CGLS then continues from the
-network's output to the same residual tolerance, so the solver stays the judge
-of the result (and the fallback: a bad guess costs iterations, not accuracy).
+network's output to the same residual tolerance, so the solver still decides
+the result (and is the fallback: a bad guess costs iterations, not accuracy).
 
 torch is used only to hold device memory and pick training crops.
 
