@@ -59,11 +59,11 @@ struct OpArgs {
 };
 
 // A 2-D tensor map over rows of ys floats (x or its column-major copy): box =
-// box_cols slices x box_rows rays; false if the driver refuses it.
+// box_cols slices x box_rows rays; false if the CUDA driver refuses it.
 bool encode_rows_map(CUtensorMap *m, const float *base, int ys, int nrows, int box_cols,
                      int box_rows);
 // A 3-D tensor map over a sinogram [na][nx][ys] (device layout): box =
-// box_cols slices x box_bins bins x 1 angle; false if the driver refuses it.
+// box_cols slices x box_bins bins x 1 angle; false if the CUDA driver refuses it.
 bool encode_sino_map(CUtensorMap *m, const float *base, int ys, int nx, int na, int box_cols,
                      int box_bins);
 

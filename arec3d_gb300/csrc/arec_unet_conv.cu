@@ -336,7 +336,7 @@ bool encode_sino_map(CUtensorMap *m, const float *base, int ys, int nx, int na, 
                CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
 }
 
-// Tensor maps of one convolution; false if the driver refuses them (the
+// Tensor maps of one convolution; false if the CUDA driver refuses them (the
 // caller then uses the gather kernel).
 static bool conv_tensor_maps(const __nv_bfloat16 *x, const __nv_bfloat16 *w, int N, int H, int Wd,
                              int Cin, int Cout, CUtensorMap *tx, CUtensorMap *tw) {
