@@ -160,6 +160,9 @@ def lib():
         for n in ("arecgb_unet_images_from_volume", "arecgb_unet_images_to_volume"):
             getattr(L, n).argtypes = [vp, vp, vp, C.c_int, C.c_int, C.c_int, C.c_float, vp]
         L.arecgb_warm_start.argtypes = [vp, vp, vp, vp, vp, vp, vp]
+        L.arecgb_unet_shape.argtypes = [vp, ip, ip, ip]
+        L.arecgb_reconstruct_host.argtypes = [vp, vp, vp, vp, C.c_int, C.c_float, C.c_int,
+                                              C.c_float, C.POINTER(SolveInfo), vp]
         L.arecgb_plan_timing.argtypes = [vp, C.c_int, dp, C.POINTER(C.c_longlong), dp,
                                          C.POINTER(C.c_longlong)]
         L.arecgb_launch_count.restype = C.c_longlong
@@ -321,6 +324,27 @@ class Plan:
         _check(lib().arecgb_sino_to_reference(_ptr(dev), _ptr(ref), self.nangles, self.ny,
                                               self.nx, self.ys, _stream(stream)),
                "arecgb_sino_to_reference")
+
+    def reconstruct_host(self, b_host, x_host, net=None, sirt_iters=0, sirt_lam=0.0,
+                         maxit=200, tol=1e-3, stream=None):
+        """One reconstruction over host buffers in the reference's layouts
+        (arecgb_reconstruct_host): b_host [nangles][ny][nx] and x_host
+        [nrays][ny] float32, as pointers or CPU tensors / arrays (page-locked
+        memory copies at full speed).  With `net`: SIRT -> warm start -> CGLS;
+        without: CGLS from zero.  Returns the CGLS SolveInfo."""
+        def hp(a):
+            if isinstance(a, int):
+                return a
+            if hasattr(a, "data_ptr"):
+                return a.data_ptr()
+            return a.ctypes.data
+        info = SolveInfo()
+        _check(lib().arecgb_reconstruct_host(self._h, hp(b_host), hp(x_host),
+                                             net._h if net is not None else None,
+                                             int(sirt_iters), float(sirt_lam), int(maxit),
+                                             float(tol), C.byref(info), _stream(stream)),
+               "arecgb_reconstruct_host")
+        return info
 
 
 class UNet:

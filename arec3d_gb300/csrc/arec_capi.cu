@@ -7,6 +7,7 @@
 #include <string.h>
 
 #include <algorithm>
+#include <chrono>
 #include <cmath>
 #include <map>
 #include <memory>
@@ -610,6 +611,7 @@ int compat_solve(bool is_cgls, int w, const arecImage &images, const float *angl
     std::vector<double> hist((size_t)std::max(maxit, 1), 0.0);
     arecgb_solve_info info;
     memset(&info, 0, sizeof(info));
+    const auto t0 = std::chrono::steady_clock::now();
     if (is_cgls && stat)
         rc = cgls_stat(p, p->d_sin[2], p->d_vol[3], warm ? 1 : 0, maxit, tol, hist.data(), &info,
                        p->stream);
@@ -634,6 +636,11 @@ int compat_solve(bool is_cgls, int w, const arecImage &images, const float *angl
                    hist[info.iterations - 1], tol);
         if (info.iterbest < maxit - 1) printf("retrieve the best solution\n");
     }
+    if (v) {
+        const double secs =
+            std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+        printf("Total time in %s = %11.3e\n", is_cgls ? "CG" : "SIRT", secs);
+    }
     return 0;
 }
 
@@ -642,6 +649,58 @@ int compat_solve(bool is_cgls, int w, const arecImage &images, const float *angl
 // ---------------------------------------------------------------------------
 // extern "C" aliases for C/FFI callers.
 extern "C" {
+
+int arecgb_reconstruct_host(arecgb_plan *plan, const float *b_host, float *x_host,
+                            arecgb_unet *net, int sirt_iters, float sirt_lam, int maxit,
+                            float tol, arecgb_solve_info *info, void *stream) {
+    Plan *p = reinterpret_cast<Plan *>(plan);
+    if (!p || !b_host || !x_host || maxit < 0 || (net && sirt_iters < 1)) {
+        set_error("arecgb_reconstruct_host: bad argument");
+        return ARECGB_ERR_ARG;
+    }
+    int rc = bind_device(p);
+    if (rc) return rc;
+    cudaStream_t st = (cudaStream_t)stream;
+    const size_t nsin = (size_t)p->na * p->ny * p->nx;
+    if ((rc = ensure(&p->d_vol[3], vol_floats(p))) || (rc = ensure(&p->d_sin[2], sin_floats(p))) ||
+        (rc = ensure_stage(p, nsin)))
+        return rc;
+    int H = 0, W = 0, B = 0;
+    if (net) {
+        if ((rc = arecgb_unet_shape(net, &H, &W, &B))) return rc;
+        const size_t n = (size_t)H * W * B;
+        if (p->img_floats < n) {
+            for (auto &v : p->d_img) {
+                cudaFree(v);
+                v = nullptr;
+            }
+            p->img_floats = 0;
+            for (auto &v : p->d_img) ARECGB_CUDA(cudaMalloc(&v, sizeof(float) * n));
+            p->img_floats = n;
+        }
+    }
+    float *d_b = p->d_sin[2], *d_x = p->d_vol[3];
+    ARECGB_CUDA(cudaMemcpyAsync(p->d_stage, b_host, sizeof(float) * nsin, cudaMemcpyHostToDevice,
+                                st));
+    if ((rc = sino_to_device_layout(p->d_stage, d_b, p->na, p->ny, p->nx, p->ys, st))) return rc;
+    arecgb_solve_info si, ci;
+    memset(&si, 0, sizeof(si));
+    memset(&ci, 0, sizeof(ci));
+    if (net) {
+        if ((rc = sirt(p, d_b, d_x, sirt_lam, sirt_iters, 0.0f, nullptr, &si, 0, st))) return rc;
+        if ((rc = arecgb_warm_start(plan, net, d_x, d_x, p->d_img[0], p->d_img[1], st)))
+            return rc;
+        rc = cgls(p, d_b, d_x, 1, maxit, tol, si.rnorm0, nullptr, &ci, st);
+    } else {
+        rc = cgls(p, d_b, d_x, 0, maxit, tol, 0.0, nullptr, &ci, st);
+    }
+    if (rc) return rc;
+    ARECGB_CUDA(cudaMemcpy2DAsync(x_host, sizeof(float) * p->ny, d_x, sizeof(float) * p->ys,
+                                  sizeof(float) * p->ny, p->nrays, cudaMemcpyDeviceToHost, st));
+    ARECGB_CUDA(cudaStreamSynchronize(st));
+    if (info) *info = ci;
+    return 0;
+}
 
 int arecgb_arecAllocateCBImage(arecImage *cb, int nx, int ny, int nz) {
     cb->nx = nx;
@@ -998,18 +1057,28 @@ void arecgb_makePeriodicSlice(int nx, int ny, float *data, float *out) {
 }
 
 // ccorr2d (AREC3D/AREC3D/align2dstack.cpp:480-521).
+// The reference's ccorr2d, fshift2d and speak return nothing; a failure here
+// (a rejected size, a CUDA error) leaves the output untouched and is reported
+// on stderr, as the other void entry points do, unless ARECGB_QUIET is set.
+static void report_void(const char *fn) {
+    if (!quiet()) fprintf(stderr, "%s: %s\n", fn, last_error());
+}
+
 void arecgb_ccorr2d(int nx, int ny, float *x, float *y, float *c) {
     std::lock_guard<std::mutex> lk(g_mu);
     const size_t n = (size_t)nx * ny;
     float *d = nullptr;
     if (cudaMalloc(&d, sizeof(float) * 3 * n) != cudaSuccess) {
         set_error("ccorr2d: device allocation failed");
+        report_void("ccorr2d");
         return;
     }
     cudaMemcpy(d, x, sizeof(float) * n, cudaMemcpyHostToDevice);
     cudaMemcpy(d + n, y, sizeof(float) * n, cudaMemcpyHostToDevice);
     if (ccorr_image(d, d + n, d + 2 * n, ny, nx, 0) == 0)
         cudaMemcpy(c, d + 2 * n, sizeof(float) * n, cudaMemcpyDeviceToHost);
+    else
+        report_void("ccorr2d");
     cudaFree(d);
 }
 
@@ -1020,6 +1089,7 @@ void arecgb_fshift2d(int nx, int ny, float *in, float *out, float sx, float sy) 
     float *d = nullptr;
     if (cudaMalloc(&d, sizeof(float) * (2 * n + 2)) != cudaSuccess) {
         set_error("fshift2d: device allocation failed");
+        report_void("fshift2d");
         return;
     }
     const float s2[2] = {sx, sy};
@@ -1027,6 +1097,8 @@ void arecgb_fshift2d(int nx, int ny, float *in, float *out, float sx, float sy) 
     cudaMemcpy(d + 2 * n, s2, sizeof(float) * 2, cudaMemcpyHostToDevice);
     if (fshift_stack(d, d + n, 1, ny, nx, d + 2 * n, d + 2 * n + 1, 0) == 0)
         cudaMemcpy(out, d + n, sizeof(float) * n, cudaMemcpyDeviceToHost);
+    else
+        report_void("fshift2d");
     cudaFree(d);
 }
 
@@ -1037,12 +1109,15 @@ void arecgb_speak(int nx, int ny, float *data, float *xt, float *yt) {
     float *d = nullptr;
     if (cudaMalloc(&d, sizeof(float) * (n + 2)) != cudaSuccess) {
         set_error("speak: device allocation failed");
+        report_void("speak");
         return;
     }
     cudaMemcpy(d, data, sizeof(float) * n, cudaMemcpyHostToDevice);
     if (peak_search(d, 1, ny, nx, d + n, d + n + 1, nullptr, nullptr, 0) == 0) {
         cudaMemcpy(xt, d + n, sizeof(float), cudaMemcpyDeviceToHost);
         cudaMemcpy(yt, d + n + 1, sizeof(float), cudaMemcpyDeviceToHost);
+    } else {
+        report_void("speak");
     }
     cudaFree(d);
 }

@@ -587,8 +587,20 @@ static bool pow2_ok(int n) { return n >= 16 && n <= 4096 && (n & (n - 1)) == 0; 
 
 static int rows_per_block(int nx) { return std::min(4096 / nx, 256 / (nx / 16)); }
 
+static std::mutex g_smem_mu;
+static std::map<std::pair<int, const void *>, size_t> g_smem;  // (device, kernel) -> limit set
+
+// Raises a kernel's dynamic shared-memory limit to at least `bytes` and never
+// lowers it: the limit is process-wide, so a caller on another host thread
+// with smaller images cannot drop it between this caller's set and launch.
 static int set_smem(const void *fn, size_t bytes) {
+    int dev = 0;
+    ARECGB_CUDA(cudaGetDevice(&dev));
+    std::lock_guard<std::mutex> lk(g_smem_mu);
+    size_t &cur = g_smem[{dev, fn}];
+    if (bytes <= cur) return 0;
     ARECGB_CUDA(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes));
+    cur = bytes;
     return 0;
 }
 
@@ -853,8 +865,7 @@ int cc_shifts_static(const float *d1, const float *d2, int nz, int ny, int nx, f
     const float2 *tw = reinterpret_cast<const float2 *>(base + kOffTw);
     const float2 *twx = tw + (nx - 16), *twy = tw + (ny - 16);
     // shared memory: 8 * G * nx = 32 KB per row block, 64 * ny <= 32 KB per
-    // column block.  The limits are set on every call: cc_shifts sets them to
-    // its own (possibly smaller) sizes.
+    // column block (set_smem only ever raises the kernels' limits).
     const int G = rows_per_block(nx);
     const size_t row_smem = sizeof(float2) * (size_t)G * plen(nx);
     const size_t col_smem = sizeof(float2) * 2 * kColTile * (size_t)plen(ny);

@@ -292,6 +292,7 @@ void plan_destroy(Plan *p) {
     for (auto &v : p->d_vol) cudaFree(v);
     for (auto &v : p->d_sin) cudaFree(v);
     cudaFree(p->d_stage);
+    for (auto &v : p->d_img) cudaFree(v);
     if (p->h_pinned) cudaFreeHost(p->h_pinned);
     if (p->stream) cudaStreamDestroy(p->stream);
     if (p->solve_stream) cudaStreamSynchronize(p->solve_stream);

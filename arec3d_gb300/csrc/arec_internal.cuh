@@ -100,6 +100,8 @@ struct Plan {
     size_t stage_floats = 0;
     float *h_pinned = nullptr;     // pinned host staging
     size_t pinned_floats = 0;
+    float *d_img[2] = {nullptr, nullptr};  // warm-start network images (arecgb_reconstruct_host)
+    size_t img_floats = 0;
 
     cudaStream_t stream = nullptr; // plan-owned stream for the compatible entry points
 

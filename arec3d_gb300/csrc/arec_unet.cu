@@ -509,6 +509,18 @@ int arecgb_unet_images_to_volume(const arecgb_plan *plan, const float *d_img, fl
     return 0;
 }
 
+int arecgb_unet_shape(const arecgb_unet *net, int *height, int *width, int *max_batch) {
+    const Net *n = reinterpret_cast<const Net *>(net);
+    if (!n) {
+        arecgb::set_error("arecgb_unet_shape: null network");
+        return ARECGB_ERR_ARG;
+    }
+    if (height) *height = n->H;
+    if (width) *width = n->W;
+    if (max_batch) *max_batch = n->maxN;
+    return 0;
+}
+
 int arecgb_warm_start(const arecgb_plan *plan, arecgb_unet *net, const float *d_x_early,
                       float *d_x0, float *d_img_in, float *d_img_out, void *stream) {
     const arecgb::Plan *p = reinterpret_cast<const arecgb::Plan *>(plan);

@@ -2,10 +2,11 @@
 1200-angle cylinder (square-pixel projector), on one GB300 per rank:
 learned-warm-start CGLS (the headline `value`) beside plain CGLS.
 
-One step = one complete reconstruction of the whole volume: 10 SIRT
-iterations, the BF16 U-Net warm start (arec3d_gb300/weights), then CGLS from
-that guess until ||A^T(b - A x_k)|| / ||A^T b|| <= 1e-3 (the denominator fixed
-at its cold-start value) or 200 iterations.  `config.plain_cgls` is the same
+One step = one complete reconstruction of the whole volume: a few SIRT
+iterations (the depth and step the weights file records), the BF16 U-Net warm
+start (arec3d_gb300/weights), then CGLS from that guess until
+||A^T(b - A x_k)|| / ||A^T b|| <= 1e-3 (the denominator fixed at its
+cold-start value) or 200 iterations.  `config.plain_cgls` is the same
 problem solved by CGLS from zero.  `--plain` (or missing weights) makes plain
 CGLS the headline.  Inputs: a seeded random-sphere cylinder with analytic line
 integrals and Poisson noise at 5e3 photons (no public dataset exists).
@@ -15,9 +16,10 @@ integrals and Poisson noise at 5e3 photons (no public dataset exists).
 Prints one JSON line on rank 0.  With N > 1 (torchrun) every rank solves its
 own replica (the path needs no exchange: replicas only, weak scaling).
 `--impl reference` times the reference's CPU algorithm (plain CGLS) for the
-same metric on this host's cores (the oracle's C restatement, one thread per
-slab of slices like the reference's MPI ranks) on a bounded sample and
-extrapolates.
+same metric on all of this host's cores (the oracle's C restatement, one
+thread per slab of slices like the reference's MPI ranks) on a bounded sample
+(every slice, a uniform subset of the angles, one iteration) and extrapolates
+linearly in angles and iterations.
 """
 import argparse
 import ctypes as C
@@ -124,6 +126,111 @@ def profiled_traffic():
         return {}
 
 
+def max_over_ranks(ms, world, device):
+    """The job's time is the slowest rank's (all-reduce MAX)."""
+    if world > 1:
+        import torch
+        import torch.distributed as dist
+
+        t = torch.tensor([ms], dtype=torch.float64, device=device)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+    return ms
+
+
+def timed_steps(fn, steps, world, stream=None):
+    """Runs fn() `steps` times between a barrier and a device synchronize on
+    both sides; returns (ms per step as the maximum over ranks, [fn()
+    results]).  Timed with CUDA events on `stream`, or with the host clock when
+    stream is None (the CPU ranks of the multi-process tests)."""
+    import torch
+
+    def barrier():
+        if world > 1:
+            import torch.distributed as dist
+
+            dist.barrier()
+
+    out = []
+    barrier()
+    if stream is not None:
+        torch.cuda.synchronize()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(steps):
+            out.append(fn())
+        e1.record(stream)
+        torch.cuda.synchronize()
+        ms = e0.elapsed_time(e1)
+    else:
+        t0 = time.perf_counter()
+        for _ in range(steps):
+            out.append(fn())
+        ms = (time.perf_counter() - t0) * 1e3
+    barrier()
+    return max_over_ranks(ms, world, "cuda" if stream is not None else "cpu") / steps, out
+
+
+def job_value(world, ms_per_step):
+    """Whole-job slices/s: every rank reconstructs its own NY-slice replica."""
+    return world * NY / (ms_per_step / 1e3)
+
+
+# Slices of the headline result whose normal-equation residual the FP64 oracle
+# recomputes (slice-separable: the residual is a sum over slices).
+FP64_SLICES = (137, 388)
+
+
+def fp64_check(gb, plan, b_s, x_s, slices):
+    """||A^T (b - A x)|| / ||A^T b|| over `slices` of the headline result,
+    recomputed with the oracle's FP64 projectors (the checker), beside the same
+    quantity evaluated by the GPU projectors in FP32.  b_s: [na][nx][k] and x_s:
+    [nrays][k] float32 host arrays of those slices."""
+    import torch
+
+    import oracle
+
+    radius = 0.5 * (NX - 1)
+    b_ref = np.ascontiguousarray(b_s.transpose(0, 2, 1), np.float64)  # [na][k][nx]
+    x64 = np.ascontiguousarray(x_s, np.float64)
+    t0 = time.perf_counter()
+    with oracle.op_threads():
+        atb = oracle.backproject64(3, radius, b_ref, plan.angles)
+        r = b_ref - oracle.project64(3, radius, x64, plan.angles)
+        atr = oracle.backproject64(3, radius, r, plan.angles)
+    rel64 = float(np.linalg.norm(atr) / np.linalg.norm(atb))
+    secs = time.perf_counter() - t0
+    # the GPU's FP32 evaluation of the same quantity (a plan of k slices)
+    k = len(slices)
+    old = os.environ.get("ARECGB_PLAN_TABLES")
+    os.environ["ARECGB_PLAN_TABLES"] = "0"  # same results without the tables
+    try:
+        p2 = gb.Plan(gb.SQ, radius, k, plan.angles)
+    finally:
+        if old is None:
+            del os.environ["ARECGB_PLAN_TABLES"]
+        else:
+            os.environ["ARECGB_PLAN_TABLES"] = old
+    bd = torch.zeros(NA, NX, p2.ys, device="cuda")
+    bd[:, :, :k] = torch.from_numpy(b_s).cuda()
+    xd = torch.zeros(p2.nrays, p2.ys, device="cuda")
+    xd[:, :k] = torch.from_numpy(x_s).cuda()
+    q = torch.zeros_like(bd)
+    p2.project(xd, q)
+    g = torch.zeros_like(xd)
+    gb_ = torch.zeros_like(xd)
+    p2.backproject(bd - q, g)
+    p2.backproject(bd, gb_)
+    rel32 = float(g.double().norm() / gb_.double().norm())
+    p2.close()
+    return {"slices": list(slices), "rel_residual_fp64": rel64, "rel_residual_gpu_fp32": rel32,
+            "abs_diff": abs(rel64 - rel32), "oracle_seconds": secs,
+            "note": "normal-equation residual of the last timed solve over these slices "
+                    "(numerator and denominator restricted to them), FP64 oracle projectors "
+                    "vs the GPU's FP32 projectors"}
+
+
 def make_problem(gb, seed, device="cuda"):
     import torch
 
@@ -140,22 +247,77 @@ def make_problem(gb, seed, device="cuda"):
     return plan, b, angles
 
 
-def cpu_sample(weighting_sq=True, slices=16, iters=1, threads=None):
-    """Reference CGLS (oracle restatement, one thread per slab) on a slab of the
-    benchmark geometry; returns seconds per slice per projector pass."""
+def host_cpu():
+    """The host's CPU as the baseline reports it: cores this process may use,
+    all online cores, and the model name."""
+    import platform
+
+    try:
+        usable = len(os.sched_getaffinity(0))
+    except (AttributeError, OSError):
+        usable = os.cpu_count() or 1
+    model = None
+    try:
+        out = subprocess.run(["lscpu"], capture_output=True, text=True, timeout=10).stdout
+        for ln in out.splitlines():
+            if ln.startswith("Model name:"):
+                model = ln.split(":", 1)[1].strip()
+                break
+    except Exception:
+        pass
+    if not model:
+        try:
+            with open("/proc/cpuinfo") as fh:
+                for ln in fh:
+                    if ln.lower().startswith(("model name", "cpu part")):
+                        model = ln.split(":", 1)[1].strip()
+                        break
+        except OSError:
+            pass
+    return {"usable": usable, "nproc": os.cpu_count(), "model": model or platform.machine(),
+            "machine": platform.machine()}
+
+
+# Angles kept in the CPU sample: every CPU_ANGLE_STEP-th of the 1200.  The
+# reference's projectors loop angle by angle with the same work per angle
+# (AREC3D/AREC3D/arecproject.cpp:595-645, 698-762), so their time is linear in
+# the number of angles; all 512 slices are kept so each rank holds the slab it
+# would hold in the full run (the per-(ray, angle) weights are shared by the
+# slab's slices, as in the reference).
+CPU_ANGLE_STEP = 50
+
+
+def cpu_sample(threads=None, iters=1, slices=NY, angle_step=CPU_ANGLE_STEP):
+    """Reference CGLS (the oracle's C restatement of cyl_cgls_SQ, one thread
+    per slab of slices like the reference's MPI ranks) on the benchmark
+    geometry with every `angle_step`-th angle; returns seconds per slice per
+    full-size projector pass (scaled to all 1200 angles) and the sample's
+    description."""
     import oracle
 
     oracle.build()
-    threads = threads or min(os.cpu_count() or 1, slices)
+    cpu = host_cpu()
+    threads = threads or cpu["usable"]
     rng = np.random.default_rng(0)
-    angles = (np.arange(NA) * (np.pi / NA)).astype(np.float32)
-    b = (rng.random((NA, slices, NX), dtype=np.float32) * 2.0).astype(np.float32)
+    angles = (np.arange(0, NA, angle_step) * (np.pi / NA)).astype(np.float32)
+    b = (rng.random((len(angles), slices, NX), dtype=np.float32) * 2.0).astype(np.float32)
     t0 = time.perf_counter()
     oracle.cgls(3, b, angles, maxit=iters, tol=0.0, nthreads=threads)
     dt = time.perf_counter() - t0
     passes = 1 + 2 * iters  # initial A^T s, then A p and A^T s per iteration
-    return dt / (slices * passes), {"slices": slices, "iterations": iters, "threads": threads,
-                                    "seconds": dt}
+    per = dt * (NA / len(angles)) / (slices * passes)
+    return per, {"slices": slices, "angles": len(angles), "iterations": iters,
+                 "threads": threads, "seconds": dt, "cpu": cpu}
+
+
+def cpu_sample_text(info, n_it):
+    return ("oracle C restatement of cyl_cgls_SQ (bit-identical to the reference build), "
+            "%d ranks (threads) x slabs of the %d slices, %d of the 1200 angles (every %dth), "
+            "%d iteration: %.1f s, extrapolated linearly to 1200 angles x %d iterations "
+            "(plain CGLS to 1e-3); host %s, %d usable of %s cores"
+            % (info["threads"], info["slices"], info["angles"], NA // info["angles"],
+               info["iterations"], info["seconds"], n_it, info["cpu"]["model"],
+               info["cpu"]["usable"], info["cpu"]["nproc"]))
 
 
 def run_reference(args, rank, world):
@@ -166,7 +328,7 @@ def run_reference(args, rank, world):
     times = []
     info = None
     for i in range(args.warmup + args.steps):
-        per, info = cpu_sample(slices=args.ref_slices, iters=1)
+        per, info = cpu_sample(angle_step=args.ref_angle_step)
         if i >= args.warmup:
             times.append(per)
     per = statistics.median(times)
@@ -178,11 +340,8 @@ def run_reference(args, rank, world):
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
         "data": "synthetic", "impl": "reference", "config": CONFIG,
         "cpu_baseline": {"value": value, "unit": "slices/s", "cores": info["threads"],
-                         "kind": "port",
-                         "sample": "oracle C restatement of cyl_cgls_SQ, %d slices x 1 CGLS "
-                                   "iteration on the 1024^2/1200-angle geometry per step, "
-                                   "extrapolated linearly to 512 slices x %d iterations"
-                                   % (info["slices"], it_gpu)},
+                         "kind": "port", "host": info["cpu"],
+                         "sample": "per step: " + cpu_sample_text(info, it_gpu)},
         "e2e": {"value": value, "unit": "slices/s", "h2d_bytes_per_step": 0,
                 "d2h_bytes_per_step": 0},
     }
@@ -365,7 +524,8 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
-    ap.add_argument("--ref-slices", type=int, default=16)
+    ap.add_argument("--ref-angle-step", type=int, default=CPU_ANGLE_STEP,
+                    help="reference arm: keep every k-th angle in each step's CPU sample")
     ap.add_argument("--ref-iters", type=int, default=32,
                     help="iterations to extrapolate the reference arm to (plain CGLS needs 32 "
                          "on this problem)")
@@ -431,71 +591,60 @@ def main():
         npix = 16 * plan.nx * plan.nx
         scratch = (torch.empty(npix, device="cuda"), torch.empty(npix, device="cuda"))
 
-    def barrier():
-        if world > 1:
-            import torch.distributed as dist
-
-            dist.barrier()
-
     def solve_plain():
         hist, info = plan.cgls(b, x, MAXIT, TOL, stream=stream)
         return info
 
     sirt_iters = getattr(net, "sirt_iters", SIRT_ITERS)
     lam = ws.sirt_lambda(plan, getattr(net, "sirt_lam_scale", 1.0))
+    stage_ev = []  # per step: events after SIRT, after the U-Net, after CGLS
 
     def solve_warm():
+        ev = [torch.cuda.Event(enable_timing=True) for _ in range(4)]
+        ev[0].record(stream)
         _, sinfo = plan.sirt(b, x, lam, sirt_iters, 0.0, stream=stream)
+        ev[1].record(stream)
         net.warm_start(plan, x, x, scratch[0], scratch[1], stream=stream)
+        ev[2].record(stream)
         hist, info = plan.cgls(b, x, MAXIT, TOL, warm=True, rnorm_ref=sinfo.rnorm0,
                                stream=stream)
+        ev[3].record(stream)
+        stage_ev.append(ev)
         return info
 
     solve = solve_warm if net is not None else solve_plain
 
-    def timed(fn, steps):
-        iters = []
-        barrier()
-        torch.cuda.synchronize()
-        e0 = torch.cuda.Event(enable_timing=True)
-        e1 = torch.cuda.Event(enable_timing=True)
-        e0.record(stream)
-        for _ in range(steps):
-            iters.append(fn().iterations)
-        e1.record(stream)
-        torch.cuda.synchronize()
-        barrier()
-        ms = e0.elapsed_time(e1)
-        if world > 1:
-            import torch.distributed as dist
-
-            t = torch.tensor([ms], device="cuda")
-            dist.all_reduce(t, op=dist.ReduceOp.MAX)
-            ms = float(t.item())
-        return ms / steps, iters
-
     for _ in range(args.warmup):
-        info = solve()
+        solve()
+    stage_ev.clear()
     # timed region: the headline pipeline, with projector timing and clocks
     clocks = ClockSampler(local)
     clocks.start()
     plan.timing(1)
     n0 = gb.launch_count()
-    ms_step, iters = timed(solve, args.steps)
+    ms_step, infos = timed_steps(solve, args.steps, world, stream)
     launches = gb.launch_count() - n0
     fp_ms, fp_calls, bp_ms, bp_calls = plan.timing(0)
     ck = clocks.stop()
-    value = world * NY / (ms_step / 1e3)
-    n_it = int(statistics.median(iters))
-    rel_final = float(info.rel_final)
+    value = job_value(world, ms_step)
+    n_it = int(statistics.median([i.iterations for i in infos]))
+    rel_final = float(infos[-1].rel_final)
+    stages = None
+    if stage_ev:
+        stages = {k: statistics.mean(ev[j].elapsed_time(ev[j + 1]) for ev in stage_ev)
+                  for j, k in enumerate(("sirt_ms", "unet_ms", "cgls_ms"))}
+    # the headline result on a few slices, kept for the FP64 check below
+    keep = list(FP64_SLICES)
+    x_keep = x[:, keep].contiguous().cpu().numpy()
+    b_keep = b[:, :, keep].contiguous().cpu().numpy()
 
     # plain CGLS beside it (the comparison the metric names), same data
     plain = None
     if net is not None:
         solve_plain()
-        pm, pit = timed(solve_plain, max(1, min(args.steps, 2)))
-        plain = {"slices_per_s": world * NY / (pm / 1e3), "ms_per_solve": pm,
-                 "iterations": int(statistics.median(pit))}
+        pm, pinfos = timed_steps(solve_plain, max(1, min(args.steps, 2)), world, stream)
+        plain = {"slices_per_s": job_value(world, pm), "ms_per_solve": pm,
+                 "iterations": int(statistics.median([i.iterations for i in pinfos]))}
 
     # Roofline of the dominant kernel from the projector times recorded in the
     # timed region.  Unit: one projection (the forward projector is 32 band
@@ -533,67 +682,52 @@ def main():
                                             bp_avg * (bp_calls / args.steps + n_it)) * 1e3 /
                 ms_step}
 
-    # End to end through the C ABI over pinned host buffers: the reference
-    # layout sinogram goes up, the reconstruction comes back, every step.
+    # End to end through one C-ABI call over page-locked host buffers in the
+    # reference's layouts (arecgb_reconstruct_host): every step the sinogram
+    # [angle][slice][bin] goes up, SIRT -> warm start -> CGLS run, and the
+    # volume [ray][slice] comes back; host-clock time around the call.
     e2e = None
     if not args.no_e2e:
-        L = gb.lib()
         b_host = torch.empty(NA, NY, NX, dtype=torch.float32, pin_memory=True)
         b_host.copy_(b[:, :, :NY].permute(0, 2, 1))
-        x_host = torch.empty(plan.nrays, plan.ys, dtype=torch.float32, pin_memory=True)
-        b_ref = torch.empty(NA, NY, NX, dtype=torch.float32, device="cuda")
-        b_dev = torch.empty_like(b)
-        x_dev = torch.zeros_like(x)
-
-        ev = [torch.cuda.Event(enable_timing=True) for _ in range(4)]
-        copy_ms = [0.0, 0.0]
+        x_host = torch.empty(plan.nrays, NY, dtype=torch.float32, pin_memory=True)
 
         def e2e_step():
-            ev[0].record(stream)
-            b_ref.copy_(b_host, non_blocking=True)
-            ev[1].record(stream)
-            plan.sino_from_reference(b_ref, b_dev, stream=stream)
-            if net is not None:
-                _, sinfo = plan.sirt(b_dev, x_dev, lam, sirt_iters, 0.0, stream=stream)
-                net.warm_start(plan, x_dev, x_dev, scratch[0], scratch[1], stream=stream)
-                plan.cgls(b_dev, x_dev, MAXIT, TOL, warm=True, rnorm_ref=sinfo.rnorm0,
-                          stream=stream)
-            else:
-                plan.cgls(b_dev, x_dev, MAXIT, TOL, stream=stream)
-            ev[2].record(stream)
-            x_host.copy_(x_dev, non_blocking=True)
-            ev[3].record(stream)
-            torch.cuda.synchronize()
-            copy_ms[0] += ev[0].elapsed_time(ev[1])
-            copy_ms[1] += ev[2].elapsed_time(ev[3])
+            return plan.reconstruct_host(b_host, x_host, net, sirt_iters, lam, MAXIT, TOL,
+                                         stream=stream)
 
         e2e_step()
-        copy_ms[0] = copy_ms[1] = 0.0
         n_e2e = max(1, min(args.steps, 2))
-        torch.cuda.synchronize()
-        t0 = time.perf_counter()
-        for _ in range(n_e2e):
-            e2e_step()
-        dt = (time.perf_counter() - t0) / n_e2e
-        e2e = {"value": world * NY / dt, "unit": "slices/s",
+        e2e_ms, e2e_infos = timed_steps(e2e_step, n_e2e, world, None)
+        # the two copies alone, timed the same way, for the breakdown
+        b_scr = torch.empty(NA, NY, NX, dtype=torch.float32, device="cuda")
+        x_scr = torch.empty(plan.nrays, NY, dtype=torch.float32, device="cuda")
+        h2d_ms, _ = timed_steps(lambda: b_scr.copy_(b_host, non_blocking=True), 3, 1, stream)
+        d2h_ms, _ = timed_steps(lambda: x_host.copy_(x_scr, non_blocking=True), 3, 1, stream)
+        del b_scr, x_scr
+        e2e = {"value": job_value(world, e2e_ms), "unit": "slices/s",
                "h2d_bytes_per_step": NA * NY * NX * 4,
-               "d2h_bytes_per_step": plan.nrays * plan.ys * 4, "ms_per_step": dt * 1e3,
-               "h2d_ms": copy_ms[0] / n_e2e, "d2h_ms": copy_ms[1] / n_e2e,
-               "path": "pinned host sinogram [angle][slice][bin] -> arecgb_sino_from_reference "
-                       "-> " + ("arecgb_sirt -> arecgb_warm_start -> arecgb_cgls" if net is not None
-                                else "arecgb_cgls") + " -> pinned host volume"}
+               "d2h_bytes_per_step": plan.nrays * NY * 4, "ms_per_step": e2e_ms,
+               "iterations": int(statistics.median([i.iterations for i in e2e_infos])),
+               "h2d_copy_ms": h2d_ms, "d2h_copy_ms": d2h_ms,
+               "h2d_gbs": NA * NY * NX * 4 / (h2d_ms / 1e3) / 1e9,
+               "d2h_gbs": plan.nrays * NY * 4 / (d2h_ms / 1e3) / 1e9,
+               "path": "pinned host sinogram [angle][slice][bin] -> arecgb_reconstruct_host ("
+                       + ("SIRT -> warm start -> CGLS" if net is not None else "CGLS")
+                       + ") -> pinned host volume [ray][slice]"}
 
     cpu = None
+    fp64 = None
     if rank == 0 and not args.no_cpu:
         n_cpu_it = plain["iterations"] if plain else n_it
-        per, cinfo = cpu_sample(slices=16, iters=1)
+        per, cinfo = cpu_sample()
         cpu_solve = per * NY * (1 + 2 * n_cpu_it)
         cpu = {"value": NY / cpu_solve, "unit": "slices/s", "cores": cinfo["threads"],
-               "kind": "port",
-               "sample": "oracle C restatement of cyl_cgls_SQ: %d slices x 1 iteration on the "
-                         "benchmark geometry (%.1f s, %d threads), extrapolated linearly to 512 "
-                         "slices x %d iterations (plain CGLS to 1e-3)"
-                         % (cinfo["slices"], cinfo["seconds"], cinfo["threads"], n_cpu_it)}
+               "kind": "port", "host": cinfo["cpu"], "sample": cpu_sample_text(cinfo, n_cpu_it)}
+        # the oracle as the checker of the headline result: its FP64 projectors
+        # recompute the normal-equation residual of the last timed solve on a
+        # few slices (the residual is a sum over slices)
+        fp64 = fp64_check(gb, plan, b_keep, x_keep, keep)
 
     if rank == 0:
         cfg = dict(CONFIG, iterations=n_it, rel_final=rel_final,
@@ -603,8 +737,9 @@ def main():
                    plan={"projector_tables_gb": plan.table_bytes() / 1e9,
                          "create_ms": getattr(plan, "create_ms", None),
                          "note": "created once per geometry, outside the timed region"})
+        cfg["fp64_check"] = fp64
         if net is not None:
-            cfg.update(warm_start=True, sirt_iters=sirt_iters,
+            cfg.update(warm_start=True, sirt_iters=sirt_iters, stage_ms=stages,
                        workload="learned warm start: SIRT-%d -> BF16 U-Net -> CGLS to "
                                 "||A^T r||/||A^T b|| <= 1e-3 (max 200 it), square-pixel "
                                 "projector, 1024^2 x 512 slices, 1200 angles over [0,180), "

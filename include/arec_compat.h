@@ -2,8 +2,9 @@
  * Reference-compatible layer of libarec_gb300.
  *
  * The library defines the reference's own C++ entry points with the reference's
- * signatures (so a program built against the reference's headers links against
- * this library unchanged):
+ * signatures, so a program built against the reference's headers links against
+ * this library unchanged (the translation units it replaces are left out of
+ * that program's build):
  *
  *   arecProject2D, arecProject2D_KB, arecProject2D_SQ        AREC3D/AREC3D/arecproject.h:55-62
  *   arecBackProject2D, arecBackProject2D_KB, arecBackProject2D_SQ
@@ -139,4 +140,46 @@ int arecgb_last_trace(double *rel, int cap, arecgb_solve_info *info);
 
 #ifdef __cplusplus
 }
+
+/* The same entry points under the reference's own C++ names and signatures
+ * (C++ linkage), for C++ callers that include this header in place of the
+ * reference's arecproject.h, arecsirt.h, arecsirt_KB.h, areccgls.h,
+ * areccgls_KB.h, areccgls_stat.h and the alignment declarations of arecImage.h
+ * and align2dstack.h. */
+int arecProject2D(arecImage cylvol, float *angles, int nangles, arecImage *projstack);
+int arecProject2D_KB(arecImage cylvol, float *angles, int nangles, arecImage *projstack);
+int arecProject2D_SQ(arecImage cylvol, float *angles, int nangles, arecImage *projstack);
+int arecBackProject2D(arecImage images, float *angles, int nangles, arecImage *bvol);
+int arecBackProject2D_KB(arecImage images, float *angles, int nangles, arecImage *bvol);
+int arecBackProject2D_SQ(arecImage images, float *angles, int nangles, arecImage *bvol);
+int cyl_sirt(MPI_Comm comm, arecImage images, float *angles, arecImage *xvol, float lam, int maxit,
+             float tol);
+int cyl_sirt_KB(MPI_Comm comm, arecImage images, float *angles, arecImage *xvol, float lam,
+                int maxit, float tol);
+int cyl_sirt_SQ(MPI_Comm comm, arecImage images, float *angles, arecImage *xvol, float lam,
+                int maxit, float tol);
+int cyl_cgls(MPI_Comm comm, arecImage images, float *angles, arecImage *xvol, float lam, int maxit,
+             float tol);
+int cyl_cgls_KB(MPI_Comm comm, arecImage images, float *angles, arecImage *xvol, float lam,
+                int maxit, float tol);
+int cyl_cgls_SQ(MPI_Comm comm, arecImage images, float *angles, arecImage *xvol, float lam,
+                int maxit, float tol);
+int cyl_cgls_stat(MPI_Comm comm, arecImage images, float *angles, arecImage *xvol, float lam,
+                  int maxit, float tol);
+int cyl_cgls_KB_stat(MPI_Comm comm, arecImage images, float *angles, arecImage *xvol, float lam,
+                     int maxit, float tol);
+int cyl_cgls_SQ_stat(MPI_Comm comm, arecImage images, float *angles, arecImage *xvol, float lam,
+                     int maxit, float tol);
+int init_weights(MPI_Comm comm, arecImage projections, arecImage *weights);
+int arecCCImages(MPI_Comm comm, arecImage images1, arecImage images2, float *sx, float *sy);
+int arecRotCCImages(MPI_Comm comm, arecImage images1, arecImage images2, int r2, float *angle);
+void arecRotateImages(arecImage *images, float *angles);
+void arecRotateImages_skew(arecImage *images, float *angles);
+void arecRotateImages_skew_safe(arecImage *images, arecImage *images_ref, float *angles);
+void arecImageTakeLog(arecImage image);
+void ccorr2d(int nx, int ny, float *x, float *y, float *c);
+void speak(int nx, int ny, float *data, float *xt, float *yt);
+void fshift2d(int nx, int ny, float *imagein, float *imageout, float sx, float sy);
+void makePeriodicSlice(int nx, int ny, float *data, float *out);
+void periodicDecomposition(arecImage img);
 #endif

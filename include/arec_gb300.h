@@ -19,6 +19,12 @@
  *   ARECGB_ERR_ARG       invalid argument (message in arecgb_last_error())
  *   ARECGB_ERR_NOMEM     device or host allocation failed
  *   ARECGB_ERR_CUDA_BASE - cudaError_t   any other CUDA runtime error
+ *
+ * The library keeps per-device state between calls (cached plans of the
+ * compatible entry points, FFT twiddle tables, the static shift-search
+ * scratch, kernel shared-memory limits).  cudaDeviceReset destroys the device
+ * memory behind that state without the library knowing: do not call the
+ * library on a device after resetting it in the same process.
  */
 #pragma once
 
@@ -278,7 +284,9 @@ int arecgb_mrc_write_device(const char *fname, const float *d_in, int nz, int ny
  * set-up (resolves the scratch address, uploads twiddle tables, synchronously)
  * and should come before any stream capture.  The call is asynchronous on
  * `stream`.  All calls on a device share the scratch: calls that can overlap
- * (other streams, unordered host threads) race. */
+ * (other streams, unordered host threads) race.  The kernels' shared-memory
+ * limits are process-wide; the library only ever raises them, so a concurrent
+ * allocating call on smaller images cannot make this launch fail. */
 int arecgb_cc_shifts_static(const float *d_img1, const float *d_img2, int nz, int ny, int nx,
                             float *d_sx, float *d_sy, int *d_ix, int *d_iy, void *stream);
 
@@ -341,6 +349,24 @@ int arecgb_unet_images_to_volume(const arecgb_plan *plan, const float *d_img, fl
  * x0 may equal x_early.  Follow with arecgb_cgls(..., warm = 1, ...). */
 int arecgb_warm_start(const arecgb_plan *plan, arecgb_unet *net, const float *d_x_early,
                       float *d_x0, float *d_img_in, float *d_img_out, void *stream);
+/* Image size and batch of a network (any pointer may be NULL). */
+int arecgb_unet_shape(const arecgb_unet *net, int *height, int *width, int *max_batch);
+
+/* One reconstruction end to end over HOST buffers in the reference's layouts
+ * (the path a caller without device memory of its own takes; no counterpart
+ * in the reference, whose cyl_cgls_SQ is the net == NULL case):
+ *   b_host [nangles][ny][nx] float (cyl_cgls_SQ's `images.data`), read;
+ *   x_host [nrays][ny] float (its `xvol->data`), written.
+ * With net != NULL: SIRT from zero (sirt_iters iterations of step sirt_lam),
+ * the network's warm start, then CGLS to ||A^T r|| / ||A^T b|| <= tol with the
+ * denominator ||A^T b|| of the cold start (at most maxit iterations); with
+ * net == NULL: CGLS from zero.  The copies are cudaMemcpyAsync on `stream`
+ * (full speed from page-locked memory).  Device buffers belong to the plan,
+ * allocated on first use and kept; the call returns after x_host is written.
+ * info (may be NULL) receives the CGLS summary. */
+int arecgb_reconstruct_host(arecgb_plan *plan, const float *b_host, float *x_host,
+                            arecgb_unet *net, int sirt_iters, float sirt_lam, int maxit,
+                            float tol, arecgb_solve_info *info, void *stream);
 
 #ifdef __cplusplus
 }

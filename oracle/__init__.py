@@ -80,12 +80,40 @@ def lib():
         L.oc_speak.argtypes = [C.c_int, C.c_int, _f32p, C.POINTER(C.c_float), C.POINTER(C.c_float),
                                C.POINTER(C.c_int), C.POINTER(C.c_int)]
         L.oc_cc_images.argtypes = [C.c_int, C.c_int, C.c_int, _f32p, _f32p, _f32p, _f32p, C.c_int]
+        L.oc_set_op_threads.argtypes = [C.c_int]
+        L.oc_set_op_threads.restype = None
         _lib = L
     return _lib
 
 
 def f32(a):
     return np.ascontiguousarray(a, dtype=np.float32)
+
+
+def host_threads():
+    """Host cores this process may use (the CPU affinity mask, else cpu_count)."""
+    try:
+        return len(os.sched_getaffinity(0))
+    except (AttributeError, OSError):
+        return os.cpu_count() or 1
+
+
+class op_threads:
+    """Context manager: threads inside every projector call of the oracle
+    (angles split in the forward projector, rays in the back projector; results
+    are bit-identical to one thread).  `with op_threads(): ...` uses all host
+    cores."""
+
+    def __init__(self, n=None):
+        self.n = n or host_threads()
+
+    def __enter__(self):
+        lib().oc_set_op_threads(self.n)
+        return self
+
+    def __exit__(self, *exc):
+        lib().oc_set_op_threads(1)
+        return False
 
 
 # --- geometry ------------------------------------------------------------------------------

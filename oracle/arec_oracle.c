@@ -198,6 +198,11 @@ static void slab_range(int ny, int nranks, int rank, int *y0, int *nyl) {
     }
 }
 
+/* Threads per projector call (1 = the reference's single loop); see op_run. */
+static int op_threads = 1;
+
+void oc_set_op_threads(int n) { op_threads = n < 1 ? 1 : n; }
+
 #define CAT2(a, b) a##b
 #define CAT(a, b) CAT2(a, b)
 #define REAL float

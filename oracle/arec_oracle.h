@@ -38,6 +38,11 @@ typedef struct {
 int oc_cyl_count(double radius, int *nx_out, int *nrays_out);
 int oc_cyl_cord(double radius, int *cord);
 
+/* Threads used inside each projector call (default 1).  The forward projector
+ * splits angles and the back projector rays, so results are bit-identical for
+ * any count; this only shortens large oracle runs. */
+void oc_set_op_threads(int n);
+
 /* Projector pair (AREC3D/AREC3D/arecproject.cpp:19-183, 351-535, 540-765).
  * x: [nrays][ny]; q: [nangles][ny][nx]; both overwritten (reference `reset`). */
 int oc_project(int weighting, double radius, int ny, const float *x, const float *angles,

@@ -13,10 +13,12 @@
 # arithmetic is the literal C++ expression order; the C restatement in
 # oracle/arec_oracle.c is built the same way and must agree bit for bit.
 #
-# Usage: oracle/build_ref.sh [REFERENCE_ROOT]   (default: /root/reference)
+# Usage: oracle/build_ref.sh [REFERENCE_ROOT]
+#   REFERENCE_ROOT defaults to $AREC3D_REFERENCE, else /root/reference.
+#   Exit status 2 when the checkout is not there (nothing is built).
 set -euo pipefail
 HERE="$(cd "$(dirname "${BASH_SOURCE[0]}")" && pwd)"
-REF="${1:-/root/reference}"
+REF="${1:-${AREC3D_REFERENCE:-/root/reference}}"
 SRC="$REF/AREC3D/AREC3D"
 TST="$REF/AREC3D/AREC3D_test"
 OUT="$HERE/_ref"

@@ -11,7 +11,7 @@ converted to float, i.e. float(double(text)), which is what numpy computes below
 Only entries 0..511 are written: the projectors evaluate the table at
 |x| <= 1.5 px, i.e. index <= 1.5 / (3/999) < 500, plus the right neighbour.
 
-Usage: python oracle/extract_kb_lut.py [REFERENCE_ROOT]   (default /root/reference)
+Usage: python oracle/extract_kb_lut.py REFERENCE_ROOT   (or set AREC3D_REFERENCE)
 """
 import os
 import re
@@ -23,7 +23,9 @@ KEEP = 512
 
 
 def main():
-    ref = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
+    ref = sys.argv[1] if len(sys.argv) > 1 else os.environ.get("AREC3D_REFERENCE")
+    if not ref:
+        raise SystemExit("usage: extract_kb_lut.py REFERENCE_ROOT (or set AREC3D_REFERENCE)")
     src = os.path.join(ref, "AREC3D", "AREC3D", "arecproject.cpp")
     text = open(src, encoding="utf-8", errors="replace").read()
     m = re.search(r"float\s+LUT\s*\[\s*LUT_SIZE\s*\]\s*=\s*\{(.*?)\};", text, re.S)

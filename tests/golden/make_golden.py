@@ -3,10 +3,11 @@ itself (AREC3D, compiled from its own sources into oracle/_ref by
 oracle/build_ref.sh) on small seeded inputs.  Run in the container that has the
 reference checkout:
 
-    bash oracle/build_ref.sh && python tests/golden/make_golden.py [--rotation|--preprocess|--prealign]
+    bash oracle/build_ref.sh && python tests/golden/make_golden.py \
+        [--rotation|--preprocess|--prealign|--compat]
 
 (each flag writes only its own file: reference_rotation.npz,
-reference_preprocess.npz, reference_prealign.npz.)
+reference_preprocess.npz, reference_prealign.npz, reference_compat.npz.)
 
 The reference's linear weighting (pmethod=1) reads two entries past its
 coordinate table; to make those reads return zero (as they do for large tables
@@ -223,8 +224,76 @@ def prealign():
     print("wrote", os.path.join(HERE, "reference_prealign.npz"))
 
 
+def _stdout_of(fn):
+    """Runs fn() with file descriptor 1 sent to a temporary file; returns
+    (fn's result, the text the C library printed)."""
+    import tempfile
+
+    sys.stdout.flush()
+    libc = ctypes.CDLL(None)
+    libc.fflush(None)
+    with tempfile.TemporaryFile(mode="w+b") as tmp:
+        saved = os.dup(1)
+        os.dup2(tmp.fileno(), 1)
+        try:
+            res = fn()
+            libc.fflush(None)
+        finally:
+            os.dup2(saved, 1)
+            os.close(saved)
+        tmp.seek(0)
+        text = tmp.read().decode()
+    return res, text
+
+
+def compat():
+    """The reference's solver entry points as a caller of the library sees
+    them: warm-started CGLS from a non-NULL xvol (areccgls.cpp:323-340), the
+    Kaiser-Bessel CGLS at an odd width (its integer radius nx/2 needs odd nx,
+    areccgls_KB.cpp:37-48), and the log lines the solvers print on rank 0
+    (areccgls.cpp:198, 358-453; arecsirt.cpp:131-156, 343-373)."""
+    import oracle as O
+
+    ctypes.CDLL("libc.so.6").mallopt(M_MMAP_THRESHOLD, 4096)
+    R = O.Reference()
+    small = np.load(os.path.join(HERE, "reference_small.npz"))
+    rng = np.random.default_rng(20261207)
+    out = {}
+    ang = small["solve_angles"]
+    for tag, nm in (("sq", "_SQ"), ("kb", "_KB")):
+        b = small["solve_%s_b" % tag]
+        if tag == "kb":  # odd width for the KB CGLS: radius 32 -> nx 65
+            nx, ny = 65, 4
+            _, nr, _ = O.cyl(32.0)
+            xt = rng.random((nr, ny), dtype=np.float32)
+            b = O.project(O.KB, 32.0, xt, ang)
+            b = (b + 0.01 * rng.standard_normal(b.shape)).astype(np.float32)
+            out["kb65_b"] = b
+            x, st = R.solve("cyl_cgls_KB", b, ang, 0.0, 8, 1e-7)
+            assert st == 0
+            out["kb65_cgls"] = x
+            x0 = (x * 0.5).astype(np.float32)
+        else:
+            x0 = small["solve_sq_sirt"]
+        out["warm_%s_x0" % tag] = x0
+        x, st = R.solve("cyl_cgls" + nm, b, ang, 0.0, 6, 1e-7, x0=x0)
+        assert st == 0
+        out["warm_%s_cgls" % tag] = x
+    b = small["solve_sq_b"]
+    (_, st), text = _stdout_of(lambda: R.solve("cyl_cgls_SQ", b, ang, 0.0, 10, 1e-7))
+    assert st == 0
+    out["log_cgls_sq"] = np.array(text)
+    (_, st), text = _stdout_of(lambda: R.solve("cyl_sirt_SQ", b, ang, 2e-4, 12, 0.0))
+    assert st == 0
+    out["log_sirt_sq"] = np.array(text)
+    np.savez_compressed(os.path.join(HERE, "reference_compat.npz"), **out)
+    print("wrote", os.path.join(HERE, "reference_compat.npz"))
+
+
 if __name__ == "__main__":
-    if "--rotation" in sys.argv:
+    if "--compat" in sys.argv:
+        compat()
+    elif "--rotation" in sys.argv:
         rotation()
     elif "--preprocess" in sys.argv:
         preprocess()
@@ -235,3 +304,4 @@ if __name__ == "__main__":
         rotation()
         preprocess()
         prealign()
+        compat()

@@ -1,6 +1,7 @@
 """Multi-process host logic of bench.py on CPU (gloo, world size 2): every rank
-runs its own replica, the timing is the maximum over ranks, and only rank 0
-reports."""
+runs its own replica through bench.py's own timing helper (barrier on both
+sides, maximum over ranks), the job's value counts every rank's slices, and
+only rank 0 reports."""
 import os
 import socket
 import subprocess
@@ -11,22 +12,19 @@ import pytest
 from conftest import ROOT
 
 WORKER = r"""
-import os, sys, json
-import torch
+import json, os, sys, time
+sys.path.insert(0, %r)
 import torch.distributed as dist
+import bench
 dist.init_process_group("gloo")
 rank, world = dist.get_rank(), dist.get_world_size()
-# a replica's local step time (ms); the job's time is the max over ranks
-local = torch.tensor([10.0 + 5.0 * rank])
-dist.barrier()
-dist.all_reduce(local, op=dist.ReduceOp.MAX)
-ms = float(local.item())
-slices = 512
-value = world * slices / (ms / 1e3)
+# a replica's step: rank r takes (r + 1) * 20 ms; the job's time is the slowest rank's
+ms, outs = bench.timed_steps(lambda: time.sleep(0.02 * (rank + 1)) or rank, 3, world, None)
+value = bench.job_value(world, ms)
 if rank == 0:
-    print(json.dumps({"ms": ms, "value": value, "world": world}))
+    print(json.dumps({"ms": ms, "value": value, "world": world, "outs": outs}))
 dist.destroy_process_group()
-"""
+""" % ROOT
 
 
 def free_port():
@@ -52,8 +50,9 @@ def test_replicas_max_over_ranks(tmp_path):
     import json
 
     res = json.loads(outs[0][0].strip().splitlines()[-1])
-    assert res["ms"] == 15.0 and res["world"] == 2
-    assert res["value"] == pytest.approx(2 * 512 / 0.015)
+    assert res["world"] == 2 and res["outs"] == [0, 0, 0]
+    assert 40.0 <= res["ms"] < 60.0  # rank 1's 40 ms per step, not rank 0's 20
+    assert res["value"] == pytest.approx(2 * 512 / (res["ms"] / 1e3))
     assert outs[1][0].strip() == ""
 
 

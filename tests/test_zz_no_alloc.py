@@ -46,8 +46,9 @@ def _run(L, fn, a, b):
     return rc, sx.cpu().numpy(), sy.cpu().numpy(), ix.cpu().numpy(), iy.cpu().numpy()
 
 
-# (16, 16, 16) before (2, 128, 256): an allocating call with small images may
-# leave the kernels' shared-memory limits below what the next static call needs
+# sizes mixed in this order so that the allocating and the static calls
+# alternate between small and large images (the shared-memory limits the
+# kernels need change with the image width)
 @pytest.mark.parametrize("nz,ny,nx", [(1, 512, 512), (64, 64, 64), (16, 16, 16), (2, 128, 256)])
 def test_static_matches_allocating(gb, nz, ny, nx):
     import torch
