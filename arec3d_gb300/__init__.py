@@ -161,6 +161,7 @@ def lib():
             getattr(L, n).argtypes = [vp, vp, vp, C.c_int, C.c_int, C.c_int, C.c_float, vp]
         L.arecgb_warm_start.argtypes = [vp, vp, vp, vp, vp, vp, vp]
         L.arecgb_unet_shape.argtypes = [vp, ip, ip, ip]
+        L.arecgb_unet_set_loss.argtypes = [vp, C.c_int, C.c_float]
         L.arecgb_reconstruct_host.argtypes = [vp, vp, vp, vp, C.c_int, C.c_float, C.c_int,
                                               C.c_float, C.POINTER(SolveInfo), vp]
         L.arecgb_plan_timing.argtypes = [vp, C.c_int, dp, C.POINTER(C.c_longlong), dp,
@@ -388,6 +389,12 @@ class UNet:
     def backward(self, dout, grads=None, stream=None):
         _check(lib().arecgb_unet_backward(self._h, _ptr(dout), _ptr(grads), _stream(stream)),
                "arecgb_unet_backward")
+
+    def set_loss(self, levels=0, ratio=1.0):
+        """Training loss: MSE (levels 0), or MSE plus ratio^s-weighted mean
+        squares of the error pooled over 2^s blocks, s = 1..levels."""
+        _check(lib().arecgb_unet_set_loss(self._h, int(levels), float(ratio)),
+               "arecgb_unet_set_loss")
 
     def train_step(self, x, target, lr, weight_decay=0.0, stream=None):
         loss = C.c_double()

@@ -6,7 +6,8 @@
 //   peak = speak(c): |c| argmax with the reference's scan-order rules,
 //          3x3 paraboloid fit, wrap to (-n/2, n/2].
 //
-// Pipeline per batch of image pairs (all FP32, power-of-two sizes 16..4096):
+// Pipeline per batch of image pairs (all FP32, sizes 2..4096 whose prime
+// factors are 2, 3, 5 and 7):
 //   1. rows:    z = x + i*y, complex FFT of each row (one transform gives the
 //               row spectra of both real images), split into the half spectra
 //               Xh, Yh [ny][nx/2+1] (Hermitian symmetry).
@@ -16,9 +17,11 @@
 //               per-row peak statistics fused.
 //   4. peak:    one block per pair reduces the row statistics exactly in the
 //               reference's x-major scan order and fits the paraboloid in FP64.
-// FFTs run in shared memory: mixed-radix Stockham passes (radix 16 and one
-// radix-2/4/8 pass), one radix-16 butterfly per thread per pass held in
-// registers, twiddles from a per-length table computed in double on the host.
+// FFTs run in shared memory: Stockham passes, twiddles from a per-length table
+// computed in double on the host.  Powers of two: radix 16 and one radix-2/4/8
+// pass, one radix-16 butterfly per thread per pass held in registers; other
+// lengths: radix 16/8/4/2 and then 7/5/3 passes, each thread holding up to 16
+// elements' butterflies.
 #include <math.h>
 
 #include <algorithm>
@@ -118,9 +121,141 @@ __device__ __forceinline__ void stockham_pass(float2 *L, int N, int Ns, int b, b
     __syncthreads();
 }
 
-// In-place forward FFT of G lines of length N (power of two, 16..4096) held in
-// shared memory at buf + l*lstride (padded lines: element i at pz(i)).  N/16 threads per line; all threads of the
-// block must call it.
+// Direct DFT (forward sign) of R = 3, 5 or 7 values in registers: the
+// butterflies of the lengths with odd prime factors.  cos / sin(2 pi m / R)
+// for m <= R / 2 (the other half by symmetry).
+template <int R>
+__device__ __forceinline__ void dft_odd(float2 *v) {
+    static_assert(R == 3 || R == 5 || R == 7, "odd radices 3, 5, 7");
+    float C[R], S[R];
+    if constexpr (R == 3) {
+        C[1] = -0.5f;
+        S[1] = 0.86602540378443865f;
+    } else if constexpr (R == 5) {
+        C[1] = 0.30901699437494742f;
+        S[1] = 0.95105651629515357f;
+        C[2] = -0.80901699437494742f;
+        S[2] = 0.58778525229247313f;
+    } else {
+        C[1] = 0.62348980185873353f;
+        S[1] = 0.78183148246802981f;
+        C[2] = -0.22252093395631440f;
+        S[2] = 0.97492791218182361f;
+        C[3] = -0.90096886790241913f;
+        S[3] = 0.43388373911755812f;
+    }
+    C[0] = 1.0f;
+    S[0] = 0.0f;
+#pragma unroll
+    for (int m = 1; m <= R / 2; m++) {
+        C[R - m] = C[m];
+        S[R - m] = -S[m];
+    }
+    float2 out[R];
+#pragma unroll
+    for (int m = 0; m < R; m++) {
+        float re = v[0].x, im = v[0].y;
+#pragma unroll
+        for (int r = 1; r < R; r++) {
+            const int e = (r * m) % R;  // v_r * exp(-2 pi i r m / R)
+            re += v[r].x * C[e] + v[r].y * S[e];
+            im += v[r].y * C[e] - v[r].x * S[e];
+        }
+        out[m] = make_float2(re, im);
+    }
+#pragma unroll
+    for (int m = 0; m < R; m++) v[m] = out[m];
+}
+
+template <int R>
+__device__ __forceinline__ void dft_any(float2 *v) {
+    if constexpr (R == 3 || R == 5 || R == 7)
+        dft_odd<R>(v);
+    else
+        dft_reg<R>(v);
+}
+
+// Lines of length n per block: G * n <= 4096 elements (16 per thread).
+__device__ __host__ __forceinline__ int lines_per_block(int n) { return n >= 4096 ? 1 : 4096 / n; }
+
+// One Stockham pass of radix R over G lines of any length N (N % R == 0,
+// G * N <= 4096), every thread of the 256 holding up to ceil(16 / R)
+// butterflies: all loads (times twiddles) before a barrier, then the
+// butterflies and the stores.  Twiddle index r * k * N / (Ns * R) < N.
+template <int R>
+__device__ void mixed_pass(float2 *buf, int N, int lstride, int G, int Ns,
+                           const float2 *__restrict__ tw) {
+    constexpr int NBT = (16 + R - 1) / R;
+    const int NR = N / R, B = G * NR, step = N / (Ns * R);
+    float2 v[NBT * R];
+#pragma unroll
+    for (int i = 0; i < NBT; i++) {
+        const int t = threadIdx.x + i * 256;
+        if (t < B) {
+            const int line = t / NR, j = t % NR, k = j % Ns;
+            const float2 *L = buf + (size_t)line * lstride;
+#pragma unroll
+            for (int r = 0; r < R; r++)
+                v[i * R + r] = cmul(L[pz(j + r * NR)], __ldg(&tw[r * k * step]));
+        }
+    }
+    __syncthreads();
+#pragma unroll
+    for (int i = 0; i < NBT; i++) {
+        const int t = threadIdx.x + i * 256;
+        if (t < B) {
+            dft_any<R>(v + i * R);
+            const int line = t / NR, j = t % NR, k = j % Ns;
+            float2 *L = buf + (size_t)line * lstride;
+            const int d = (j / Ns) * Ns * R + k;
+#pragma unroll
+            for (int r = 0; r < R; r++) L[pz(d + r * Ns)] = v[i * R + r];
+        }
+    }
+    __syncthreads();
+}
+
+// Lengths whose prime factors are 2, 3, 5 and 7 (the reference's FFTW takes any
+// length; these cover the detector and crop sizes the alignment sees).
+static inline bool smooth_length(int n) {
+    if (n < 2 || n > 4096) return false;
+    const int primes[4] = {2, 3, 5, 7};
+    for (int p : primes)
+        while (n % p == 0) n /= p;
+    return n == 1;
+}
+
+// Forward FFT of G lines of a length that is not a power of two: radix 16, 8,
+// 4, 2, 7, 5, 3 passes in that order (the product of the radices done is Ns).
+__device__ void fft_lines_mixed(float2 *buf, int N, int lstride, int G, const float2 *tw) {
+    int rest = N, Ns = 1;
+    while (rest > 1) {
+        int R;
+        if (rest % 16 == 0) R = 16;
+        else if (rest % 8 == 0) R = 8;
+        else if (rest % 4 == 0) R = 4;
+        else if (rest % 2 == 0) R = 2;
+        else if (rest % 7 == 0) R = 7;
+        else if (rest % 5 == 0) R = 5;
+        else R = 3;
+        switch (R) {
+            case 16: mixed_pass<16>(buf, N, lstride, G, Ns, tw); break;
+            case 8: mixed_pass<8>(buf, N, lstride, G, Ns, tw); break;
+            case 4: mixed_pass<4>(buf, N, lstride, G, Ns, tw); break;
+            case 2: mixed_pass<2>(buf, N, lstride, G, Ns, tw); break;
+            case 7: mixed_pass<7>(buf, N, lstride, G, Ns, tw); break;
+            case 5: mixed_pass<5>(buf, N, lstride, G, Ns, tw); break;
+            default: mixed_pass<3>(buf, N, lstride, G, Ns, tw); break;
+        }
+        Ns *= R;
+        rest /= R;
+    }
+}
+
+// In-place forward FFT of G lines of length N (power of two, 16..4096; G * N
+// <= 4096) held in shared memory at buf + l*lstride (padded lines: element i
+// at pz(i)).  N/16 threads per line, one radix-16 butterfly per thread per
+// pass; all threads of the block must call it.
 __device__ void fft_lines(float2 *buf, int N, int lstride, int G, const float2 *tw) {
     const int tpl = N / 16;
     const int line = threadIdx.x / tpl, b = threadIdx.x % tpl;
@@ -134,6 +269,17 @@ __device__ void fft_lines(float2 *buf, int N, int lstride, int G, const float2 *
         else stockham_pass<2>(L, N, Ns, b, active, tw);
         Ns *= R;
     }
+}
+
+// The kernels below are instantiated twice: MIXED = false for power-of-two
+// lengths (fft_lines), true for the other lengths (fft_lines_mixed), so the
+// power-of-two kernels keep their own register allocation.
+template <bool MIXED>
+__device__ __forceinline__ void fft_any(float2 *buf, int N, int lstride, int G, const float2 *tw) {
+    if constexpr (MIXED)
+        fft_lines_mixed(buf, N, lstride, G, tw);
+    else
+        fft_lines(buf, N, lstride, G, tw);
 }
 
 // ---------------------------------------------------------------------------
@@ -151,13 +297,14 @@ struct RowStat {
 constexpr int kLoadBatch = 16;
 
 // Pass 1: rows of z = x + i*y -> half spectra of x and y.
+template <bool MIXED>
 __global__ void __launch_bounds__(256, 2) k_cc_rows_fwd(const float *__restrict__ x,
                                                      const float *__restrict__ y,
                                                      float2 *__restrict__ Xh,
                                                      float2 *__restrict__ Yh, int nx, int ny,
                                                      const float2 *__restrict__ tw) {
     extern __shared__ float2 sm[];
-    const int G = 4096 / nx < 256 / (nx / 16) ? 4096 / nx : 256 / (nx / 16);
+    const int G = lines_per_block(nx);
     const int row0 = blockIdx.x * G, pair = blockIdx.y;
     const int H = nx / 2 + 1;
     const size_t img = (size_t)pair * nx * ny;
@@ -178,12 +325,12 @@ __global__ void __launch_bounds__(256, 2) k_cc_rows_fwd(const float *__restrict_
         }
     }
     __syncthreads();
-    fft_lines(sm, nx, plen(nx), G, tw);
+    fft_any<MIXED>(sm, nx, plen(nx), G, tw);
     const size_t half = (size_t)pair * ny * H;
     for (int i = threadIdx.x; i < G * H; i += blockDim.x) {
         const int l = i / H, k = i % H, row = row0 + l;
         if (row >= ny) continue;
-        const float2 Z = sm[l * plen(nx) + pz(k)], Zm = sm[l * plen(nx) + pz((nx - k) & (nx - 1))];
+        const float2 Z = sm[l * plen(nx) + pz(k)], Zm = sm[l * plen(nx) + pz(k ? nx - k : 0)];
         Xh[half + (size_t)row * H + k] = make_float2(0.5f * (Z.x + Zm.x), 0.5f * (Z.y - Zm.y));
         Yh[half + (size_t)row * H + k] = make_float2(0.5f * (Z.y + Zm.y), -0.5f * (Z.x - Zm.x));
     }
@@ -194,6 +341,7 @@ __global__ void __launch_bounds__(256, 2) k_cc_rows_fwd(const float *__restrict_
 // share an SM); W = IDFT_col(conj(X)*Y) overwrites Xh.
 constexpr int kColTile = 4;
 static inline int col_tile(int ny) { return ny <= 1024 ? 4 : (ny <= 2048 ? 2 : 1); }
+template <bool MIXED>
 __global__ void __launch_bounds__(256, 2) k_cc_cols(float2 *__restrict__ Xh,
                                                  const float2 *__restrict__ Yh, int nx, int ny,
                                                  const float2 *__restrict__ tw, int ct) {
@@ -225,9 +373,9 @@ __global__ void __launch_bounds__(256, 2) k_cc_cols(float2 *__restrict__ Xh,
         }
     }
     __syncthreads();
-    const int G = max(1, 256 / (ny / 16));
+    const int G = lines_per_block(ny);
     for (int l0 = 0; l0 < 2 * ct; l0 += G)
-        fft_lines(sm + (size_t)l0 * PN, ny, PN, min(G, 2 * ct - l0), tw);
+        fft_any<MIXED>(sm + (size_t)l0 * PN, ny, PN, min(G, 2 * ct - l0), tw);
     // conj(X)*Y, conjugated again for the inverse transform (IDFT = conj DFT conj)
     for (int i = threadIdx.x; i < ct * ny; i += blockDim.x) {
         const int c = i / ny, row = i % ny, o = c * PN + pz(row);
@@ -237,7 +385,7 @@ __global__ void __launch_bounds__(256, 2) k_cc_cols(float2 *__restrict__ Xh,
     }
     __syncthreads();
     for (int l0 = 0; l0 < ct; l0 += G)
-        fft_lines(sm + (size_t)l0 * PN, ny, PN, min(G, ct - l0), tw);
+        fft_any<MIXED>(sm + (size_t)l0 * PN, ny, PN, min(G, ct - l0), tw);
     for (int i = threadIdx.x; i < ct * ny; i += blockDim.x) {
         const int row = i / ct, c = i % ct;
         if (c < nc) {
@@ -258,12 +406,13 @@ __device__ __forceinline__ RowStat stat_merge(RowStat a, RowStat b) {
 }
 
 // Pass 3: inverse row transforms -> c rows, with per-row peak statistics.
+template <bool MIXED>
 __global__ void __launch_bounds__(256, 2) k_cc_rows_inv(const float2 *__restrict__ Wh,
                                                      float *__restrict__ c, RowStat *stats,
                                                      int nx, int ny,
                                                      const float2 *__restrict__ tw) {
     extern __shared__ float2 sm[];
-    const int G = 4096 / nx < 256 / (nx / 16) ? 4096 / nx : 256 / (nx / 16);
+    const int G = lines_per_block(nx);
     const int row0 = blockIdx.x * G, pair = blockIdx.y;
     const int H = nx / 2 + 1;
     const size_t half = (size_t)pair * ny * H;
@@ -289,7 +438,7 @@ __global__ void __launch_bounds__(256, 2) k_cc_rows_inv(const float2 *__restrict
         }
     }
     __syncthreads();
-    fft_lines(sm, nx, plen(nx), G, tw);
+    fft_any<MIXED>(sm, nx, plen(nx), G, tw);
     // one warp per row for the statistics
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const size_t img = (size_t)pair * nx * ny;
@@ -465,11 +614,12 @@ __global__ void __launch_bounds__(256) k_peak(const float *__restrict__ c,
 //   symmetric and only the real part is kept.
 
 // Pass 1: real rows -> complex spectra of the rows.
+template <bool MIXED>
 __global__ void __launch_bounds__(256) k_fs_rows(const float *__restrict__ in,
                                                  float2 *__restrict__ C, int nx, int ny,
                                                  const float2 *__restrict__ tw) {
     extern __shared__ float2 sm[];
-    const int G = 4096 / nx < 256 / (nx / 16) ? 4096 / nx : 256 / (nx / 16);
+    const int G = lines_per_block(nx);
     const int row0 = blockIdx.x * G;
     const size_t img = (size_t)blockIdx.y * nx * ny;
     for (int i = threadIdx.x; i < G * nx; i += blockDim.x) {
@@ -477,7 +627,7 @@ __global__ void __launch_bounds__(256) k_fs_rows(const float *__restrict__ in,
         sm[l * plen(nx) + pz(c)] = make_float2(row < ny ? in[img + (size_t)row * nx + c] : 0.f, 0.f);
     }
     __syncthreads();
-    fft_lines(sm, nx, plen(nx), G, tw);
+    fft_any<MIXED>(sm, nx, plen(nx), G, tw);
     for (int i = threadIdx.x; i < G * nx; i += blockDim.x) {
         const int l = i / nx, c = i % nx, row = row0 + l;
         if (row < ny) C[img + (size_t)row * nx + c] = sm[l * plen(nx) + pz(c)];
@@ -490,6 +640,7 @@ __device__ __forceinline__ float fs_freq(int i, int n) {
 }
 
 // Pass 2: column transforms, the phase factor, inverse column transforms.
+template <bool MIXED>
 __global__ void __launch_bounds__(256) k_fs_cols(float2 *__restrict__ C, int nx, int ny,
                                                  const float *__restrict__ sxs,
                                                  const float *__restrict__ sys,
@@ -502,12 +653,12 @@ __global__ void __launch_bounds__(256) k_fs_cols(float2 *__restrict__ C, int nx,
     const int PN = plen(ny);
     for (int i = threadIdx.x; i < kColTile * ny; i += blockDim.x) {
         const int row = i / kColTile, c = i % kColTile;
-        sm[c * PN + pz(row)] = C[img + (size_t)row * nx + c0 + c];
+        sm[c * PN + pz(row)] = c0 + c < nx ? C[img + (size_t)row * nx + c0 + c] : make_float2(0.f, 0.f);
     }
     __syncthreads();
-    const int G = max(1, 256 / (ny / 16));
+    const int G = lines_per_block(ny);
     for (int l0 = 0; l0 < kColTile; l0 += G)
-        fft_lines(sm + (size_t)l0 * PN, ny, PN, min(G, kColTile - l0), tw);
+        fft_any<MIXED>(sm + (size_t)l0 * PN, ny, PN, min(G, kColTile - l0), tw);
     for (int i = threadIdx.x; i < kColTile * ny; i += blockDim.x) {
         const int c = i / ny, row = i % ny, o = c * PN + pz(row);
         const float t = __fadd_rn(__fmul_rn(sx, fs_freq(c0 + c, nx)), __fmul_rn(sy, fs_freq(row, ny)));
@@ -521,20 +672,21 @@ __global__ void __launch_bounds__(256) k_fs_cols(float2 *__restrict__ C, int nx,
     }
     __syncthreads();
     for (int l0 = 0; l0 < kColTile; l0 += G)
-        fft_lines(sm + (size_t)l0 * PN, ny, PN, min(G, kColTile - l0), tw);
+        fft_any<MIXED>(sm + (size_t)l0 * PN, ny, PN, min(G, kColTile - l0), tw);
     for (int i = threadIdx.x; i < kColTile * ny; i += blockDim.x) {
         const int row = i / kColTile, c = i % kColTile;
         const float2 w = sm[c * PN + pz(row)];
-        C[img + (size_t)row * nx + c0 + c] = make_float2(w.x, -w.y);
+        if (c0 + c < nx) C[img + (size_t)row * nx + c0 + c] = make_float2(w.x, -w.y);
     }
 }
 
 // Pass 3: inverse row transforms, real part, divided by nx*ny.
+template <bool MIXED>
 __global__ void __launch_bounds__(256) k_fs_rows_inv(const float2 *__restrict__ C,
                                                      float *__restrict__ out, int nx, int ny,
                                                      const float2 *__restrict__ tw) {
     extern __shared__ float2 sm[];
-    const int G = 4096 / nx < 256 / (nx / 16) ? 4096 / nx : 256 / (nx / 16);
+    const int G = lines_per_block(nx);
     const int row0 = blockIdx.x * G;
     const size_t img = (size_t)blockIdx.y * nx * ny;
     for (int i = threadIdx.x; i < G * nx; i += blockDim.x) {
@@ -547,7 +699,7 @@ __global__ void __launch_bounds__(256) k_fs_rows_inv(const float2 *__restrict__ 
         sm[l * plen(nx) + pz(c)] = z;
     }
     __syncthreads();
-    fft_lines(sm, nx, plen(nx), G, tw);
+    fft_any<MIXED>(sm, nx, plen(nx), G, tw);
     const float scale = (float)(nx * ny);
     for (int i = threadIdx.x; i < G * nx; i += blockDim.x) {
         const int l = i / nx, c = i % nx, row = row0 + l;
@@ -585,7 +737,7 @@ static int twiddles(int N, const float2 **out) {
 
 static bool pow2_ok(int n) { return n >= 16 && n <= 4096 && (n & (n - 1)) == 0; }
 
-static int rows_per_block(int nx) { return std::min(4096 / nx, 256 / (nx / 16)); }
+static int rows_per_block(int nx) { return lines_per_block(nx); }
 
 static std::mutex g_smem_mu;
 static std::map<std::pair<int, const void *>, size_t> g_smem;  // (device, kernel) -> limit set
@@ -616,13 +768,17 @@ static int correlate_batch(const float *d1, const float *d2, int np, int ny, int
     const int ct = col_tile(ny);
     const size_t row_smem = sizeof(float2) * (size_t)G * plen(nx);
     const size_t col_smem = sizeof(float2) * 2 * ct * (size_t)plen(ny);
-    if ((rc = set_smem((const void *)k_cc_rows_fwd, row_smem))) return rc;
-    if ((rc = set_smem((const void *)k_cc_rows_inv, row_smem))) return rc;
-    if ((rc = set_smem((const void *)k_cc_cols, col_smem))) return rc;
+    // kernel instantiations for the two lengths (MIXED: not a power of two)
+    auto rows_fwd = pow2_ok(nx) ? k_cc_rows_fwd<false> : k_cc_rows_fwd<true>;
+    auto rows_inv = pow2_ok(nx) ? k_cc_rows_inv<false> : k_cc_rows_inv<true>;
+    auto cols = pow2_ok(ny) ? k_cc_cols<false> : k_cc_cols<true>;
+    if ((rc = set_smem((const void *)rows_fwd, row_smem))) return rc;
+    if ((rc = set_smem((const void *)rows_inv, row_smem))) return rc;
+    if ((rc = set_smem((const void *)cols, col_smem))) return rc;
     const int H = nx / 2 + 1;
-    k_cc_rows_fwd<<<dim3((ny + G - 1) / G, np), 256, row_smem, st>>>(d1, d2, Xh, Yh, nx, ny, twx);
-    k_cc_cols<<<dim3((H + ct - 1) / ct, np), 256, col_smem, st>>>(Xh, Yh, nx, ny, twy, ct);
-    k_cc_rows_inv<<<dim3((ny + G - 1) / G, np), 256, row_smem, st>>>(Xh, c, stats, nx, ny, twx);
+    rows_fwd<<<dim3((ny + G - 1) / G, np), 256, row_smem, st>>>(d1, d2, Xh, Yh, nx, ny, twx);
+    cols<<<dim3((H + ct - 1) / ct, np), 256, col_smem, st>>>(Xh, Yh, nx, ny, twy, ct);
+    rows_inv<<<dim3((ny + G - 1) / G, np), 256, row_smem, st>>>(Xh, c, stats, nx, ny, twx);
     ARECGB_CUDA(cudaGetLastError());
     return 0;
 }
@@ -651,8 +807,9 @@ static int cc_alloc(CcScratch &s, int np, int ny, int nx, bool need_c) {
 
 int cc_shifts(const float *d1, const float *d2, int nz, int ny, int nx, float *sx, float *sy,
               int *ix, int *iy, cudaStream_t st) {
-    if (!pow2_ok(nx) || !pow2_ok(ny) || nz < 0 || !d1 || !d2 || !sx || !sy) {
-        set_error("cc_shifts: nx and ny must be powers of two in [16, 4096]");
+    if (!smooth_length(nx) || !smooth_length(ny) || nz < 0 || !d1 || !d2 || !sx || !sy) {
+        set_error("cc_shifts: nx and ny must be in [2, 4096] with prime factors 2, 3, 5, 7 "
+                  "(got " + std::to_string(nx) + " x " + std::to_string(ny) + ")");
         return ARECGB_ERR_ARG;
     }
     if (nz == 0) return 0;
@@ -680,8 +837,9 @@ int cc_shifts(const float *d1, const float *d2, int nz, int ny, int nx, float *s
 }
 
 int ccorr_image(const float *dx, const float *dy, float *dc, int ny, int nx, cudaStream_t st) {
-    if (!pow2_ok(nx) || !pow2_ok(ny)) {
-        set_error("ccorr2d: nx and ny must be powers of two in [16, 4096]");
+    if (!smooth_length(nx) || !smooth_length(ny)) {
+        set_error("ccorr2d: nx and ny must be in [2, 4096] with prime factors 2, 3, 5, 7 (got " +
+                  std::to_string(nx) + " x " + std::to_string(ny) + ")");
         return ARECGB_ERR_ARG;
     }
     CcScratch s;
@@ -694,8 +852,10 @@ int ccorr_image(const float *dx, const float *dy, float *dc, int ny, int nx, cud
 
 int fshift_stack(const float *d_in, float *d_out, int nz, int ny, int nx, const float *d_sx,
                  const float *d_sy, cudaStream_t st) {
-    if (!pow2_ok(nx) || !pow2_ok(ny) || ny > 2048 || nz < 0 || !d_in || !d_out || !d_sx || !d_sy) {
-        set_error("fshift2d: nx (16..4096) and ny (16..2048) must be powers of two");
+    if (!smooth_length(nx) || !smooth_length(ny) || ny > 2048 || nz < 0 || !d_in || !d_out ||
+        !d_sx || !d_sy) {
+        set_error("fshift2d: nx in [2, 4096] and ny in [2, 2048] with prime factors 2, 3, 5, 7 "
+                  "(got " + std::to_string(nx) + " x " + std::to_string(ny) + ")");
         return ARECGB_ERR_ARG;
     }
     if (nz == 0) return 0;
@@ -706,9 +866,12 @@ int fshift_stack(const float *d_in, float *d_out, int nz, int ny, int nx, const 
     const int G = rows_per_block(nx);
     const size_t row_smem = sizeof(float2) * (size_t)G * plen(nx);
     const size_t col_smem = sizeof(float2) * kColTile * (size_t)plen(ny);
-    if ((rc = set_smem((const void *)k_fs_rows, row_smem))) return rc;
-    if ((rc = set_smem((const void *)k_fs_rows_inv, row_smem))) return rc;
-    if ((rc = set_smem((const void *)k_fs_cols, col_smem))) return rc;
+    auto fs_rows = pow2_ok(nx) ? k_fs_rows<false> : k_fs_rows<true>;
+    auto fs_rows_inv = pow2_ok(nx) ? k_fs_rows_inv<false> : k_fs_rows_inv<true>;
+    auto fs_cols = pow2_ok(ny) ? k_fs_cols<false> : k_fs_cols<true>;
+    if ((rc = set_smem((const void *)fs_rows, row_smem))) return rc;
+    if ((rc = set_smem((const void *)fs_rows_inv, row_smem))) return rc;
+    if ((rc = set_smem((const void *)fs_cols, col_smem))) return rc;
     // images per batch: complex scratch near 1 GiB
     const size_t per = sizeof(float2) * (size_t)nx * ny;
     const int batch = (int)std::max<size_t>(1, std::min<size_t>(nz, (1ull << 30) / per));
@@ -717,11 +880,11 @@ int fshift_stack(const float *d_in, float *d_out, int nz, int ny, int nx, const 
     for (int z0 = 0; z0 < nz && !rc; z0 += batch) {
         const int nb = std::min(batch, nz - z0);
         const size_t off = (size_t)z0 * nx * ny;
-        k_fs_rows<<<dim3((ny + G - 1) / G, nb), 256, row_smem, st>>>(d_in + off, C, nx, ny, twx);
-        k_fs_cols<<<dim3(nx / kColTile, nb), 256, col_smem, st>>>(C, nx, ny, d_sx + z0, d_sy + z0,
-                                                                twy);
-        k_fs_rows_inv<<<dim3((ny + G - 1) / G, nb), 256, row_smem, st>>>(C, d_out + off, nx, ny,
-                                                                       twx);
+        fs_rows<<<dim3((ny + G - 1) / G, nb), 256, row_smem, st>>>(d_in + off, C, nx, ny, twx);
+        fs_cols<<<dim3((nx + kColTile - 1) / kColTile, nb), 256, col_smem, st>>>(
+            C, nx, ny, d_sx + z0, d_sy + z0, twy);
+        fs_rows_inv<<<dim3((ny + G - 1) / G, nb), 256, row_smem, st>>>(C, d_out + off, nx, ny,
+                                                                     twx);
         count_launches(3);
         cudaError_t e = cudaGetLastError();
         if (e != cudaSuccess) {
@@ -869,14 +1032,16 @@ int cc_shifts_static(const float *d1, const float *d2, int nz, int ny, int nx, f
     const int G = rows_per_block(nx);
     const size_t row_smem = sizeof(float2) * (size_t)G * plen(nx);
     const size_t col_smem = sizeof(float2) * 2 * kColTile * (size_t)plen(ny);
-    if ((rc = set_smem((const void *)k_cc_rows_fwd, row_smem))) return rc;
-    if ((rc = set_smem((const void *)k_cc_rows_inv, row_smem))) return rc;
-    if ((rc = set_smem((const void *)k_cc_cols, col_smem))) return rc;
+    if ((rc = set_smem((const void *)k_cc_rows_fwd<false>, row_smem))) return rc;
+    if ((rc = set_smem((const void *)k_cc_rows_inv<false>, row_smem))) return rc;
+    if ((rc = set_smem((const void *)k_cc_cols<false>, col_smem))) return rc;
     const int H = nx / 2 + 1;
-    k_cc_rows_fwd<<<dim3((ny + G - 1) / G, nz), 256, row_smem, st>>>(d1, d2, Xh, Yh, nx, ny, twx);
-    k_cc_cols<<<dim3((H + kColTile - 1) / kColTile, nz), 256, col_smem, st>>>(Xh, Yh, nx, ny, twy,
+    k_cc_rows_fwd<false><<<dim3((ny + G - 1) / G, nz), 256, row_smem, st>>>(d1, d2, Xh, Yh, nx, ny,
+                                                                           twx);
+    k_cc_cols<false><<<dim3((H + kColTile - 1) / kColTile, nz), 256, col_smem, st>>>(Xh, Yh, nx, ny, twy,
                                                                             kColTile);
-    k_cc_rows_inv<<<dim3((ny + G - 1) / G, nz), 256, row_smem, st>>>(Xh, c, stats, nx, ny, twx);
+    k_cc_rows_inv<false><<<dim3((ny + G - 1) / G, nz), 256, row_smem, st>>>(Xh, c, stats, nx, ny,
+                                                                           twx);
     k_peak<<<nz, 256, 0, st>>>(c, stats, nx, ny, sx, sy, ix, iy);
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) {

@@ -47,6 +47,13 @@ struct Net {
     __nv_bfloat16 *wbf = nullptr, *wflip = nullptr;
     int step = 0;
     bool mirrors_fresh = false;
+    // training loss: loss_levels = 0 is the mean square error; > 0 adds the
+    // error pooled over 2^s x 2^s blocks for s = 1..loss_levels, weighted
+    // loss_ratio^s (low frequencies count more, as in the normal-equation
+    // residual the solver's stopping test measures)
+    int loss_levels = 0;
+    float loss_ratio = 1.f;
+    float *pyr = nullptr;
 
     // activations (P0 = maxN*H*W pixels, P1 = P0/4, ...)
     __nv_bfloat16 *a1, *e1, *q1, *a2, *e2, *q2, *a3, *e3, *q3, *a4, *e4;
@@ -138,7 +145,7 @@ static int create(Net **out, int H, int W, int maxN, int train, uint64_t seed) {
         A(grads, off) A(m, off) A(v, off) A(wflip, off)
         A(gX, P0 * 64) A(gY, P0 * 64) A(gpre, P0 * 32)
         A(de1, P0 * 32) A(de2, P1 * 64) A(de3, P2 * 128) A(out, P0) A(dout, P0)
-        A(partials, kLossBlocks)
+        A(partials, kLossBlocks) A(pyr, P0 / 3 + 64)
     }
 #undef A
     if (!rc && train) {
@@ -318,7 +325,11 @@ static int train_step(Net *n, const float *x, const float *target, int N, float 
     if (rc) return rc;
     const size_t P0 = (size_t)N * n->H * n->W;
     ARECGB_CUDA(cudaMemsetAsync(n->grads, 0, sizeof(float) * n->nparams, st));
-    mse(n->out, target, n->dout, n->partials, P0, 1.f / (float)P0, kLossBlocks, st);
+    if (n->loss_levels > 0)
+        multiscale_loss(n->out, target, n->pyr, n->dout, n->partials, N, n->H, n->W,
+                        n->loss_levels, n->loss_ratio, 1.f / (float)P0, kLossBlocks, st);
+    else
+        mse(n->out, target, n->dout, n->partials, P0, 1.f / (float)P0, kLossBlocks, st);
     if ((rc = backward(n, n->dout, st))) return rc;
     n->step++;
     const float b1 = 0.9f, b2 = 0.999f;
@@ -506,6 +517,19 @@ int arecgb_unet_images_to_volume(const arecgb_plan *plan, const float *d_img, fl
     arecgb::unet::img_to_cyl(d_img, p->d_rows, d_vol, p->nx, npad, p->ys, y0, count, scale,
                              (cudaStream_t)stream);
     ARECGB_CUDA(cudaGetLastError());
+    return 0;
+}
+
+int arecgb_unet_set_loss(arecgb_unet *net, int levels, float ratio) {
+    Net *n = N_(net);
+    if (!n || !n->train || levels < 0 || !(ratio > 0.f) || (levels > 0 &&
+        (n->H % (1 << levels) || n->W % (1 << levels)))) {
+        arecgb::set_error("arecgb_unet_set_loss: needs a training net, levels >= 0 with H and W "
+                          "divisible by 2^levels, ratio > 0");
+        return ARECGB_ERR_ARG;
+    }
+    n->loss_levels = levels;
+    n->loss_ratio = ratio;
     return 0;
 }
 

@@ -47,6 +47,12 @@ void conv_wgrad(const __nv_bfloat16 *x, const __nv_bfloat16 *dpre, float *gw, fl
 void flip_weights(const float *w, __nv_bfloat16 *wt, int Cin, int Cout, cudaStream_t st);
 void mse(const float *out, const float *target, float *dout, double *partial, size_t n, float scale,
          int nblocks, cudaStream_t st);
+// Multi-scale loss (sum over levels s = 0..levels of ratio^s x the mean square
+// of the error averaged over 2^s x 2^s blocks) and its gradient; pyr holds the
+// pooled levels (N H W / 3 floats suffice).
+void multiscale_loss(const float *out, const float *target, float *pyr, float *dout,
+                     double *partial, int N, int H, int W, int levels, float ratio, float scale,
+                     int nblocks, cudaStream_t st);
 void adamw(float *w, const float *g, float *m, float *v, size_t n, float lr, float b1, float b2,
            float eps, float wd, float bc1, float bc2, cudaStream_t st);
 void cyl_to_img(const float *vol, const RowInfo *rows, float *img, int nx, int npad, int ys,

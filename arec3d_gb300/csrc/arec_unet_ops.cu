@@ -391,6 +391,60 @@ __global__ void k_mse(const float *__restrict__ out, const float *__restrict__ t
     if (threadIdx.x == 0) partial[blockIdx.x] = red[0];
 }
 
+// Multi-scale loss: level s of the error pyramid is the error out - target
+// averaged over 2^s x 2^s blocks (level 0 the error itself).  Pooling by 2 of
+// level s-1 into level s; level 1 is pooled straight from out - target.
+__global__ void k_err_pool(const float *__restrict__ a, const float *__restrict__ b,
+                           float *__restrict__ y, int N, int H, int W) {
+    const int Ho = H / 2, Wo = W / 2;
+    GRID_STRIDE(p, (size_t)N * Ho * Wo) {
+        const int xo = (int)(p % Wo), yo = (int)((p / Wo) % Ho), n = (int)(p / ((size_t)Wo * Ho));
+        const size_t i0 = ((size_t)n * H + 2 * yo) * W + 2 * xo;
+        float s = a[i0] + a[i0 + 1] + a[i0 + W] + a[i0 + W + 1];
+        if (b) s -= b[i0] + b[i0 + 1] + b[i0 + W] + b[i0 + W + 1];
+        y[p] = 0.25f * s;
+    }
+}
+
+// dout = scale * 2 * sum_s alpha_s * level_s(block of p), alpha_s = ratio^s
+// (each level's mean square, summed with weight alpha_s, is the loss; a pixel
+// carries 4^-s of its level-s cell's square).
+__global__ void k_multiscale_grad(const float *__restrict__ out, const float *__restrict__ target,
+                                  const float *__restrict__ pyr, float *__restrict__ dout,
+                                  double *__restrict__ partial, int N, int H, int W, int levels,
+                                  float ratio, float scale) {
+    __shared__ double red[256];
+    double acc = 0.0;
+    GRID_STRIDE(p, (size_t)N * H * W) {
+        const int x = (int)(p % W), yy = (int)((p / W) % H), n = (int)(p / ((size_t)W * H));
+        const float e = out[p] - target[p];
+        float g = e, a = 1.0f;
+        double l = (double)e * e;
+        const float *lev = pyr;
+        int h = H, w = W;
+        double frac = 1.0;
+        for (int s = 1; s <= levels; s++) {
+            h >>= 1;
+            w >>= 1;
+            a *= ratio;
+            frac *= 0.25;
+            const float v = lev[((size_t)n * h + (yy >> s)) * w + (x >> s)];
+            g += a * v;
+            l += (double)a * v * v * frac;
+            lev += (size_t)N * h * w;
+        }
+        dout[p] = scale * 2.f * g;
+        acc += l;
+    }
+    red[threadIdx.x] = acc;
+    __syncthreads();
+    for (int o = 128; o > 0; o >>= 1) {
+        if ((int)threadIdx.x < o) red[threadIdx.x] += red[threadIdx.x + o];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) partial[blockIdx.x] = red[0];
+}
+
 // AdamW on fp32 master weights; refreshes the bf16 copy.
 __global__ void k_adamw(float *__restrict__ w, const float *__restrict__ g, float *__restrict__ m,
                         float *__restrict__ v, size_t n, float lr, float b1, float b2, float eps,
@@ -525,6 +579,26 @@ void flip_weights(const float *w, __nv_bfloat16 *wt, int Cin, int Cout, cudaStre
 void mse(const float *out, const float *target, float *dout, double *partial, size_t n, float scale,
          int nblocks, cudaStream_t st) {
     k_mse<<<nblocks, 256, 0, st>>>(out, target, dout, partial, n, scale);
+}
+void multiscale_loss(const float *out, const float *target, float *pyr, float *dout,
+                     double *partial, int N, int H, int W, int levels, float ratio, float scale,
+                     int nblocks, cudaStream_t st) {
+    float *lev = pyr;
+    const float *prev = nullptr;
+    int h = H, w = W;
+    for (int s = 1; s <= levels; s++) {
+        const size_t n = (size_t)N * (h / 2) * (w / 2);
+        if (s == 1)
+            k_err_pool<<<blocks_for(n), 256, 0, st>>>(out, target, lev, N, h, w);
+        else
+            k_err_pool<<<blocks_for(n), 256, 0, st>>>(prev, nullptr, lev, N, h, w);
+        prev = lev;
+        lev += n;
+        h /= 2;
+        w /= 2;
+    }
+    k_multiscale_grad<<<nblocks, 256, 0, st>>>(out, target, pyr, dout, partial, N, H, W, levels,
+                                               ratio, scale);
 }
 void adamw(float *w, const float *g, float *m, float *v, size_t n, float lr, float b1, float b2,
            float eps, float wd, float bc1, float bc2, cudaStream_t st) {

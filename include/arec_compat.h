@@ -108,9 +108,14 @@ int arecgb_init_weights(MPI_Comm comm, arecImage projections, arecImage *weights
 /* Alignment. */
 int arecgb_arecCCImages(MPI_Comm comm, arecImage images1, arecImage images2, float *sx,
                         float *sy);
+/* ccorr2d and arecCCImages: nx, ny in [2, 4096] with prime factors 2, 3, 5, 7
+ * (the reference's FFTW takes any length; other lengths return
+ * ARECGB_ERR_ARG from arecCCImages, and ccorr2d leaves c untouched and reports
+ * the error on stderr). */
 void arecgb_ccorr2d(int nx, int ny, float *x, float *y, float *c);
 void arecgb_speak(int nx, int ny, float *data, float *xt, float *yt);
-/* Fourier shift of one image (powers of two: nx 16..4096, ny 16..2048). */
+/* Fourier shift of one image (nx 2..4096, ny 2..2048, prime factors 2, 3, 5,
+ * 7; otherwise the output is left untouched and the error reported on stderr). */
 void arecgb_fshift2d(int nx, int ny, float *imagein, float *imageout, float sx, float sy);
 /* Rotation search and rotations (2 <= r2 <= min(2048, nx/2, ny/2)). */
 int arecgb_arecRotCCImages(MPI_Comm comm, arecImage images1, arecImage images2, int r2,

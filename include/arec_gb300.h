@@ -167,7 +167,9 @@ long long arecgb_launch_count(void);
  * memory, reference layout [nz][ny][nx] (replaces the loop of arecCCImages,
  * AREC3D/AREC3D/arecImage.cpp:414-428: ccorr2d + speak per pair).
  * sx, sy (device, nz floats): sub-pixel shifts; ix, iy (device, optional):
- * 0-based integer peak positions.  nx and ny must be powers of two in [16, 4096]. */
+ * 0-based integer peak positions.  nx and ny in [2, 4096] whose prime factors
+ * are 2, 3, 5 and 7 (powers of two take the fastest transforms); other
+ * lengths return ARECGB_ERR_ARG. */
 int arecgb_cc_shifts(const float *d_img1, const float *d_img2, int nz, int ny, int nx,
                      float *d_sx, float *d_sy, int *d_ix, int *d_iy, void *stream);
 
@@ -175,8 +177,9 @@ int arecgb_cc_shifts(const float *d_img1, const float *d_img2, int nz, int ny, i
  * (d_sx[i], d_sy[i]) pixels each (replaces the per-image loop over fshift2d,
  * AREC3D/AREC3D/align2dstack.cpp:566-630, used by the alignment driver,
  * AREC3D.cpp:219,230): out = Re(IDFT(DFT(in) exp(-2 pi i (sx kx + sy ky)))) /
- * (nx ny) with the reference's frequencies and float phase.  nx a power of two
- * in [16, 4096], ny in [16, 2048].  d_in and d_out may not overlap. */
+ * (nx ny) with the reference's frequencies and float phase.  nx in [2, 4096],
+ * ny in [2, 2048], both with prime factors 2, 3, 5 and 7 only.  d_in and d_out
+ * may not overlap. */
 int arecgb_fshift2d_device(const float *d_in, float *d_out, int nz, int ny, int nx,
                            const float *d_sx, const float *d_sy, void *stream);
 
@@ -349,6 +352,11 @@ int arecgb_unet_images_to_volume(const arecgb_plan *plan, const float *d_img, fl
  * x0 may equal x_early.  Follow with arecgb_cgls(..., warm = 1, ...). */
 int arecgb_warm_start(const arecgb_plan *plan, arecgb_unet *net, const float *d_x_early,
                       float *d_x0, float *d_img_in, float *d_img_out, void *stream);
+/* Training loss of a training net: levels = 0 (default) the mean square error
+ * over the images; levels > 0 adds, for s = 1..levels, ratio^s times the mean
+ * square of the error averaged over 2^s x 2^s blocks (H and W divisible by
+ * 2^levels), so low spatial frequencies weigh more. */
+int arecgb_unet_set_loss(arecgb_unet *net, int levels, float ratio);
 /* Image size and batch of a network (any pointer may be NULL). */
 int arecgb_unet_shape(const arecgb_unet *net, int *height, int *width, int *max_batch);
 

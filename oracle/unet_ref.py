@@ -141,3 +141,25 @@ def forward_and_grads(params, layers, nparams, x, dout, bf16=True):
     y = forward(t, xt, bf16=bf16)
     (y * torch.as_tensor(np.asarray(dout, np.float64))).sum().backward()
     return y.detach().numpy(), pack_grads(t, layers, nparams)
+
+
+def multiscale_loss_grad(out, target, levels, ratio):
+    """The library's multi-scale training loss and its gradient w.r.t. the
+    output, in FP64: with e = out - target and level s the error averaged over
+    2^s x 2^s blocks (level 0 = e), loss = sum_s ratio^s * mean(level_s^2) and
+    d loss / d out(p) = 2 / P * sum_s ratio^s * level_s(block of p), P the
+    number of pixels (the mean over level s is over P / 4^s cells, each holding
+    4^s pixels).  out, target: [N][H][W]."""
+    e = np.asarray(out, np.float64) - np.asarray(target, np.float64)
+    n, h, w = e.shape
+    P = e.size
+    loss = float(np.mean(e * e))
+    grad = e.copy()
+    lev = e
+    for s in range(1, levels + 1):
+        lev = 0.25 * (lev[:, 0::2, 0::2] + lev[:, 1::2, 0::2] + lev[:, 0::2, 1::2] +
+                      lev[:, 1::2, 1::2])
+        a = float(ratio) ** s
+        loss += a * float(np.mean(lev * lev))
+        grad += a * np.repeat(np.repeat(lev, 2 ** s, axis=1), 2 ** s, axis=2)
+    return loss, 2.0 / P * grad

@@ -113,12 +113,63 @@ def test_speak_rules(gb, oc):
 
 
 def test_bad_sizes_rejected(gb):
-    a = np.zeros((1, 48, 48), np.float32)
+    """Lengths with a prime factor above 7 are refused with ARECGB_ERR_ARG (and
+    a message naming the sizes); the reference's FFTW takes any length."""
+    a = np.zeros((1, 48, 97), np.float32)
     sx, sy, st = gb.arecCCImages(a, a)
     assert st == gb.ERR_ARG
+    assert "97" in gb.last_error()
 
 
-@pytest.mark.parametrize("shape", [(32, 64), (128, 128), (256, 512)])
+# Lengths that are not powers of two (prime factors 2, 3, 5, 7), as crops and
+# binning of real detectors give: the mixed-radix transforms against the
+# oracle's double-precision FFT (radix 2 + Bluestein), as the reference plans
+# FFTW for any nx, ny (AREC3D/AREC3D/align2dstack.cpp:490-520, 577-629).
+@pytest.mark.parametrize("shape", [(12, 20), (48, 60), (75, 100), (96, 210), (343, 250)])
+def test_ccorr2d_image_any_size(gb, oc, shape):
+    import torch
+
+    ny, nx = shape
+    a, b, _ = make_pairs(2, 1, ny, nx)
+    c_ref = oc.ccorr2d(a[0], b[0])
+    x, y = torch.from_numpy(a[0]).cuda(), torch.from_numpy(b[0]).cuda()
+    c = torch.zeros_like(x)
+    gb.ccorr2d_device(x, y, c)
+    assert rel_l2(c.cpu().numpy(), c_ref) < 1e-5
+    assert rel_l2(gb.ccorr2d(a[0], b[0]), c_ref) < 1e-5
+
+
+@pytest.mark.parametrize("shape", [(750, 1000), (1536, 2048), (1000, 750), (90, 96)])
+def test_shift_search_any_size(gb, oc, shape):
+    import torch
+
+    ny, nx = shape
+    nz = 3
+    a, b, truth = make_pairs(17, nz, ny, nx)
+    sx_ref, sy_ref = oc.cc_images(a, b, nthreads=oc.host_threads())
+    ix_ref, iy_ref = [], []
+    for i in range(nz):
+        _, _, ix, iy = oc.speak(oc.ccorr2d(a[i], b[i]))
+        ix_ref.append(ix)
+        iy_ref.append(iy)
+    da, db = torch.from_numpy(a).cuda(), torch.from_numpy(b).cuda()
+    sx = torch.zeros(nz, device="cuda")
+    sy = torch.zeros(nz, device="cuda")
+    ix = torch.zeros(nz, dtype=torch.int32, device="cuda")
+    iy = torch.zeros(nz, dtype=torch.int32, device="cuda")
+    gb.cc_shifts(da, db, sx, sy, ix, iy)
+    assert ix.cpu().numpy().tolist() == ix_ref
+    assert iy.cpu().numpy().tolist() == iy_ref
+    assert np.abs(sx.cpu().numpy() - sx_ref).max() < 0.05
+    assert np.abs(sy.cpu().numpy() - sy_ref).max() < 0.05
+    assert np.abs(sx.cpu().numpy() - truth[:, 0]).max() < 0.25
+    sx2, sy2, st = gb.arecCCImages(a, b)
+    assert st == 0
+    np.testing.assert_array_equal(sx2, sx.cpu().numpy())
+
+
+@pytest.mark.parametrize("shape", [(32, 64), (128, 128), (256, 512), (60, 90), (250, 375),
+                                   (21, 35)])
 def test_fshift2d_matches_oracle(gb, oc, shape):
     """Fourier shift of an image stack (fshift2d, align2dstack.cpp:566-630)
     against the oracle (pinned to the reference build), through the device

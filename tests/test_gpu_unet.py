@@ -219,3 +219,42 @@ def test_unet_train_step_reduces_loss(gb):
     losses = [net.train_step(xd, td, 2e-3) for _ in range(60)]
     print("unet training loss %.4e -> %.4e" % (losses[0], losses[-1]))
     assert losses[-1] < 0.2 * losses[0]
+
+
+def test_multiscale_loss_against_oracle(gb):
+    """The multi-scale training loss (error pooled over 2^s blocks, weight
+    ratio^s): the loss the library reports matches the oracle's formula on the
+    network's own output, and the gradient it trains with agrees with the
+    oracle's d loss / d out pushed through the (separately checked) backward
+    kernels: on AdamW's first steps every parameter moves against the sign of
+    its gradient."""
+    import torch
+
+    from oracle import unet_ref
+
+    size, batch, levels, ratio = 64, 2, 4, 2.0
+    net = gb.UNet(size, batch, train=True, seed=9)
+    net.set_loss(levels, ratio)
+    rng = np.random.default_rng(9)
+    x = _inputs(rng, batch, size)
+    target = (x + 0.3 * np.roll(x, 2, axis=1) + 0.2).astype(np.float32)
+    xd, td = torch.from_numpy(x).cuda(), torch.from_numpy(target).cuda()
+    y = torch.zeros_like(xd)
+    net.forward(xd, y)
+    loss_ref, dout = unet_ref.multiscale_loss_grad(y.cpu().numpy(), target, levels, ratio)
+    p0 = torch.zeros(net.nparams, device="cuda")
+    net.get_params(p0)
+    loss = net.train_step(xd, td, 0.0)  # lr 0: the parameters stay
+    assert loss == pytest.approx(loss_ref, rel=1e-5)
+    g = torch.zeros(net.nparams, device="cuda")
+    net.forward(xd, y)
+    net.backward(torch.from_numpy(dout.astype(np.float32)).cuda(), g)
+    net.train_step(xd, td, 1e-4)
+    p1 = torch.zeros_like(p0)
+    net.get_params(p1)
+    g, step = g.cpu().numpy(), (p1 - p0).cpu().numpy()
+    big = np.abs(g) > 1e-3 * np.abs(g).max()
+    agree = np.mean(np.sign(step[big]) == -np.sign(g[big]))
+    print("multi-scale loss %.6e (oracle %.6e); update direction agrees on %.4f of %d params"
+          % (loss, loss_ref, agree, int(big.sum())))
+    assert agree > 0.999
