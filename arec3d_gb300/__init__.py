@@ -26,6 +26,13 @@ LIN, KB, SQ = 1, 2, 3
 ERR_ARG, ERR_NOMEM, ERR_CUDA_BASE = -90, -91, -100
 
 
+class Problem(C.Structure):
+    """`arecgb_problem`: one cylinder of an uneven batch (device buffers)."""
+    _fields_ = [("weighting", C.c_int), ("radius", C.c_double), ("ny", C.c_int),
+                ("nangles", C.c_int), ("angles", C.POINTER(C.c_float)), ("d_b", C.c_void_p),
+                ("d_x", C.c_void_p)]
+
+
 class SolveInfo(C.Structure):
     _fields_ = [("iterations", C.c_int), ("iterbest", C.c_int), ("restarts", C.c_int),
                 ("status", C.c_int), ("lam_final", C.c_float), ("rnorm0", C.c_double),
@@ -162,6 +169,10 @@ def lib():
         L.arecgb_warm_start.argtypes = [vp, vp, vp, vp, vp, vp, vp]
         L.arecgb_unet_shape.argtypes = [vp, ip, ip, ip]
         L.arecgb_unet_set_loss.argtypes = [vp, C.c_int, C.c_float]
+        L.arecgb_cylinder_info.argtypes = [C.c_double, C.c_int, ip, ip, ip]
+        L.arecgb_solve_uneven.argtypes = [C.POINTER(Problem), C.c_int, C.c_size_t, vp, C.c_int,
+                                          C.c_float, C.c_int, C.c_float, C.POINTER(SolveInfo),
+                                          ip, vp]
         L.arecgb_reconstruct_host.argtypes = [vp, vp, vp, vp, C.c_int, C.c_float, C.c_int,
                                               C.c_float, C.POINTER(SolveInfo), vp]
         L.arecgb_plan_timing.argtypes = [vp, C.c_int, dp, C.POINTER(C.c_longlong), dp,
@@ -433,6 +444,36 @@ def cgls_batch(plans, bs, xs, maxit, tol, warm=None, rnorm_ref=None, stream=None
     _check(lib().arecgb_cgls_batch(hp, hb, hx, w, n, maxit, tol, rr, info, _stream(stream)),
            "arecgb_cgls_batch")
     return list(info)
+
+
+def cylinder_info(radius, ny):
+    """(nx, nrays, ys) of the reference's cylinder of this radius with ny slices."""
+    nx, nr, ys = C.c_int(), C.c_int(), C.c_int()
+    _check(lib().arecgb_cylinder_info(float(radius), int(ny), C.byref(nx), C.byref(nr),
+                                      C.byref(ys)), "arecgb_cylinder_info")
+    return nx.value, nr.value, ys.value
+
+
+def solve_uneven(problems, budget_bytes, maxit=200, tol=1e-3, net=None, stream=None):
+    """Uneven batch (arecgb_solve_uneven).  problems: list of dicts with
+    weighting, radius, ny, angles (float32 array), b and x (device tensors in
+    the device layouts).  Returns (list of SolveInfo, list of wave indices)."""
+    n = len(problems)
+    arr = (Problem * n)()
+    keep = []
+    for i, p in enumerate(problems):
+        ang = np.ascontiguousarray(p["angles"], dtype=np.float32)
+        keep.append(ang)
+        arr[i] = Problem(int(p.get("weighting", SQ)), float(p["radius"]), int(p["ny"]), len(ang),
+                         ang.ctypes.data_as(C.POINTER(C.c_float)), _ptr(p["b"]), _ptr(p["x"]))
+    info = (SolveInfo * n)()
+    waves = (C.c_int * n)()
+    sirt_iters = getattr(net, "sirt_iters", 0) if net is not None else 0
+    lam_scale = getattr(net, "sirt_lam_scale", 1.0) if net is not None else 1.0
+    _check(lib().arecgb_solve_uneven(arr, n, int(budget_bytes), net._h if net is not None else None,
+                                     int(sirt_iters), float(lam_scale), int(maxit), float(tol),
+                                     info, waves, _stream(stream)), "arecgb_solve_uneven")
+    return list(info), list(waves)
 
 
 def launch_count():

@@ -66,7 +66,7 @@ static int choose_vec(int ys) {
 }
 
 int plan_create(Plan **out, int weighting, double radius, int ny, int nangles,
-                const float *angles_host) {
+                const float *angles_host, bool tables) {
     *out = nullptr;
     if (weighting < ARECGB_LIN || weighting > ARECGB_SQ) {
         set_error("plan_create: weighting must be 1 (LIN), 2 (KB) or 3 (SQ)");
@@ -259,7 +259,7 @@ int plan_create(Plan **out, int weighting, double radius, int ny, int nangles,
         plan_destroy(p);
         return cuda_status(e);
     }
-    if (int rc = plan_build_tables(p)) {
+    if (int rc = tables ? plan_build_tables(p) : 0) {
         plan_destroy(p);
         return rc;
     }

@@ -135,8 +135,10 @@ constexpr int kGroupAngles = 4;        // angles per forward-projection block
 constexpr int kFpBins = 8;             // detector bins per forward-projection block
 
 // Geometry / plans (arec_geometry.cu)
+// tables = false: never build the optional projector tables (the kernels then
+// compute the same values as they go; for callers that budget device memory).
 int plan_create(Plan **out, int weighting, double radius, int ny, int nangles,
-                const float *angles_host);
+                const float *angles_host, bool tables = true);
 void plan_destroy(Plan *p);
 size_t vol_floats(const Plan *p);
 size_t sin_floats(const Plan *p);

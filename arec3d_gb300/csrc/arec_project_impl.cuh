@@ -208,6 +208,30 @@ __device__ __forceinline__ void cp_async_wait() {
     asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory");
 }
 
+// lds_lane when `pred` is nonzero, else the registers keep their values: a
+// predicated shared-memory load (no branch, no bandwidth when off).  VEC >= 4.
+// `a` is the shared-memory address of the lane's first piece (lane_piece(lane,
+// 0)); the second piece of VEC = 8 is 128 floats further.
+template <int VEC>
+__device__ __forceinline__ void lds_lane_if(unsigned pred, unsigned a, float (&v)[VEC]) {
+    static_assert(VEC == 4 || VEC == 8, "one or two float4 pieces");
+    if constexpr (VEC == 8) {
+        asm volatile(
+            "{\n\t.reg .pred p;\n\tsetp.ne.u32 p, %8, 0;\n\t"
+            "@p ld.shared.v4.f32 {%0, %1, %2, %3}, [%9];\n\t"
+            "@p ld.shared.v4.f32 {%4, %5, %6, %7}, [%9+512];\n\t}\n"
+            : "+f"(v[0]), "+f"(v[1]), "+f"(v[2]), "+f"(v[3]), "+f"(v[4]), "+f"(v[5]), "+f"(v[6]),
+              "+f"(v[7])
+            : "r"(pred), "r"(a));
+    } else {
+        asm volatile(
+            "{\n\t.reg .pred p;\n\tsetp.ne.u32 p, %4, 0;\n\t"
+            "@p ld.shared.v4.f32 {%0, %1, %2, %3}, [%5];\n\t}\n"
+            : "+f"(v[0]), "+f"(v[1]), "+f"(v[2]), "+f"(v[3])
+            : "r"(pred), "r"(a));
+    }
+}
+
 // One staged footprint row (a bin's slices) into a lane's registers; a bin off
 // the detector was never copied and reads as zero.
 template <int VEC>
@@ -269,6 +293,7 @@ __device__ __forceinline__ float4 bp_plan(const OpArgs &A, const float4 &myray, 
         hi = max(hi, __shfl_xor_sync(0xffffffffu, hi, o));
     }
     const bool use = b != INT_MIN / 2 && b - lo <= FW - 3;
+    if (!use) t.w0 = t.w1 = t.w2 = 0.f;  // code 0: the ray adds nothing
     const int gbase = lane & ~7;
     int cb = INT_MIN / 4, m = 0, my_code = 0, my_m = 0;
 #pragma unroll
@@ -456,6 +481,10 @@ __global__ void __launch_bounds__(128 * NSC, NSC == 1 ? 4 : 1)
     for (int r = 0; r < 8; r++)
 #pragma unroll
         for (int q = 0; q < VEC; q++) acc[r][q] = 0.f;
+    // the register ring; zero until a ray loads it (finite for zero weights)
+    float R0[VEC], R1[VEC], R2[VEC];
+#pragma unroll
+    for (int q = 0; q < VEC; q++) R0[q] = R1[q] = R2[q] = 0.f;
 
     bool ok = true;
     int t0 = 0;  // angles staged before this chunk (buffer t % NB, use t / NB)
@@ -504,29 +533,50 @@ __global__ void __launch_bounds__(128 * NSC, NSC == 1 ? 4 : 1)
             if (ok && yok) {
                 const float *F = foot + (size_t)buf * FW * SPAN + yw;
                 // the ring (slots 0, 1, 2); a warp's first used ray loads all three
-                float R0[VEC], R1[VEC], R2[VEC];
+                if constexpr (VEC >= 4) {
+                    // branch-free: each slot's load is predicated on the plan's
+                    // code; rays with code 0 have zero weights (and the ring
+                    // holds finite staged values), so their FMAs add nothing
+                    const unsigned Fa = smem_u32(F + lane_piece<VEC>(lane, 0));
 #pragma unroll
-                for (int r = 0; r < 8; r++) {
-                    const float4 e = sw[ai * 32 + rg * 8 + r];
-                    const int code = __float_as_int(e.x), act = code & 3;
-                    if (act == 0) continue;
-                    const float *row = F + (code >> 8) * SPAN;
-                    if (act == 2) {
+                    for (int r = 0; r < 8; r++) {
+                        const float4 e = sw[ai * 32 + rg * 8 + r];
+                        const int code = __float_as_int(e.x), act = code & 3;
                         const int slot = (code >> 2) & 3;
-                        if (slot == 0)
-                            lds_lane<VEC>(row, lane, R0);
-                        else if (slot == 1)
-                            lds_lane<VEC>(row, lane, R1);
-                        else
-                            lds_lane<VEC>(row, lane, R2);
-                    } else if (act == 3) {
-                        lds_lane<VEC>(row, lane, R0);
-                        lds_lane<VEC>(row + SPAN, lane, R1);
-                        lds_lane<VEC>(row + 2 * SPAN, lane, R2);
+                        const bool all3 = act == 3, one = act == 2;
+                        const unsigned a = Fa + (unsigned)(code >> 8) * (SPAN * 4u);
+                        const unsigned step = all3 ? SPAN * 4u : 0u;
+                        lds_lane_if<VEC>(all3 || (one && slot == 0), a, R0);
+                        lds_lane_if<VEC>(all3 || (one && slot == 1), a + step, R1);
+                        lds_lane_if<VEC>(all3 || (one && slot == 2), a + 2 * step, R2);
+                        fma_row<VEC>(acc[r], e.y, R0);
+                        fma_row<VEC>(acc[r], e.z, R1);
+                        fma_row<VEC>(acc[r], e.w, R2);
                     }
-                    fma_row<VEC>(acc[r], e.y, R0);
-                    fma_row<VEC>(acc[r], e.z, R1);
-                    fma_row<VEC>(acc[r], e.w, R2);
+                } else {
+#pragma unroll
+                    for (int r = 0; r < 8; r++) {
+                        const float4 e = sw[ai * 32 + rg * 8 + r];
+                        const int code = __float_as_int(e.x), act = code & 3;
+                        if (act == 0) continue;
+                        const float *row = F + (code >> 8) * SPAN;
+                        if (act == 2) {
+                            const int slot = (code >> 2) & 3;
+                            if (slot == 0)
+                                lds_lane<VEC>(row, lane, R0);
+                            else if (slot == 1)
+                                lds_lane<VEC>(row, lane, R1);
+                            else
+                                lds_lane<VEC>(row, lane, R2);
+                        } else if (act == 3) {
+                            lds_lane<VEC>(row, lane, R0);
+                            lds_lane<VEC>(row + SPAN, lane, R1);
+                            lds_lane<VEC>(row + 2 * SPAN, lane, R2);
+                        }
+                        fma_row<VEC>(acc[r], e.y, R0);
+                        fma_row<VEC>(acc[r], e.z, R1);
+                        fma_row<VEC>(acc[r], e.w, R2);
+                    }
                 }
             }
             __syncwarp();  // this warp's reads of the buffer are done

@@ -406,9 +406,9 @@ __global__ void k_err_pool(const float *__restrict__ a, const float *__restrict_
     }
 }
 
-// dout = scale * 2 * sum_s alpha_s * level_s(block of p), alpha_s = ratio^s
-// (each level's mean square, summed with weight alpha_s, is the loss; a pixel
-// carries 4^-s of its level-s cell's square).
+// dout = scale * 2 * sum_s alpha_s * level_s(block of p), alpha_s = ratio^s;
+// the loss sum_s alpha_s * mean(level_s^2) is accumulated per pixel as
+// sum_s alpha_s * level_s(block of p)^2 (the caller divides by the pixels).
 __global__ void k_multiscale_grad(const float *__restrict__ out, const float *__restrict__ target,
                                   const float *__restrict__ pyr, float *__restrict__ dout,
                                   double *__restrict__ partial, int N, int H, int W, int levels,
@@ -422,15 +422,14 @@ __global__ void k_multiscale_grad(const float *__restrict__ out, const float *__
         double l = (double)e * e;
         const float *lev = pyr;
         int h = H, w = W;
-        double frac = 1.0;
         for (int s = 1; s <= levels; s++) {
             h >>= 1;
             w >>= 1;
             a *= ratio;
-            frac *= 0.25;
             const float v = lev[((size_t)n * h + (yy >> s)) * w + (x >> s)];
             g += a * v;
-            l += (double)a * v * v * frac;
+            // summed over the cell's 4^s pixels and divided by P: the cell mean
+            l += (double)a * v * v;
             lev += (size_t)N * h * w;
         }
         dout[p] = scale * 2.f * g;

@@ -360,6 +360,43 @@ int arecgb_unet_set_loss(arecgb_unet *net, int levels, float ratio);
 /* Image size and batch of a network (any pointer may be NULL). */
 int arecgb_unet_shape(const arecgb_unet *net, int *height, int *width, int *max_batch);
 
+/* Detector bins nx = round(2 radius + 1), rays and slice stride ys of the
+ * reference's cylinder of this radius (arecAllocateCylImage,
+ * AREC3D/AREC3D/arecImage.cpp:29-86), without creating a plan: the sizes of
+ * the device layouts (volume [nrays][ys], sinogram [nangles][nx][ys]). */
+int arecgb_cylinder_info(double radius, int ny, int *nx, int *nrays, int *ys);
+
+/* One problem of an uneven batch: weighting, cylinder radius, slices, angles
+ * (host, radians) and its device sinogram (read) and volume (written), in the
+ * device layouts (arecgb_cylinder_info gives the sizes; padding slices zero). */
+typedef struct arecgb_problem {
+    int weighting;
+    double radius;
+    int ny;
+    int nangles;
+    const float *angles;
+    const float *d_b;
+    float *d_x;
+} arecgb_problem;
+
+/* Many cylinders of uneven radius, width, slices and angles on one GPU (no
+ * counterpart in the reference, which solves one cylinder per run over MPI
+ * ranks, AREC3D/AREC3D/AREC3D.cpp:293-315).  Inputs and results stay where
+ * the caller put them; the solver workspace of all problems may exceed device
+ * memory, so the problems are packed into waves whose workspace fits
+ * budget_bytes (first fit, largest first; a problem above the budget runs
+ * alone).  Per wave: a plan per problem (without the optional projector
+ * tables), with `net` the learned warm start per problem (SIRT of sirt_iters
+ * iterations at step sirt_lam_scale / (nangles nx), then the network; every
+ * nx must fit the network's images), then one batched CGLS of all the wave's
+ * problems, one CUDA graph launch per iteration, each to
+ * ||A^T r|| / ||A^T b|| <= tol (max maxit iterations).  info[i] (may be NULL)
+ * receives problem i's CGLS summary and wave_of[i] (may be NULL) its wave.
+ * Synchronises. */
+int arecgb_solve_uneven(const arecgb_problem *probs, int n, size_t budget_bytes,
+                        arecgb_unet *net, int sirt_iters, float sirt_lam_scale, int maxit,
+                        float tol, arecgb_solve_info *info, int *wave_of, void *stream);
+
 /* One reconstruction end to end over HOST buffers in the reference's layouts
  * (the path a caller without device memory of its own takes; no counterpart
  * in the reference, whose cyl_cgls_SQ is the net == NULL case):

@@ -269,16 +269,20 @@ def compat():
             b = O.project(O.KB, 32.0, xt, ang)
             b = (b + 0.01 * rng.standard_normal(b.shape)).astype(np.float32)
             out["kb65_b"] = b
-            x, st = R.solve("cyl_cgls_KB", b, ang, 0.0, 8, 1e-7)
+            x, st = R.solve("cyl_cgls_KB", b, ang, 0.0, 6, 1e-7)
             assert st == 0
             out["kb65_cgls"] = x
+            out["kb65_maxit"] = np.array(6)
             x0 = (x * 0.5).astype(np.float32)
+            maxit = 5
         else:
             x0 = small["solve_sq_sirt"]
+            maxit = 6
         out["warm_%s_x0" % tag] = x0
-        x, st = R.solve("cyl_cgls" + nm, b, ang, 0.0, 6, 1e-7, x0=x0)
+        x, st = R.solve("cyl_cgls" + nm, b, ang, 0.0, maxit, 1e-7, x0=x0)
         assert st == 0
         out["warm_%s_cgls" % tag] = x
+        out["warm_%s_maxit" % tag] = np.array(maxit)
     b = small["solve_sq_b"]
     (_, st), text = _stdout_of(lambda: R.solve("cyl_cgls_SQ", b, ang, 0.0, 10, 1e-7))
     assert st == 0
