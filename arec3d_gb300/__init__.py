@@ -170,9 +170,9 @@ def lib():
         L.arecgb_unet_shape.argtypes = [vp, ip, ip, ip]
         L.arecgb_unet_set_loss.argtypes = [vp, C.c_int, C.c_float]
         L.arecgb_cylinder_info.argtypes = [C.c_double, C.c_int, ip, ip, ip]
-        L.arecgb_solve_uneven.argtypes = [C.POINTER(Problem), C.c_int, C.c_size_t, vp, C.c_int,
-                                          C.c_float, C.c_int, C.c_float, C.POINTER(SolveInfo),
-                                          ip, vp]
+        L.arecgb_solve_uneven.argtypes = [C.POINTER(Problem), C.c_int, C.c_size_t,
+                                          C.POINTER(vp), C.c_int, C.c_int, C.c_double, C.c_int,
+                                          C.c_float, C.POINTER(SolveInfo), ip, vp]
         L.arecgb_reconstruct_host.argtypes = [vp, vp, vp, vp, C.c_int, C.c_float, C.c_int,
                                               C.c_float, C.POINTER(SolveInfo), vp]
         L.arecgb_plan_timing.argtypes = [vp, C.c_int, dp, C.POINTER(C.c_longlong), dp,
@@ -454,10 +454,13 @@ def cylinder_info(radius, ny):
     return nx.value, nr.value, ys.value
 
 
-def solve_uneven(problems, budget_bytes, maxit=200, tol=1e-3, net=None, stream=None):
+def solve_uneven(problems, budget_bytes, maxit=200, tol=1e-3, nets=None, stream=None):
     """Uneven batch (arecgb_solve_uneven).  problems: list of dicts with
     weighting, radius, ny, angles (float32 array), b and x (device tensors in
-    the device layouts).  Returns (list of SolveInfo, list of wave indices)."""
+    the device layouts); nets: warm-start networks (the same parameters at
+    several image sizes) or None.  Returns (list of SolveInfo, list of wave
+    indices)."""
+    nets = list(nets or [])
     n = len(problems)
     arr = (Problem * n)()
     keep = []
@@ -468,11 +471,12 @@ def solve_uneven(problems, budget_bytes, maxit=200, tol=1e-3, net=None, stream=N
                          ang.ctypes.data_as(C.POINTER(C.c_float)), _ptr(p["b"]), _ptr(p["x"]))
     info = (SolveInfo * n)()
     waves = (C.c_int * n)()
-    sirt_iters = getattr(net, "sirt_iters", 0) if net is not None else 0
-    lam_scale = getattr(net, "sirt_lam_scale", 1.0) if net is not None else 1.0
-    _check(lib().arecgb_solve_uneven(arr, n, int(budget_bytes), net._h if net is not None else None,
-                                     int(sirt_iters), float(lam_scale), int(maxit), float(tol),
-                                     info, waves, _stream(stream)), "arecgb_solve_uneven")
+    hn = (C.c_void_p * max(1, len(nets)))(*[nt._h.value for nt in nets])
+    sirt_iters = getattr(nets[0], "sirt_iters", 0) if nets else 0
+    lam_scale = getattr(nets[0], "sirt_lam_scale", 1.0) if nets else 1.0
+    _check(lib().arecgb_solve_uneven(arr, n, int(budget_bytes), hn, len(nets), int(sirt_iters),
+                                     float(lam_scale), int(maxit), float(tol), info, waves,
+                                     _stream(stream)), "arecgb_solve_uneven")
     return list(info), list(waves)
 
 

@@ -284,6 +284,8 @@ void plan_destroy(Plan *p) {
     cudaFree(p->d_tiles);
     cudaFree(p->d_taps);
     cudaFree(p->d_kinv);
+    cudaFree(p->d_lin_off);
+    cudaFree(p->d_lin_list);
     cudaFree(p->d_xT);
     cudaFree(p->d_bpw);
     cudaFree(p->d_bpf);

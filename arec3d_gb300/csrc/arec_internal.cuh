@@ -74,6 +74,8 @@ struct Plan {
     // kernels compute the same values without them.
     float4 *d_taps = nullptr;     // [ngroups][nrays][4], rays in each group's line order
     int *d_kinv = nullptr;        // column-major ray index -> ray index
+    int *d_lin_off = nullptr;     // linear weighting: per angle, rays by first bin (offsets)
+    int *d_lin_list = nullptr;    //   and the rays themselves (see k_lin_index)
     float *d_xT = nullptr;        // [nrays][ys]: x in column-major ray order (column sweeps)
     float4 *d_bpw = nullptr;      // [ntiles][na][32]
     int2 *d_bpf = nullptr;        // [ntiles][na]

@@ -14,6 +14,7 @@ int launch_bp_kb(const OpArgs &, int, int, dim3, const float *, float *, const C
 int launch_bp_sq(const OpArgs &, int, int, dim3, const float *, float *, const CUtensorMap &,
                  int, cudaStream_t);
 int launch_fp_lin(const OpArgs &, int, const float *, float *, cudaStream_t);
+int launch_lin_index(const OpArgs &, int *, int *, cudaStream_t);
 int launch_tables_sq(const OpArgs &, int, float4 *, float4 *, int2 *, cudaStream_t);
 int launch_tables_kb(const OpArgs &, int, float4 *, float4 *, int2 *, cudaStream_t);
 int launch_fpb_kb(const OpArgs &, int, dim3, const float *, float *, int, int, int, int,
@@ -44,6 +45,8 @@ static OpArgs make_args(const Plan *p, const int *skip) {
     A.bpw = p->d_bpw;
     A.bpf = p->d_bpf;
     A.kinv = p->d_kinv;
+    A.lin_off = p->d_lin_off;
+    A.lin_list = p->d_lin_list;
     return A;
 }
 
@@ -153,8 +156,8 @@ int forward_project(const Plan *p, const float *d_x, float *d_q, double *d_norm2
         const int ntile = (p->nx + kFpBins - 1) / kFpBins;
         rc = 0;
         // With the tables: tensor maps over x and over its column-major copy
-        // (gathered here when there are column sweeps), box = 32 rays x SPAN
-        // slices; the kernels stage each line's pixels as one tile.
+        // (gathered here when there are column sweeps), box = 8 rays x SPAN
+        // slices; the kernels stage a line's n pixels as ceil(n / 8) boxes.
         CUtensorMap tmx, tmxT;
         memset(&tmx, 0, sizeof(tmx));
         memset(&tmxT, 0, sizeof(tmxT));
@@ -168,8 +171,8 @@ int forward_project(const Plan *p, const float *d_x, float *d_q, double *d_norm2
                     p->d_kinv, p->nrays, ys4);
                 count_launches(1);
             }
-            if (!encode_rows_map(&tmx, d_x, p->ys, p->nrays, span, kFpStage) ||
-                !encode_rows_map(&tmxT, p->d_xT, p->ys, p->nrays, span, kFpStage)) {
+            if (!encode_rows_map(&tmx, d_x, p->ys, p->nrays, span, kFpBox) ||
+                !encode_rows_map(&tmxT, p->d_xT, p->ys, p->nrays, span, kFpBox)) {
                 set_error("forward_project: tensor map encoding failed");
                 return ARECGB_ERR_ARG;
             }
@@ -242,8 +245,36 @@ int back_project(const Plan *p, const float *d_s, float *d_g, double *d_norm2,
 // otherwise the kernels compute the same values as they go.  The tables hold
 // exactly what the kernels would compute (the same device functions), so
 // results do not depend on them.
+// The linear weighting's ray index (per angle, the rays grouped by first bin:
+// na x (nrays + nx + 2) ints), which makes its forward projection a gather
+// with a fixed summation order.  Built when it takes at most 40 % of the free
+// memory (else the forward projection scatters with atomics).
+static int plan_build_lin_index(Plan *p) {
+    const size_t b_off = sizeof(int) * (size_t)p->na * (p->nx + 2);
+    const size_t b_list = sizeof(int) * (size_t)p->na * p->nrays;
+    size_t free_b = 0, total_b = 0;
+    if (cudaMemGetInfo(&free_b, &total_b) != cudaSuccess) return 0;
+    if ((double)(b_off + b_list) > 0.4 * (double)free_b) return 0;
+    if (cudaMalloc(&p->d_lin_off, b_off) != cudaSuccess ||
+        cudaMalloc(&p->d_lin_list, b_list) != cudaSuccess) {
+        cudaGetLastError();  // not sticky: run with the scatter
+        cudaFree(p->d_lin_off);
+        cudaFree(p->d_lin_list);
+        p->d_lin_off = nullptr;
+        p->d_lin_list = nullptr;
+        return 0;
+    }
+    const OpArgs A = make_args(p, nullptr);
+    launch_lin_index(A, p->d_lin_off, p->d_lin_list, p->stream);
+    count_launches(1);
+    ARECGB_CUDA(cudaGetLastError());
+    ARECGB_CUDA(cudaStreamSynchronize(p->stream));
+    p->table_bytes = b_off + b_list;
+    return 0;
+}
+
 int plan_build_tables(Plan *p) {
-    if (p->weighting == ARECGB_LIN) return 0;
+    if (p->weighting == ARECGB_LIN) return plan_build_lin_index(p);
     const char *env = getenv("ARECGB_PLAN_TABLES");
     if (env && env[0] == '0') return 0;
     const size_t b_taps = sizeof(float4) * (size_t)p->ngroups * p->nrays * 4 +

@@ -50,6 +50,11 @@ struct OpArgs {
     double *partials;
     const int *skip;
     int *err;
+    // linear weighting: per angle, the rays grouped by first bin (lin_off
+    // [na][nx+2]: bucket j holds the rays whose first bin is j - 1; lin_list
+    // [na][nrays]: ray indices, ascending within a bucket)
+    const int *lin_off;
+    const int *lin_list;
     // optional per-plan tables (null when the plan has none)
     const float4 *taps;  // [ngroups][nrays][4]: ray_taps of each forward-projection angle
                          // group's (up to 4) angles per ray: (iqx, w0, w1, w2)
@@ -707,6 +712,7 @@ __device__ __forceinline__ bool strip_line_extent(float ca, float cl, float T1, 
 }
 
 constexpr int kFpStage = 32;  // staged pixels per line: the union of the group's candidates
+constexpr int kFpBox = 8;     // rays per TMA box: a line stages ceil(n / 8) boxes
 
 // Candidate pixel range [clo, chi] on line li for one angle: pixels whose
 // centre bin may fall in [b0-1, b0+BT] (a margin of one pixel each side; the
@@ -937,23 +943,25 @@ __global__ void __launch_bounds__(kFpThreads, 3)
                     if (lane == 0) atomicOr(A.err, 16);
                 }
                 // the staged pixels of a line are consecutive rays in the
-                // line's order: one tile of US rays x SPAN slices from x (row
-                // sweeps) or its column-major copy (column sweeps), and one
-                // contiguous taps record
+                // line's order: ceil(n / 8) tiles of 8 rays x SPAN slices from
+                // x (row sweeps) or its column-major copy (column sweeps), and
+                // one contiguous taps record
                 const int n = ok ? lf.y : 0;  // a wait gave up: stage nothing more
+                const int nbox = (n + kFpBox - 1) / kFpBox;
                 if (lane == 0) {
                     uinfo[2 * buf + 1] = n;
                     __threadfence_block();  // counts before the arrival
                     umma::mbar_arrive_expect_tx(
-                        &full[buf], n ? (uint32_t)(US * SPAN * 4 + n * 16 * NA) : 0u);
-                    if (n) {
-                        umma::tma_load_2d(stg + (size_t)buf * US * SPAN, orient ? &tmxT : &tmx, yb,
-                                          lf.x, &full[buf]);
-                        umma::bulk_g2s(rayb + buf * US * NA,
-                                       A.taps + ((size_t)grp * A.nrays + lf.x) * NA,
-                                       (uint32_t)n * 16u * NA, &full[buf]);
-                    }
+                        &full[buf],
+                        n ? (uint32_t)(nbox * kFpBox * SPAN * 4 + n * 16 * NA) : 0u);
                 }
+                __syncwarp();
+                if (lane < nbox)
+                    umma::tma_load_2d(stg + ((size_t)buf * US + lane * kFpBox) * SPAN,
+                                      orient ? &tmxT : &tmx, yb, lf.x + lane * kFpBox, &full[buf]);
+                if (lane == 0 && n)
+                    umma::bulk_g2s(rayb + buf * US * NA, A.taps + ((size_t)grp * A.nrays + lf.x) * NA,
+                                   (uint32_t)n * 16u * NA, &full[buf]);
                 __syncwarp();
             }
             return;
@@ -1135,8 +1143,9 @@ __global__ void __launch_bounds__(kFpThreads, 3)
 // ---------------------------------------------------------------------------
 // Forward projection for the linear weighting.  Its ray coordinates are the
 // reference's shifted table entries (not a pixel grid), so the strip sweep does
-// not apply; this path scatters with atomics.  It exists for parity with
-// pmethod=1, not for speed; its float summation order is not fixed.
+// not apply.  With the plan's ray index (k_lin_index) each output bin gathers
+// its rays in a fixed order (fp_lin_gather, deterministic); without it this
+// kernel scatters with atomics, whose float summation order is not fixed.
 template <int VEC>
 __global__ void __launch_bounds__(256) fp_lin_kernel(OpArgs A, const float *__restrict__ x,
                                                      float *__restrict__ q) {
@@ -1163,6 +1172,75 @@ __global__ void __launch_bounds__(256) fp_lin_kernel(OpArgs A, const float *__re
 #pragma unroll
             for (int c = 0; c < VEC; c++) atomicAdd(qa + (size_t)(b + 1) * A.ys + c, tp.w1 * v[c]);
     }
+}
+
+// The linear weighting's ray index, one thread per angle: count the rays of
+// each first bin b0 = iqx - 1 in [-1, nx - 1] (the rays that reach the
+// detector), prefix sums, then place the rays in ascending order (a second
+// pass, the offsets advancing as cursors and shifted back afterwards).  The
+// first bins come from the projectors' own ray_taps, so the gather below and
+// the back projector use identical coefficients.
+static __global__ void __launch_bounds__(64) k_lin_index(OpArgs A, int *off, int *list) {
+    const int a = blockIdx.x * blockDim.x + threadIdx.x;
+    if (a >= A.na) return;
+    const int nb = A.nx + 1;  // buckets j = b0 + 1
+    int *o = off + (size_t)a * (nb + 1);
+    int *l = list + (size_t)a * A.nrays;
+    const AngleParams ap = A.ang[a];
+    for (int j = 0; j <= nb; j++) o[j] = 0;
+    for (int k = 0; k < A.nrays; k++) {
+        const int j = ray_taps<ARECGB_LIN>(A.ray[k], ap, A.r_hi, A.r_lo).iqx;  // b0 + 1
+        if (j >= 0 && j < nb) o[j + 1]++;
+    }
+    for (int j = 1; j <= nb; j++) o[j] += o[j - 1];
+    for (int k = 0; k < A.nrays; k++) {
+        const int j = ray_taps<ARECGB_LIN>(A.ray[k], ap, A.r_hi, A.r_lo).iqx;
+        if (j >= 0 && j < nb) l[o[j]++] = k;
+    }
+    for (int j = nb; j > 0; j--) o[j] = o[j - 1];  // o[j] was the end of bucket j
+    o[0] = 0;
+}
+
+// Linear weighting, gather: one warp per (angle, bin, slice chunk); bin b
+// takes w0 of the rays whose first bin is b, then w1 of those whose first bin
+// is b - 1, each in ascending ray order, as the reference's per-ray products
+// added in float (arecproject.cpp:75-95).
+template <int VEC>
+__global__ void __launch_bounds__(256) fp_lin_gather(OpArgs A, const float *__restrict__ x,
+                                                     float *__restrict__ q) {
+    if (A.skip && *A.skip) return;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const long long gw = (long long)blockIdx.x * 8 + warp;
+    const int nchunk = (A.ys + 32 * VEC - 1) / (32 * VEC);
+    if (gw >= (long long)A.na * A.nx * nchunk) return;
+    const int c = (int)(gw % nchunk);
+    const int b = (int)((gw / nchunk) % A.nx);
+    const int a = (int)(gw / ((long long)nchunk * A.nx));
+    const int y0 = c * 32 * VEC + lane * VEC;
+    const bool yok = y0 < A.ys;
+    const int *o = A.lin_off + (size_t)a * (A.nx + 2);
+    const int *l = A.lin_list + (size_t)a * A.nrays;
+    const AngleParams ap = A.ang[a];
+    float acc[VEC];
+#pragma unroll
+    for (int v = 0; v < VEC; v++) acc[v] = 0.f;
+#pragma unroll
+    for (int t = 0; t < 2; t++) {
+        const int j = b + 1 - t;  // t = 0: first bin b (w0); t = 1: first bin b - 1 (w1)
+        const int e = o[j + 1];
+        for (int i = o[j]; i < e; i++) {
+            const int k = l[i];
+            const Taps tp = ray_taps<ARECGB_LIN>(A.ray[k], ap, A.r_hi, A.r_lo);
+            const float w = t == 0 ? tp.w0 : tp.w1;
+            if (yok) {
+                float v[VEC];
+                ldv<VEC>(x + (size_t)k * A.ys + y0, v);
+#pragma unroll
+                for (int u = 0; u < VEC; u++) acc[u] = __fadd_rn(acc[u], __fmul_rn(w, v[u]));
+            }
+        }
+    }
+    if (yok) stv<VEC>(q + ((size_t)a * A.nx + b) * A.ys + y0, acc);
 }
 
 }  // namespace arecgb
@@ -1248,10 +1326,20 @@ int launch_fpb(const OpArgs &A, int vec, dim3 grid, const float *x, float *q, in
     return launch_fpb_one<W, 8, BT>(A, grid, x, q, g0, ngo, lo, hi, tmx, tmxT, st);
 }
 
-// Linear weighting (scatter).
+// Linear weighting: the gather when the plan has its ray index, else the
+// scatter (q zeroed by the caller either way).
 template <int W>
 int launch_fp(const OpArgs &A, int vec, const float *x, float *q, cudaStream_t st) {
     static_assert(W == ARECGB_LIN, "the other weightings use the banded kernel");
+    if (A.lin_off && A.lin_list) {
+        const long long nw = (long long)A.na * A.nx * ((A.ys + 32 * vec - 1) / (32 * vec));
+        const unsigned blocks = (unsigned)((nw + 7) / 8);
+        if (vec == 1) fp_lin_gather<1><<<blocks, 256, 0, st>>>(A, x, q);
+        else if (vec == 2) fp_lin_gather<2><<<blocks, 256, 0, st>>>(A, x, q);
+        else if (vec == 4) fp_lin_gather<4><<<blocks, 256, 0, st>>>(A, x, q);
+        else fp_lin_gather<8><<<blocks, 256, 0, st>>>(A, x, q);
+        return 0;
+    }
     const long long n = (long long)A.nrays * (A.ys / vec);
     const unsigned blocks = (unsigned)((n + 255) / 256);
     if (vec == 1) fp_lin_kernel<1><<<blocks, 256, 0, st>>>(A, x, q);

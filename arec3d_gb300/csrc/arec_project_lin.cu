@@ -12,4 +12,9 @@ int launch_fp_lin(const OpArgs &A, int vec, const float *x, float *q, cudaStream
     return launch_fp<ARECGB_LIN>(A, vec, x, q, st);
 }
 
+int launch_lin_index(const OpArgs &A, int *off, int *list, cudaStream_t st) {
+    k_lin_index<<<(A.na + 63) / 64, 64, 0, st>>>(A, off, list);
+    return 0;
+}
+
 }  // namespace arecgb

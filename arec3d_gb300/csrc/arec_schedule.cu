@@ -74,22 +74,30 @@ int arecgb_cylinder_info(double radius, int ny, int *nx, int *nrays, int *ys) {
 }
 
 int arecgb_solve_uneven(const arecgb_problem *probs, int n, size_t budget_bytes,
-                        arecgb_unet *net, int sirt_iters, float sirt_lam_scale, int maxit,
-                        float tol, arecgb_solve_info *info, int *wave_of, void *stream) {
-    if (!probs || n < 1 || maxit < 0 || (net && sirt_iters < 1)) {
+                        arecgb_unet *const *nets, int n_nets, int sirt_iters,
+                        double sirt_lam_scale, int maxit, float tol, arecgb_solve_info *info,
+                        int *wave_of, void *stream) {
+    if (!probs || n < 1 || maxit < 0 || n_nets < 0 || (n_nets > 0 && (!nets || sirt_iters < 1))) {
         set_error("arecgb_solve_uneven: bad arguments");
         return ARECGB_ERR_ARG;
     }
     cudaStream_t st = (cudaStream_t)stream;
-    int H = 0, W = 0, B = 0;
-    if (net) {
-        int rc = arecgb_unet_shape(net, &H, &W, &B);
+    // the networks (the same parameters at several image sizes): each problem
+    // takes the smallest whose images hold its width
+    std::vector<int> netH(n_nets), netB(n_nets);
+    size_t img_floats = 0;
+    for (int k = 0; k < n_nets; k++) {
+        int H = 0, W = 0, B = 0;
+        int rc = arecgb_unet_shape(nets[k], &H, &W, &B);
         if (rc) return rc;
+        netH[k] = std::min(H, W);
+        netB[k] = B;
+        img_floats = std::max(img_floats, (size_t)H * W * B);
     }
+    std::vector<int> net_of(n, -1);
     // workspace bytes per problem: CGLS's 3 volume + 2 sinogram vectors, the
     // ray table and a margin for the plan's other tables and partials
     std::vector<size_t> bytes(n);
-    std::vector<int> nxs(n);
     for (int i = 0; i < n; i++) {
         const arecgb_problem &q = probs[i];
         if (q.weighting < ARECGB_LIN || q.weighting > ARECGB_SQ || q.ny < 1 || q.nangles < 1 ||
@@ -99,14 +107,14 @@ int arecgb_solve_uneven(const arecgb_problem *probs, int n, size_t budget_bytes,
         }
         int nx = 0, nr = 0;
         cylinder_counts(q.radius, &nx, &nr);
-        if (net && (nx > H || nx > W)) {
+        for (int k = 0; k < n_nets; k++)
+            if (netH[k] >= nx && (net_of[i] < 0 || netH[k] < netH[net_of[i]])) net_of[i] = k;
+        if (n_nets > 0 && net_of[i] < 0) {
             set_error("arecgb_solve_uneven: problem " + std::to_string(i) + " is " +
-                      std::to_string(nx) + " bins wide, wider than the network's images (" +
-                      std::to_string(H) + ")");
+                      std::to_string(nx) + " bins wide, wider than every network's images");
             return ARECGB_ERR_ARG;
         }
         const size_t ys = (size_t)round8(q.ny);
-        nxs[i] = nx;
         bytes[i] = sizeof(float) * (3 * (size_t)nr * ys + 2 * (size_t)q.nangles * nx * ys) +
                    sizeof(float4) * (size_t)nr + (64u << 20);
     }
@@ -133,9 +141,9 @@ int arecgb_solve_uneven(const arecgb_problem *probs, int n, size_t budget_bytes,
         cudaFree(img[0]);
         cudaFree(img[1]);
     };
-    if (net) {
+    if (n_nets > 0) {
         for (auto &p : img) {
-            cudaError_t e = cudaMalloc(&p, sizeof(float) * (size_t)H * W * B);
+            cudaError_t e = cudaMalloc(&p, sizeof(float) * img_floats);
             if (e != cudaSuccess) {
                 free_img();
                 set_error(std::string("arecgb_solve_uneven: ") + cudaGetErrorString(e));
@@ -162,11 +170,12 @@ int arecgb_solve_uneven(const arecgb_problem *probs, int n, size_t budget_bytes,
         }
         // the learned warm start, problem by problem (SIRT at the step the
         // network was trained with, then x0 = net(SIRT) scaled back)
-        for (int j = 0; !rc && net && j < m; j++) {
+        for (int j = 0; !rc && n_nets > 0 && j < m; j++) {
             Plan *p = plans[j];
+            arecgb_unet *net = nets[net_of[wv[j]]];
             arecgb_solve_info si;
             memset(&si, 0, sizeof(si));
-            const float lam = sirt_lam_scale / ((float)p->na * (float)p->nx);
+            const float lam = (float)(sirt_lam_scale / ((double)p->na * (double)p->nx));
             rc = sirt(p, bs[j], xs[j], lam, sirt_iters, 0.0f, nullptr, &si, 0, st);
             if (!rc)
                 rc = arecgb_warm_start(reinterpret_cast<arecgb_plan *>(p), net, xs[j], xs[j],

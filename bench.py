@@ -351,9 +351,8 @@ def run_reference(args, rank, world):
 def extra_config(args):
     """Measurements of the other benchmark configurations (one JSON line each;
     not the headline): 1 = SIRT x50 at 256^2 x 64 slices / 180 angles;
-    3 = shift search over 720 pairs of 2048^2 images; 5 = a seeded subset of
-    the uneven batch (cylinders of radius 128-1024, uneven slices and angles)
-    solved by the batched CGLS."""
+    3 = shift search over 720 pairs of 2048^2 images; 5 = the uneven batch of
+    64 cylinders (uneven_batch)."""
     import math
 
     import torch
@@ -423,27 +422,86 @@ def extra_config(args):
                "hbm_gbs": n * 2 * 4 * size * size / (ms / 1e3) / 1e9,
                "max_abs_shift_error_px": float(err.max())}
     else:
-        rng = np.random.default_rng(5)
-        k = args.batch_problems
-        plans, bs, xs, sl = [], [], [], 0
-        for i in range(k):
-            r = float(rng.uniform(128, 1024 if i == 0 else 512))
-            nx = int(round(2 * r + 1))
-            ny = int(rng.integers(32, 513)) // 8 * 8 or 8
-            na = int(rng.integers(360, 1801))
-            plan, b = ws.make_problem(gb, nx, na, ny, 5e3, 500 + i, "sphere")
-            plans.append(plan)
-            bs.append(b)
-            xs.append(torch.zeros(plan.nrays, plan.ys, device="cuda"))
-            sl += ny
-        ms, infos = timed(lambda: gb.cgls_batch(plans, bs, xs, 200, 1e-3, stream=st), args.steps)
-        out = {"config": 5, "workload": "uneven batch subset: %d cylinders, radius 128-1024 "
-               "(first) / 128-512, 32-512 slices, 360-1800 angles, Poisson 5e3, batched CGLS "
-               "to 1e-3" % k,
-               "value": sl / (ms / 1e3), "unit": "slices/s", "ms_per_batch": ms,
-               "problems": [{"nx": p.nx, "slices": p.ny, "angles": p.nangles,
-                             "iterations": inf.iterations} for p, inf in zip(plans, infos)]}
+        out = uneven_batch(args, gb, syn, ws, timed)
     print(json.dumps(out))
+
+
+def uneven_batch(args, gb, syn, ws, timed):
+    """Config 5: 64 cylinders (radius U[128, 1024] px, detector 2 r + 16 bins,
+    32-512 slices, 360-1800 angles over [0, 180), random-sphere phantoms at
+    5e3 photons; problem 0 the largest instance the configuration names,
+    r = 1024 with 512 slices and 1800 angles), solved together by the
+    library's scheduler (arecgb_solve_uneven): waves of problems whose solver
+    workspace fits the budget, each wave's problems warm-started by the
+    network (one size per width class) and solved by one batched CGLS (one
+    CUDA graph launch per iteration for the whole wave) to 1e-3.  Inputs and
+    results stay resident in HBM."""
+    import torch
+
+    rng = np.random.default_rng(5)
+    k = args.batch_problems
+    specs = [(1024.0, 512, 1800)]
+    for _ in range(k - 1):
+        specs.append((float(rng.uniform(128, 1024)), int(rng.integers(32, 513)),
+                      int(rng.integers(360, 1801))))
+    scale = args.c5_scale
+    problems, slices = [], 0
+    t0 = time.perf_counter()
+    for i, (r, ny, na) in enumerate(specs):
+        r = max(16.0, r * scale)
+        ny = max(8, int(ny * scale)) if scale < 1 else ny
+        nx = int(2 * round(r) + 16)
+        radius = 0.5 * (nx - 1)
+        angles = syn.uniform_angles(na)
+        _, nr, ys = gb.cylinder_info(radius, ny)
+        nsph = max(8, int(round(200 * (r / 500.0) ** 2 * ny / 512)))
+        ph = syn.sphere_cylinder_phantom(500 + i, nx, ny, n_spheres=nsph, cyl_radius=r - 4,
+                                         r_max=min(80.0, 0.5 * (r - 4)))
+        b = syn.sphere_sinogram(ph, nx, ny, angles, ys=ys)
+        syn.poisson_log(b, 5e3, 700 + i, ny)
+        x = torch.zeros(nr, ys, device="cuda")
+        problems.append(dict(radius=radius, ny=ny, angles=angles, b=b, x=x, nx=nx, na=na))
+        slices += ny
+    torch.cuda.synchronize()
+    gen_s = time.perf_counter() - t0
+    nets = []
+    if not args.plain and os.path.exists(args.weights):
+        widths = sorted({p["nx"] for p in problems})
+        lo = 0
+        for size, batch in ((512, 16), (1024, 8), (2072, 4)):
+            if any(lo < w <= size for w in widths):
+                net, _ = ws.load(gb, args.weights, size, batch)
+                nets.append(net)
+            lo = size
+    free, total = torch.cuda.mem_get_info()
+    budget = int(args.c5_budget_gb * 1e9) if args.c5_budget_gb else int(0.8 * free) - (2 << 30)
+    st = torch.cuda.current_stream()
+
+    def run():
+        return gb.solve_uneven(problems, budget, maxit=MAXIT, tol=TOL, nets=nets, stream=st)
+
+    # one timed pass (a pass is minutes long at full size; no separate warm-up)
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(st)
+    infos, waves = run()
+    e1.record(st)
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1)
+    out = {"config": 5,
+           "workload": "uneven batch: %d cylinders, radius 128-1024 px (problem 0: 1024, 512 "
+                       "slices, 1800 angles), detector 2r+16 bins, 32-512 slices, 360-1800 "
+                       "angles, random spheres, Poisson 5e3; %s CGLS to 1e-3 (max %d it), "
+                       "waves under a %.0f GB workspace budget"
+                       % (k, "learned warm start +" if nets else "plain", MAXIT, budget / 1e9),
+           "value": slices / (ms / 1e3), "unit": "slices/s", "ms_per_batch": ms,
+           "slices": slices, "waves": max(waves) + 1, "setup_s": gen_s,
+           "resident_gb": sum(p["b"].numel() + p["x"].numel() for p in problems) * 4 / 1e9,
+           "scale": scale,
+           "problems": [{"nx": p["nx"], "slices": p["ny"], "angles": p["na"],
+                         "iterations": inf.iterations, "rel_final": inf.rel_final, "wave": w}
+                        for p, inf, w in zip(problems, infos, waves)]}
+    return out
 
 
 def unet_only(args):
@@ -540,7 +598,11 @@ def main():
     ap.add_argument("--plain", action="store_true", help="plain CGLS only (no warm start)")
     ap.add_argument("--config", type=int, default=0, choices=[0, 1, 3, 5],
                     help="measure another benchmark configuration instead of the headline")
-    ap.add_argument("--batch-problems", type=int, default=8, help="problems for --config 5")
+    ap.add_argument("--batch-problems", type=int, default=64, help="problems for --config 5")
+    ap.add_argument("--c5-scale", type=float, default=1.0,
+                    help="--config 5: scale radii (and slices below 1) for a smaller test run")
+    ap.add_argument("--c5-budget-gb", type=float, default=0.0,
+                    help="--config 5: solver workspace budget (default: most of the free HBM)")
     ap.add_argument("--pairs", type=int, default=720, help="image pairs for --config 3")
     ap.add_argument("--unet-only", action="store_true",
                     help="run only the warm-start network's inference (for profiling)")

@@ -386,16 +386,18 @@ typedef struct arecgb_problem {
  * memory, so the problems are packed into waves whose workspace fits
  * budget_bytes (first fit, largest first; a problem above the budget runs
  * alone).  Per wave: a plan per problem (without the optional projector
- * tables), with `net` the learned warm start per problem (SIRT of sirt_iters
- * iterations at step sirt_lam_scale / (nangles nx), then the network; every
- * nx must fit the network's images), then one batched CGLS of all the wave's
- * problems, one CUDA graph launch per iteration, each to
+ * tables), with n_nets > 0 the learned warm start per problem (SIRT of
+ * sirt_iters iterations at step sirt_lam_scale / (nangles nx), then the
+ * smallest of the networks `nets` whose images hold the problem's width: the
+ * same parameters at several image sizes), then one batched CGLS of all the
+ * wave's problems, one CUDA graph launch per iteration, each to
  * ||A^T r|| / ||A^T b|| <= tol (max maxit iterations).  info[i] (may be NULL)
  * receives problem i's CGLS summary and wave_of[i] (may be NULL) its wave.
  * Synchronises. */
 int arecgb_solve_uneven(const arecgb_problem *probs, int n, size_t budget_bytes,
-                        arecgb_unet *net, int sirt_iters, float sirt_lam_scale, int maxit,
-                        float tol, arecgb_solve_info *info, int *wave_of, void *stream);
+                        arecgb_unet *const *nets, int n_nets, int sirt_iters,
+                        double sirt_lam_scale, int maxit, float tol, arecgb_solve_info *info,
+                        int *wave_of, void *stream);
 
 /* One reconstruction end to end over HOST buffers in the reference's layouts
  * (the path a caller without device memory of its own takes; no counterpart

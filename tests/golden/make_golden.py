@@ -269,10 +269,10 @@ def compat():
             b = O.project(O.KB, 32.0, xt, ang)
             b = (b + 0.01 * rng.standard_normal(b.shape)).astype(np.float32)
             out["kb65_b"] = b
-            x, st = R.solve("cyl_cgls_KB", b, ang, 0.0, 6, 1e-7)
+            x, st = R.solve("cyl_cgls_KB", b, ang, 0.0, 5, 1e-7)
             assert st == 0
             out["kb65_cgls"] = x
-            out["kb65_maxit"] = np.array(6)
+            out["kb65_maxit"] = np.array(5)
             x0 = (x * 0.5).astype(np.float32)
             maxit = 5
         else:

@@ -85,6 +85,15 @@ def test_cylinder_allocation_matches_oracle(lib, oc, r):
     lib.arecImageFree(im)
 
 
+@pytest.mark.parametrize("r,ny", [(0.5, 1), (12.0, 5), (63.5, 300), (1031.5, 512)])
+def test_cylinder_info_matches_oracle(lib, oc, r, ny):
+    """arecgb_cylinder_info: the device layout sizes of a cylinder without a plan."""
+    import arec3d_gb300 as gb
+
+    nx, nr, _ = oc.cyl(r)
+    assert gb.cylinder_info(r, ny) == (nx, nr, (ny + 7) // 8 * 8)
+
+
 def test_image_cyl2cb_roundtrip(lib):
     """"ImageCyl2CB" (AREC3D_test.cpp:326-363)."""
     L = lib.lib()

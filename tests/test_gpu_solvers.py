@@ -4,7 +4,7 @@ import numpy as np
 import pytest
 
 from conftest import rel_l2, uniform_angles
-from devutil import empty_vol, sino_to_dev, vol_from_dev, vol_to_dev
+from devutil import empty_sino, empty_vol, sino_to_dev, vol_from_dev, vol_to_dev
 
 pytestmark = pytest.mark.gpu
 
@@ -207,3 +207,51 @@ def test_cgls_stat_parity(gb, oc, w):
     xc, st = getattr(gb, name)(b, ang, maxit=10, tol=1e-7)
     assert st == 0
     assert rel_l2(xc, x_ref) < max(TOL, FRAC * e_ref)
+
+
+def test_solve_uneven_waves_match_single_solves(gb):
+    """arecgb_solve_uneven: five cylinders of uneven radius, slices and angles
+    under a budget that forces several waves give exactly the results of
+    solving each alone (plans without tables compute the same values), with
+    and without the learned warm start (SIRT -> U-Net -> CGLS with the cold
+    start's denominator, as the single-problem pipeline does)."""
+    import torch
+
+    from arec3d_gb300 import synthetic as syn
+    from arec3d_gb300 import warmstart as ws
+
+    rng = np.random.default_rng(55)
+    specs = [(60.5, 24, 90), (31.5, 8, 40), (90.0, 40, 120), (47.5, 16, 64), (20.0, 8, 30)]
+    probs, singles = [], []
+    net, _ = ws.load(gb, ws.DEFAULT_WEIGHTS, 184, 4)
+    for radius, ny, na in specs:
+        ang = syn.uniform_angles(na)
+        plan = gb.Plan(gb.SQ, radius, ny, ang)
+        xt = rng.random((plan.nrays, ny), dtype=np.float32)
+        qd = empty_sino(plan)
+        plan.project(vol_to_dev(plan, xt), qd)
+        qd[:, :, :ny] += 0.02 * torch.randn(plan.nangles, plan.nx, ny, device="cuda")
+        singles.append((plan, qd))
+        probs.append(dict(radius=radius, ny=ny, angles=ang, b=qd, x=empty_vol(plan)))
+    nxv = [gb.cylinder_info(r, ny)[:2] for r, ny, _ in specs]
+    assert [(p.nx, p.nrays) for p, _ in singles] == nxv
+    for use_net in (False, True):
+        budget = 1 << 20  # 1 MiB of workspace: every problem its own wave
+        infos, waves = gb.solve_uneven(probs, budget, maxit=30, tol=1e-3,
+                                       nets=[net] if use_net else None)
+        assert sorted(waves) == list(range(len(specs)))
+        for i, (plan, qd) in enumerate(singles):
+            x = empty_vol(plan)
+            if use_net:
+                info, _ = ws.solve(gb, plan, qd, x, net=net, tol=1e-3, maxit=30)
+            else:
+                _, info = plan.cgls(qd, x, 30, 1e-3)
+            assert infos[i].iterations == info.iterations
+            np.testing.assert_array_equal(vol_from_dev(plan, probs[i]["x"]), vol_from_dev(plan, x))
+        # one wave for all of them gives the same answers too
+        infos2, waves2 = gb.solve_uneven(probs, 1 << 40, maxit=30, tol=1e-3,
+                                         nets=[net] if use_net else None)
+        assert set(waves2) == {0}
+        assert [i.iterations for i in infos2] == [i.iterations for i in infos]
+        print("uneven batch (%s): iterations %s" % ("warm" if use_net else "plain",
+                                                    [i.iterations for i in infos]))
