@@ -278,9 +278,10 @@ constexpr int kBpBuf = 3;  // footprint buffers in flight
 // bins b .. b+2 of its current ray in a register ring; the plan says, per
 // ray, which ring slot takes which footprint row (the centre bin moves by at
 // most one bin between neighbouring pixels) and rotates the weights to the
-// slots.  Entry (code, wa, wb, wc): code bits 0-1 action (0 skip, 1 same
-// bins, 2 one row enters slot bits 2-3, 3 three rows), bits 8+ footprint row
-// of the (first) row entering; wa, wb, wc the weights of slots 0, 1, 2.
+// slots.  Entry (code, wa, wb, wc): code bits 0-2 the slots that load (0: the
+// ray keeps the ring, or is skipped with zero weights; one bit: one row enters
+// that slot; 7: three rows enter slots 0, 1, 2), bits 8+ footprint row of the
+// (first) row entering; wa, wb, wc the weights of slots 0, 1, 2.
 // Also the tile's footprint: first bin fb and bins spanned fn (<= FW; wide:
 // the taps reach further, an impossible case reported by the caller).
 template <int W, int FW>
@@ -309,15 +310,15 @@ __device__ __forceinline__ float4 bp_plan(const OpArgs &A, const float4 &myray, 
         if (ur) {
             const int d = br - cb, rr = br - lo;
             if (d == 0) {
-                code = 1;
+                code = 0;
             } else if (d == 1) {  // bin cb (slot m) leaves, bin br + 2 enters
-                code = 2 | (m << 2) | ((rr + 2) << 8);
+                code = (1 << m) | ((rr + 2) << 8);
                 m = m == 2 ? 0 : m + 1;
             } else if (d == -1) {  // bin cb + 2 leaves, bin br enters
                 m = m == 0 ? 2 : m - 1;
-                code = 2 | (m << 2) | (rr << 8);
+                code = (1 << m) | (rr << 8);
             } else {
-                code = 3 | (rr << 8);
+                code = 7 | (rr << 8);
                 m = 0;
             }
             cb = br;
@@ -539,21 +540,19 @@ __global__ void __launch_bounds__(128 * NSC, NSC == 1 ? 4 : 1)
                 const float *F = foot + (size_t)buf * FW * SPAN + yw;
                 // the ring (slots 0, 1, 2); a warp's first used ray loads all three
                 if constexpr (VEC >= 4) {
-                    // branch-free: each slot's load is predicated on the plan's
-                    // code; rays with code 0 have zero weights (and the ring
-                    // holds finite staged values), so their FMAs add nothing
+                    // branch-free: each slot's load is predicated on its bit of
+                    // the plan's code; skipped rays have zero weights (and the
+                    // ring holds finite staged values), so their FMAs add nothing
                     const unsigned Fa = smem_u32(F + lane_piece<VEC>(lane, 0));
 #pragma unroll
                     for (int r = 0; r < 8; r++) {
                         const float4 e = sw[ai * 32 + rg * 8 + r];
-                        const int code = __float_as_int(e.x), act = code & 3;
-                        const int slot = (code >> 2) & 3;
-                        const bool all3 = act == 3, one = act == 2;
-                        const unsigned a = Fa + (unsigned)(code >> 8) * (SPAN * 4u);
-                        const unsigned step = all3 ? SPAN * 4u : 0u;
-                        lds_lane_if<VEC>(all3 || (one && slot == 0), a, R0);
-                        lds_lane_if<VEC>(all3 || (one && slot == 1), a + step, R1);
-                        lds_lane_if<VEC>(all3 || (one && slot == 2), a + 2 * step, R2);
+                        const unsigned code = (unsigned)__float_as_int(e.x), mask = code & 7u;
+                        const unsigned a = Fa + (code >> 8) * (SPAN * 4u);
+                        const unsigned step = mask == 7u ? SPAN * 4u : 0u;
+                        lds_lane_if<VEC>(mask & 1u, a, R0);
+                        lds_lane_if<VEC>(mask & 2u, a + step, R1);
+                        lds_lane_if<VEC>(mask & 4u, a + 2 * step, R2);
                         fma_row<VEC>(acc[r], e.y, R0);
                         fma_row<VEC>(acc[r], e.z, R1);
                         fma_row<VEC>(acc[r], e.w, R2);
@@ -562,21 +561,18 @@ __global__ void __launch_bounds__(128 * NSC, NSC == 1 ? 4 : 1)
 #pragma unroll
                     for (int r = 0; r < 8; r++) {
                         const float4 e = sw[ai * 32 + rg * 8 + r];
-                        const int code = __float_as_int(e.x), act = code & 3;
-                        if (act == 0) continue;
+                        const int code = __float_as_int(e.x), mask = code & 7;
                         const float *row = F + (code >> 8) * SPAN;
-                        if (act == 2) {
-                            const int slot = (code >> 2) & 3;
-                            if (slot == 0)
-                                lds_lane<VEC>(row, lane, R0);
-                            else if (slot == 1)
-                                lds_lane<VEC>(row, lane, R1);
-                            else
-                                lds_lane<VEC>(row, lane, R2);
-                        } else if (act == 3) {
+                        if (mask == 7) {
                             lds_lane<VEC>(row, lane, R0);
                             lds_lane<VEC>(row + SPAN, lane, R1);
                             lds_lane<VEC>(row + 2 * SPAN, lane, R2);
+                        } else if (mask == 1) {
+                            lds_lane<VEC>(row, lane, R0);
+                        } else if (mask == 2) {
+                            lds_lane<VEC>(row, lane, R1);
+                        } else if (mask == 4) {
+                            lds_lane<VEC>(row, lane, R2);
                         }
                         fma_row<VEC>(acc[r], e.y, R0);
                         fma_row<VEC>(acc[r], e.z, R1);
