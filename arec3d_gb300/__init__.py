@@ -73,6 +73,8 @@ def lib():
         L.arecgb_plan_check.argtypes = [vp]
         L.arecgb_project.argtypes = [vp, vp, vp, vp, vp]
         L.arecgb_backproject.argtypes = [vp, vp, vp, vp, vp]
+        L.arecgb_fbp.argtypes = [vp, vp, vp, vp, vp, vp]
+        L.arecgb_ramp_filter.argtypes = [vp, vp, vp, vp]
         L.arecgb_cgls.argtypes = [vp, vp, vp, C.c_int, C.c_int, C.c_float, C.c_double, dp,
                                   C.POINTER(SolveInfo), vp]
         L.arecgb_sirt.argtypes = [vp, vp, vp, C.c_float, C.c_int, C.c_float, dp,
@@ -265,6 +267,16 @@ class Plan:
         _check(lib().arecgb_backproject(self._h, _ptr(s), _ptr(g), _ptr(norm2), _stream(stream)),
                "arecgb_backproject")
 
+    def fbp(self, b, x, work, atb_norm2=None, stream=None):
+        """x = (pi / nangles) A^T (ramp * b); work receives the filtered
+        sinogram; atb_norm2 (device double), if given, ||A^T b||^2."""
+        _check(lib().arecgb_fbp(self._h, _ptr(b), _ptr(x), _ptr(work), _ptr(atb_norm2),
+                                _stream(stream)), "arecgb_fbp")
+
+    def ramp_filter(self, s, f, stream=None):
+        _check(lib().arecgb_ramp_filter(self._h, _ptr(s), _ptr(f), _stream(stream)),
+               "arecgb_ramp_filter")
+
     def cgls(self, b, x, maxit, tol, warm=False, rnorm_ref=0.0, stream=None):
         hist = np.zeros(max(maxit, 1), np.float64)
         info = SolveInfo()
@@ -342,8 +354,10 @@ class Plan:
         """One reconstruction over host buffers in the reference's layouts
         (arecgb_reconstruct_host): b_host [nangles][ny][nx] and x_host
         [nrays][ny] float32, as pointers or CPU tensors / arrays (page-locked
-        memory copies at full speed).  With `net`: SIRT -> warm start -> CGLS;
-        without: CGLS from zero.  Returns the CGLS SolveInfo."""
+        memory copies at full speed).  With `net`: the network's input (SIRT
+        of sirt_iters iterations, or the filtered back projection when
+        sirt_iters is 0) -> warm start -> CGLS; without: CGLS from zero.
+        Returns the CGLS SolveInfo."""
         def hp(a):
             if isinstance(a, int):
                 return a

@@ -127,6 +127,27 @@ int arecgb_backproject(arecgb_plan *plan, const float *d_s, float *d_g, double *
     return back_project(P(plan), d_s, d_g, d_norm2, nullptr, (cudaStream_t)stream);
 }
 
+int arecgb_fbp(arecgb_plan *plan, const float *d_b, float *d_x, float *d_work,
+               double *d_atb_norm2, void *stream) {
+    if (!plan || !d_b || !d_x || !d_work) {
+        set_error("arecgb_fbp: null argument");
+        return ARECGB_ERR_ARG;
+    }
+    int rc = bind_device(P(plan));
+    if (rc) return rc;
+    return fbp(P(plan), d_b, d_x, d_work, d_atb_norm2, (cudaStream_t)stream);
+}
+
+int arecgb_ramp_filter(arecgb_plan *plan, const float *d_s, float *d_f, void *stream) {
+    if (!plan || !d_s || !d_f) {
+        set_error("arecgb_ramp_filter: null argument");
+        return ARECGB_ERR_ARG;
+    }
+    int rc = bind_device(P(plan));
+    if (rc) return rc;
+    return ramp_filter(P(plan), d_s, d_f, (cudaStream_t)stream);
+}
+
 int arecgb_cgls(arecgb_plan *plan, const float *d_b, float *d_x, int warm, int maxit, float tol,
                 double rnorm_ref, double *rel_history, arecgb_solve_info *info, void *stream) {
     if (!plan || !d_b || !d_x || maxit < 0) {
@@ -654,7 +675,7 @@ int arecgb_reconstruct_host(arecgb_plan *plan, const float *b_host, float *x_hos
                             arecgb_unet *net, int sirt_iters, float sirt_lam, int maxit,
                             float tol, arecgb_solve_info *info, void *stream) {
     Plan *p = reinterpret_cast<Plan *>(plan);
-    if (!p || !b_host || !x_host || maxit < 0 || (net && sirt_iters < 1)) {
+    if (!p || !b_host || !x_host || maxit < 0 || sirt_iters < 0) {
         set_error("arecgb_reconstruct_host: bad argument");
         return ARECGB_ERR_ARG;
     }
@@ -686,7 +707,18 @@ int arecgb_reconstruct_host(arecgb_plan *plan, const float *b_host, float *x_hos
     arecgb_solve_info si, ci;
     memset(&si, 0, sizeof(si));
     memset(&ci, 0, sizeof(ci));
-    if (net) {
+    if (net && sirt_iters == 0) {
+        // the filtered back projection as the network's input; ||A^T b||, the
+        // cold start's denominator, from one more back projection
+        if ((rc = ensure(&p->d_sin[0], sin_floats(p))) || (rc = ensure_red(p))) return rc;
+        double *d_n2 = p->d_sred + 2 * kSredBlocks;
+        if ((rc = fbp(p, d_b, d_x, p->d_sin[0], d_n2, st))) return rc;
+        ARECGB_CUDA(cudaMemcpyAsync(p->h_sred, d_n2, sizeof(double), cudaMemcpyDeviceToHost, st));
+        if ((rc = arecgb_warm_start(plan, net, d_x, d_x, p->d_img[0], p->d_img[1], st)))
+            return rc;
+        ARECGB_CUDA(cudaStreamSynchronize(st));
+        rc = cgls(p, d_b, d_x, 1, maxit, tol, sqrt(p->h_sred[0]), nullptr, &ci, st);
+    } else if (net) {
         if ((rc = sirt(p, d_b, d_x, sirt_lam, sirt_iters, 0.0f, nullptr, &si, 0, st))) return rc;
         if ((rc = arecgb_warm_start(plan, net, d_x, d_x, p->d_img[0], p->d_img[1], st)))
             return rc;

@@ -282,6 +282,7 @@ void plan_destroy(Plan *p) {
     cudaFree(p->d_w);
     cudaFree(p->d_groups);
     cudaFree(p->d_tiles);
+    cudaFree(p->d_ramp);
     cudaFree(p->d_taps);
     cudaFree(p->d_kinv);
     cudaFree(p->d_lin_off);

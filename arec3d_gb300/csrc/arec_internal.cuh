@@ -103,6 +103,8 @@ struct Plan {
     float *h_pinned = nullptr;     // pinned host staging
     size_t pinned_floats = 0;
     float *d_img[2] = {nullptr, nullptr};  // warm-start network images (arecgb_reconstruct_host)
+    float *d_ramp = nullptr;      // ramp filter taps (odd distances), built on first use
+    int ramp_n = 0;
     size_t img_floats = 0;
 
     cudaStream_t stream = nullptr; // plan-owned stream for the compatible entry points
@@ -156,6 +158,16 @@ int plan_timing(const Plan *p, int mode, double *fp_ms, long long *fp_calls, dou
 int plan_autotune(Plan *p, float *d_x, float *d_q, cudaStream_t st);
 int plan_build_tables(Plan *p);
 int bp_grid_blocks(const Plan *p);
+
+// Filtered back projection (arec_fbp.cu): the Ram-Lak ramp filter along bins
+// (weight pi / nangles folded in), and x = A^T (ramp * b) [with ||A^T b||^2].
+int ramp_filter(Plan *p, const float *d_s, float *d_f, cudaStream_t st);
+int fbp(Plan *p, const float *d_b, float *d_x, float *d_work, double *d_norm2, cudaStream_t st);
+
+// The solvers' reduction scratch (arec_solver.cu): d_sred holds 2 kSredBlocks
+// partials and two results, h_sred two pinned doubles.
+constexpr int kSredBlocks = 1024;
+int ensure_red(Plan *p);
 
 // Layout kernels and vector ops (arec_vector.cu)
 int sino_to_device_layout(const float *d_ref, float *d_dev, int na, int ny, int nx, int ys,

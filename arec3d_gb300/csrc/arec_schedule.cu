@@ -77,7 +77,7 @@ int arecgb_solve_uneven(const arecgb_problem *probs, int n, size_t budget_bytes,
                         arecgb_unet *const *nets, int n_nets, int sirt_iters,
                         double sirt_lam_scale, int maxit, float tol, arecgb_solve_info *info,
                         int *wave_of, void *stream) {
-    if (!probs || n < 1 || maxit < 0 || n_nets < 0 || (n_nets > 0 && (!nets || sirt_iters < 1))) {
+    if (!probs || n < 1 || maxit < 0 || n_nets < 0 || sirt_iters < 0 || (n_nets > 0 && !nets)) {
         set_error("arecgb_solve_uneven: bad arguments");
         return ARECGB_ERR_ARG;
     }
@@ -168,20 +168,48 @@ int arecgb_solve_uneven(const arecgb_problem *probs, int n, size_t budget_bytes,
             xs[j] = q.d_x;
             if (wave_of) wave_of[wv[j]] = (int)w;
         }
-        // the learned warm start, problem by problem (SIRT at the step the
-        // network was trained with, then x0 = net(SIRT) scaled back)
+        // the learned warm start, problem by problem: the network's input (SIRT
+        // at the step the network was trained with, or with sirt_iters = 0 the
+        // filtered back projection), then x0 = net(input) scaled back
         for (int j = 0; !rc && n_nets > 0 && j < m; j++) {
             Plan *p = plans[j];
             arecgb_unet *net = nets[net_of[wv[j]]];
-            arecgb_solve_info si;
-            memset(&si, 0, sizeof(si));
-            const float lam = (float)(sirt_lam_scale / ((double)p->na * (double)p->nx));
-            rc = sirt(p, bs[j], xs[j], lam, sirt_iters, 0.0f, nullptr, &si, 0, st);
+            if (sirt_iters == 0) {
+                // the filtered sinogram goes to the sinogram scratch CGLS uses next
+                if (!p->d_sin[0]) {
+                    const size_t ns = sin_floats(p);
+                    cudaError_t e = cudaMalloc(&p->d_sin[0], sizeof(float) * ns);
+                    if (e == cudaSuccess) e = cudaMemsetAsync(p->d_sin[0], 0, sizeof(float) * ns, st);
+                    if (e != cudaSuccess) {
+                        set_error(std::string("arecgb_solve_uneven: ") + cudaGetErrorString(e));
+                        rc = cuda_status(e);
+                        break;
+                    }
+                }
+                if ((rc = ensure_red(p))) break;
+                double *d_n2 = p->d_sred + 2 * kSredBlocks;
+                rc = fbp(p, bs[j], xs[j], p->d_sin[0], d_n2, st);
+                if (!rc) {
+                    cudaError_t e = cudaMemcpyAsync(p->h_sred, d_n2, sizeof(double),
+                                                    cudaMemcpyDeviceToHost, st);
+                    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+                    if (e != cudaSuccess) {
+                        set_error(std::string("arecgb_solve_uneven: ") + cudaGetErrorString(e));
+                        rc = cuda_status(e);
+                    }
+                }
+                rref[j] = rc ? 0.0 : sqrt(p->h_sred[0]);  // ||A^T b||: the cold start's
+            } else {
+                arecgb_solve_info si;
+                memset(&si, 0, sizeof(si));
+                const float lam = (float)(sirt_lam_scale / ((double)p->na * (double)p->nx));
+                rc = sirt(p, bs[j], xs[j], lam, sirt_iters, 0.0f, nullptr, &si, 0, st);
+                rref[j] = si.rnorm0;  // ||A^T b||: the cold start's denominator
+            }
             if (!rc)
                 rc = arecgb_warm_start(reinterpret_cast<arecgb_plan *>(p), net, xs[j], xs[j],
                                        img[0], img[1], st);
             warm[j] = 1;
-            rref[j] = si.rnorm0;  // ||A^T b||: the cold start's denominator
         }
         if (!rc)
             rc = cgls_batch(plans.data(), bs.data(), xs.data(), warm.data(), m, maxit, tol,

@@ -401,7 +401,17 @@ static int ensure_workspace(Plan *p, int nvol, int nsin) {
     return ARECGB_OK;
 }
 
-constexpr int kRedBlocks = 1024;
+constexpr int kRedBlocks = kSredBlocks;
+
+int ensure_red(Plan *p) {
+    if (!p->d_sred) ARECGB_CUDA(cudaMalloc(&p->d_sred, sizeof(double) * (2 * kSredBlocks + 2)));
+    if (!p->h_sred && cudaMallocHost(&p->h_sred, sizeof(double) * 2) != cudaSuccess) {
+        p->h_sred = nullptr;
+        set_error("pinned allocation failed");
+        return ARECGB_ERR_NOMEM;
+    }
+    return 0;
+}
 
 // One CGLS iteration (reference areccgls.cpp:375-456) as a fixed launch sequence.
 static int cgls_iteration(Plan *p, SolveState *S, double *hist, float *x, float *s, float *q,
@@ -696,12 +706,7 @@ int sirt(Plan *p, const float *d_b, float *d_x, float lam, int maxit, float tol,
     if (rc) return rc;
     const size_t nv = vol_floats(p);
     float *bvol = p->d_vol[0], *pvol = p->d_vol[1], *grad = p->d_vol[2], *proj = p->d_sin[0];
-    if (!p->d_sred) ARECGB_CUDA(cudaMalloc(&p->d_sred, sizeof(double) * (2 * kRedBlocks + 2)));
-    if (!p->h_sred && cudaMallocHost(&p->h_sred, sizeof(double) * 2) != cudaSuccess) {
-        p->h_sred = nullptr;
-        set_error("sirt: pinned allocation failed");
-        return ARECGB_ERR_NOMEM;
-    }
+    if ((rc = ensure_red(p))) return rc;
     double *red = p->d_sred, *h_red = p->h_sred;
     double relnrm0 = 1.00001, bnorm2 = 0.0, bnorm = 0.0, atb_norm = 0.0, rel_last = 0.0;
     int restarts = 0, iter = 1, count = 0;

@@ -131,3 +131,42 @@ def poisson_log(p, photons, seed, ny, device="cuda", chunk=64):
         counts = torch.poisson(photons * torch.exp(-blk), generator=g)
         blk.copy_(-torch.log(torch.clamp(counts, min=1.0) / photons))
     return p
+
+
+def cylinder_coords(radius):
+    """Pixel-centre coordinates (x, z) relative to the axis of the rays of the
+    reference's cylinder of this radius, in its ray order (iz-major; a pixel is
+    a ray when (int)(ix - r)^2 + (int)(iz - r)^2 <= (int)(r r), truncation
+    toward zero: arecAllocateCylImage, AREC3D/AREC3D/arecImage.cpp:29-86)."""
+    n = int(round(2 * radius + 1))
+    ix, iz = np.meshgrid(np.arange(n), np.arange(n))
+    xs = np.trunc(ix - radius).astype(np.int64)
+    zs = np.trunc(iz - radius).astype(np.int64)
+    m = xs * xs + zs * zs <= int(radius * radius)
+    return (ix[m] - radius).astype(np.float64), (iz[m] - radius).astype(np.float64)
+
+
+def sphere_volume(ph, radius, ny, ys=None, device="cuda"):
+    """The sphere phantom's attenuation at the pixel centres of the cylinder,
+    [nrays][ys] float32 (torch; padding slices zero): the ground truth a
+    reconstruction is compared with."""
+    torch = _torch()
+    ys = ys or ((ny + 7) // 8) * 8
+    cx, cz = cylinder_coords(radius)
+    px = torch.tensor(cx, device=device)
+    pz = torch.tensor(cz, device=device)
+    out = torch.zeros(px.numel(), ys, dtype=torch.float64, device=device)
+    out[:, :ny] += ph["mu_cyl"] * ((px * px + pz * pz) <= ph["R"] ** 2).double()[:, None]
+    for i in range(len(ph["r"])):
+        rad, mu, cy = float(ph["r"][i]), float(ph["mu"][i]), float(ph["cy"][i])
+        y0, y1 = max(0, int(math.floor(cy - rad))), min(ny, int(math.ceil(cy + rad)) + 1)
+        if y1 <= y0:
+            continue
+        d2 = (px - float(ph["cx"][i])) ** 2 + (pz - float(ph["cz"][i])) ** 2
+        idx = torch.nonzero(d2 <= rad * rad).squeeze(1)
+        if idx.numel() == 0:
+            continue
+        yy = torch.arange(y0, y1, device=device, dtype=torch.float64)
+        inside = (d2[idx][:, None] + (yy[None, :] - cy) ** 2) <= rad * rad
+        out[idx, y0:y1] += mu * inside.double()
+    return out.float()

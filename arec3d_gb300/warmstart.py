@@ -3,8 +3,8 @@ the U-Net on the GPU, and the warm-started solve, all through the library's C
 ABI (arecgb_sirt, arecgb_cgls, arecgb_unet_*, arecgb_warm_start).
 
 A pair is one synthetic volume reconstructed twice from the same noisy data:
-a few SIRT iterations (the network input, cheap) and many CGLS iterations (the
-target).  Images are the cylinder's slices on a zero-padded square grid,
+a cheap first reconstruction (the network input: a few SIRT iterations, or
+the filtered back projection) and many CGLS iterations (the target).  Images are the cylinder's slices on a zero-padded square grid,
 normalised by the RMS of the SIRT volume over the cylinder, the normalisation
 arecgb_warm_start applies at inference.  Plain CGLS then continues from the
 network's output to the same residual tolerance, so the solver still decides
@@ -12,7 +12,7 @@ the result (and is the fallback: a bad guess costs iterations, not accuracy).
 
 torch is used only to hold device memory and pick training crops.
 
-    python -m arec3d_gb300.warmstart --out arec3d_gb300/weights/unet_warm_start.npz
+    python -m arec3d_gb300.warmstart --input fbp --out arec3d_gb300/weights/unet_warm_start.npz
 """
 import argparse
 import json
@@ -59,10 +59,25 @@ def make_problem(gb, nx, na, slices, photons, seed, kind="sphere", device="cuda"
     return plan, b
 
 
+def first_reconstruction(plan, b, x, inp, lam_scale=1.0, work=None):
+    """The network input: inp "fbp" (filtered back projection) or an int k
+    (k SIRT iterations from zero at step lam_scale / (nangles nx)).  Returns
+    ||A^T b||, the cold start's CGLS denominator, which both compute."""
+    import torch
+
+    if inp == "fbp":
+        n2 = torch.zeros(1, dtype=torch.float64, device="cuda")
+        plan.fbp(b, x, torch.empty_like(b) if work is None else work, atb_norm2=n2)
+        return math.sqrt(float(n2.item()))
+    _, sinfo = plan.sirt(b, x, sirt_lambda(plan, lam_scale), int(inp), 0.0)
+    return sinfo.rnorm0
+
+
 def make_pairs(gb, nx, na, slices, photons, seed, kind="sphere", sirt_iters=(SIRT_ITERS,),
                cgls_iters=CGLS_ITERS, lam_scale=1.0):
     """{k: (input, target)} image stacks [slices][npad][npad] on the device, one
-    pair per SIRT depth k in `sirt_iters` (the CGLS target is shared)."""
+    pair per input k in `sirt_iters` (a SIRT depth, or "fbp"; the CGLS target
+    is shared)."""
     import torch
 
     plan, b = make_problem(gb, nx, na, slices, photons, seed, kind)
@@ -72,7 +87,8 @@ def make_pairs(gb, nx, na, slices, photons, seed, kind="sphere", sirt_iters=(SIR
     npad = pad8(plan.nx)
     out = {}
     for k in sirt_iters:
-        plan.sirt(b, xs, sirt_lambda(plan, lam_scale), k, 0.0)
+        xs.zero_()
+        first_reconstruction(plan, b, xs, k, lam_scale)
         rms = volume_rms(plan, xs)
         inp = torch.empty(slices, npad, npad, device="cuda")
         tgt = torch.empty_like(inp)
@@ -149,29 +165,35 @@ def load(gb, path, size, max_batch):
         raise ValueError("%s: parameter layout does not match this library's network" % path)
     net.set_params(torch.from_numpy(params.copy()).cuda())
     meta = json.loads(str(z["meta"]))
-    net.sirt_iters = int(meta.get("sirt_iters", SIRT_ITERS))
+    net.input = "fbp" if meta.get("input") == "fbp" else "sirt"
+    net.sirt_iters = 0 if net.input == "fbp" else int(meta.get("sirt_iters", SIRT_ITERS))
     net.sirt_lam_scale = float(meta.get("sirt_lam_scale", 1.0))
     return net, meta
 
 
-def solve(gb, plan, b, x, net=None, tol=1e-3, maxit=200, sirt_iters=None, scratch=None):
+def solve(gb, plan, b, x, net=None, tol=1e-3, maxit=200, sirt_iters=None, scratch=None,
+          start=None):
     """CGLS to ||A^T r|| / ||A^T b|| <= tol, warm-started by the network when
-    `net` is given (SIRT -> U-Net -> CGLS), else from zero.  Returns
-    (CGLS info, seconds of each stage)."""
+    `net` is given (first reconstruction -> U-Net -> CGLS: the network's input
+    kind, SIRT or the filtered back projection, is in its metadata), from the
+    filtered back projection alone with start="fbp", else from zero.  Returns
+    (CGLS info, seconds of each stage: "input" for the first reconstruction)."""
     import torch
 
     st = {}
     t = time.perf_counter()
     rnorm_ref = 0.0
-    if net is not None:
-        if sirt_iters is None:
-            sirt_iters = getattr(net, "sirt_iters", SIRT_ITERS)
-        lam = sirt_lambda(plan, getattr(net, "sirt_lam_scale", 1.0))
-        _, sinfo = plan.sirt(b, x, lam, sirt_iters, 0.0)
-        rnorm_ref = sinfo.rnorm0  # ||A^T b||, the cold start's denominator
+    if net is not None or start == "fbp":
+        if start == "fbp" or getattr(net, "input", "sirt") == "fbp":
+            inp = "fbp"
+        else:
+            inp = sirt_iters if sirt_iters is not None else getattr(net, "sirt_iters", SIRT_ITERS)
+        rnorm_ref = first_reconstruction(plan, b, x, inp, getattr(net, "sirt_lam_scale", 1.0),
+                                         work=scratch[2] if scratch and len(scratch) > 2 else None)
         torch.cuda.synchronize()
-        st["sirt"] = time.perf_counter() - t
+        st["input"] = time.perf_counter() - t
         t = time.perf_counter()
+    if net is not None:
         if scratch is None:
             npix = net.max_batch * net.size * net.size
             scratch = (torch.empty(npix, device="cuda"), torch.empty(npix, device="cuda"))
@@ -179,7 +201,7 @@ def solve(gb, plan, b, x, net=None, tol=1e-3, maxit=200, sirt_iters=None, scratc
         torch.cuda.synchronize()
         st["unet"] = time.perf_counter() - t
         t = time.perf_counter()
-    _, info = plan.cgls(b, x, maxit, tol, warm=net is not None, rnorm_ref=rnorm_ref)
+    _, info = plan.cgls(b, x, maxit, tol, warm=rnorm_ref > 0.0, rnorm_ref=rnorm_ref)
     torch.cuda.synchronize()
     st["cgls"] = time.perf_counter() - t
     return info, st
@@ -191,8 +213,9 @@ def main():
     ap = argparse.ArgumentParser(description=__doc__.split("\n\n")[0])
     ap.add_argument("--out", default=DEFAULT_WEIGHTS,
                     help="weights file; with several --sirt-iters, _sirt<k> is appended")
-    ap.add_argument("--sirt-iters", default=str(SIRT_ITERS),
-                    help="SIRT depth(s) of the network input, comma separated")
+    ap.add_argument("--input", default=str(SIRT_ITERS),
+                    help="network input(s), comma separated: a SIRT depth, or fbp (the "
+                         "filtered back projection)")
     ap.add_argument("--sirt-lam-scale", type=float, default=1.0,
                     help="SIRT step as a multiple of 1/(nangles*nx)")
     ap.add_argument("--steps", type=int, default=3000)
@@ -205,7 +228,7 @@ def main():
     ap.add_argument("--seed", type=int, default=50000)
     args = ap.parse_args()
     gb.build()
-    ks = [int(k) for k in args.sirt_iters.split(",")]
+    ks = [k if k == "fbp" else int(k) for k in args.input.split(",")]
     datasets = {k: [] for k in ks}
     desc = []
     seed = args.seed
@@ -223,11 +246,14 @@ def main():
     for k in ks:
         net, hist = train(gb, datasets[k], steps=args.steps, batch=args.batch, crop=args.crop,
                           lr=args.lr, seed=args.seed)
-        meta = {"sirt_iters": k, "sirt_lam_scale": args.sirt_lam_scale,
-                "cgls_iters": CGLS_ITERS, "sets": desc, "steps": args.steps,
-                "batch": args.batch, "crop": args.crop, "lr": args.lr,
-                "final_loss": float(np.mean(hist[-50:])), "first_loss": float(hist[0])}
-        out = args.out if len(ks) == 1 else args.out.replace(".npz", "_sirt%d.npz" % k)
+        meta = {"input": "fbp" if k == "fbp" else "sirt", "cgls_iters": CGLS_ITERS,
+                "sets": desc, "steps": args.steps, "batch": args.batch, "crop": args.crop,
+                "lr": args.lr, "final_loss": float(np.mean(hist[-50:])),
+                "first_loss": float(hist[0])}
+        if k != "fbp":
+            meta.update(sirt_iters=k, sirt_lam_scale=args.sirt_lam_scale)
+        tag = "fbp" if k == "fbp" else "sirt%d" % k
+        out = args.out if len(ks) == 1 else args.out.replace(".npz", "_%s.npz" % tag)
         save(net, out, meta)
         print(json.dumps(dict(meta, out=out)), flush=True)
         del net

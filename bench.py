@@ -2,14 +2,17 @@
 1200-angle cylinder (square-pixel projector), on one GB300 per rank:
 learned-warm-start CGLS (the headline `value`) beside plain CGLS.
 
-One step = one complete reconstruction of the whole volume: a few SIRT
-iterations (the depth and step the weights file records), the BF16 U-Net warm
-start (arec3d_gb300/weights), then CGLS from that guess until
-||A^T(b - A x_k)|| / ||A^T b|| <= 1e-3 (the denominator fixed at its
-cold-start value) or 200 iterations.  `config.plain_cgls` is the same
-problem solved by CGLS from zero.  `--plain` (or missing weights) makes plain
-CGLS the headline.  Inputs: a seeded random-sphere cylinder with analytic line
-integrals and Poisson noise at 5e3 photons (no public dataset exists).
+One step = one complete reconstruction of the whole volume: the network's
+input (the filtered back projection, or the SIRT iterations the weights file
+records), the BF16 U-Net warm start (arec3d_gb300/weights), then CGLS from
+that guess until ||A^T(b - A x_k)|| / ||A^T b|| <= 1e-3 (the denominator
+fixed at its cold-start value) or 200 iterations.  Beside it, on the same
+data: `config.plain_cgls` (CGLS from zero), `config.fbp_cgls` (CGLS from the
+filtered back projection, no network) and `config.sirt_net_cgls` (the network
+trained on SIRT input), each with its error against the phantom.  `--plain`
+(or missing weights) makes plain CGLS the headline.  Inputs: a seeded
+random-sphere cylinder with analytic line integrals and Poisson noise at 5e3
+photons (no public dataset exists).
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
 
@@ -244,6 +247,7 @@ def make_problem(gb, seed, device="cuda"):
     b = syn.sphere_sinogram(ph, NX, NY, angles, ys=plan.ys, device=device)
     syn.poisson_log(b, PHOTONS, seed + 1, NY, device=device)
     torch.cuda.synchronize()
+    plan.phantom = ph
     return plan, b, angles
 
 
@@ -608,6 +612,9 @@ def main():
                     help="run only the warm-start network's inference (for profiling)")
     ap.add_argument("--weights", default=os.path.join(ROOT, "arec3d_gb300", "weights",
                                                       "unet_warm_start.npz"))
+    ap.add_argument("--weights-sirt", default=os.path.join(ROOT, "arec3d_gb300", "weights",
+                                                           "unet_warm_start_sirt4.npz"),
+                    help="the network trained on SIRT input, timed beside the headline")
     args = ap.parse_args()
     rank, local, world = dist_env()
     if args.kernels_only:
@@ -626,7 +633,10 @@ def main():
 
     import torch
 
+    import math
+
     import arec3d_gb300 as gb
+    from arec3d_gb300 import synthetic as syn
     from arec3d_gb300 import warmstart as ws
 
     torch.cuda.set_device(local)
@@ -648,33 +658,49 @@ def main():
 
     # the learned warm start: committed weights, inference net over 16 slices at a time
     net, meta = None, {}
+    npix = 16 * plan.nx * plan.nx
     if not args.plain and os.path.exists(args.weights):
         net, meta = ws.load(gb, args.weights, plan.nx, 16)
-        npix = 16 * plan.nx * plan.nx
         scratch = (torch.empty(npix, device="cuda"), torch.empty(npix, device="cuda"))
+    work = torch.empty_like(b)     # the filtered sinogram
+    atb2 = torch.zeros(1, dtype=torch.float64, device="cuda")
 
     def solve_plain():
         hist, info = plan.cgls(b, x, MAXIT, TOL, stream=stream)
         return info
 
-    sirt_iters = getattr(net, "sirt_iters", SIRT_ITERS)
+    def first_reconstruction(kind, iters, lam):
+        """FBP or SIRT from zero into x; returns ||A^T b|| (both compute it)."""
+        if kind == "fbp":
+            plan.fbp(b, x, work, atb_norm2=atb2, stream=stream)
+            return math.sqrt(float(atb2.item()))
+        _, sinfo = plan.sirt(b, x, lam, iters, 0.0, stream=stream)
+        return sinfo.rnorm0
+
+    def warm_pipeline(nt, stage_ev=None):
+        kind = getattr(nt, "input", "fbp") if nt is not None else "fbp"
+        iters = getattr(nt, "sirt_iters", SIRT_ITERS)
+        lam_n = ws.sirt_lambda(plan, getattr(nt, "sirt_lam_scale", 1.0))
+
+        def solve():
+            ev = [torch.cuda.Event(enable_timing=True) for _ in range(4)]
+            ev[0].record(stream)
+            rn = first_reconstruction(kind, iters, lam_n)
+            ev[1].record(stream)
+            if nt is not None:
+                nt.warm_start(plan, x, x, scratch[0], scratch[1], stream=stream)
+            ev[2].record(stream)
+            hist, info = plan.cgls(b, x, MAXIT, TOL, warm=True, rnorm_ref=rn, stream=stream)
+            ev[3].record(stream)
+            if stage_ev is not None:
+                stage_ev.append(ev)
+            return info
+        return solve
+
+    stage_ev = []  # per step: events after the input, after the U-Net, after CGLS
+    solve = warm_pipeline(net, stage_ev) if net is not None else solve_plain
+    sirt_iters = getattr(net, "sirt_iters", SIRT_ITERS) if net is not None else 0
     lam = ws.sirt_lambda(plan, getattr(net, "sirt_lam_scale", 1.0))
-    stage_ev = []  # per step: events after SIRT, after the U-Net, after CGLS
-
-    def solve_warm():
-        ev = [torch.cuda.Event(enable_timing=True) for _ in range(4)]
-        ev[0].record(stream)
-        _, sinfo = plan.sirt(b, x, lam, sirt_iters, 0.0, stream=stream)
-        ev[1].record(stream)
-        net.warm_start(plan, x, x, scratch[0], scratch[1], stream=stream)
-        ev[2].record(stream)
-        hist, info = plan.cgls(b, x, MAXIT, TOL, warm=True, rnorm_ref=sinfo.rnorm0,
-                               stream=stream)
-        ev[3].record(stream)
-        stage_ev.append(ev)
-        return info
-
-    solve = solve_warm if net is not None else solve_plain
 
     for _ in range(args.warmup):
         solve()
@@ -694,19 +720,41 @@ def main():
     stages = None
     if stage_ev:
         stages = {k: statistics.mean(ev[j].elapsed_time(ev[j + 1]) for ev in stage_ev)
-                  for j, k in enumerate(("sirt_ms", "unet_ms", "cgls_ms"))}
+                  for j, k in enumerate(("input_ms", "unet_ms", "cgls_ms"))}
     # the headline result on a few slices, kept for the FP64 check below
     keep = list(FP64_SLICES)
     x_keep = x[:, keep].contiguous().cpu().numpy()
     b_keep = b[:, :, keep].contiguous().cpu().numpy()
+    truth = syn.sphere_volume(plan.phantom, 0.5 * (NX - 1), NY, plan.ys)
+    tnorm = float(truth[:, :NY].double().pow(2).sum().sqrt())
 
-    # plain CGLS beside it (the comparison the metric names), same data
-    plain = None
+    def err_truth():
+        return float((x[:, :NY].double() - truth[:, :NY].double()).pow(2).sum().sqrt()) / tnorm
+
+    err_headline = err_truth()
+
+    # the other pipelines beside it, same data (untimed warm-up, then 1-2 steps)
+    def compare(fn):
+        fn()
+        pm, pinfos = timed_steps(fn, max(1, min(args.steps, 2)), world, stream)
+        return {"slices_per_s": job_value(world, pm), "ms_per_solve": pm,
+                "iterations": int(statistics.median([i.iterations for i in pinfos])),
+                "error_vs_phantom": err_truth()}
+
+    plain = fbp_only = sirt_net = None
     if net is not None:
-        solve_plain()
-        pm, pinfos = timed_steps(solve_plain, max(1, min(args.steps, 2)), world, stream)
-        plain = {"slices_per_s": job_value(world, pm), "ms_per_solve": pm,
-                 "iterations": int(statistics.median([i.iterations for i in pinfos]))}
+        plain = compare(solve_plain)
+        fbp_only = compare(warm_pipeline(None))
+        if os.path.exists(args.weights_sirt):
+            net_s, meta_s = ws.load(gb, args.weights_sirt, plan.nx, 16)
+            sirt_net = compare(warm_pipeline(net_s))
+            sirt_net.update(input="SIRT-%d" % net_s.sirt_iters,
+                            weights=os.path.relpath(args.weights_sirt, ROOT))
+            del net_s
+        for d in (plain, fbp_only, sirt_net):
+            if d:
+                d["speedup_vs_plain"] = d["slices_per_s"] / plain["slices_per_s"]
+    del truth
 
     # Roofline of the dominant kernel from the projector times recorded in the
     # timed region.  Unit: one projection (the forward projector is 32 band
@@ -775,7 +823,8 @@ def main():
                "h2d_gbs": NA * NY * NX * 4 / (h2d_ms / 1e3) / 1e9,
                "d2h_gbs": plan.nrays * NY * 4 / (d2h_ms / 1e3) / 1e9,
                "path": "pinned host sinogram [angle][slice][bin] -> arecgb_reconstruct_host ("
-                       + ("SIRT -> warm start -> CGLS" if net is not None else "CGLS")
+                       + (("filtered back projection" if sirt_iters == 0 else "SIRT")
+                          + " -> warm start -> CGLS" if net is not None else "CGLS")
                        + ") -> pinned host volume [ray][slice]"}
 
     cpu = None
@@ -800,17 +849,20 @@ def main():
                          "create_ms": getattr(plan, "create_ms", None),
                          "note": "created once per geometry, outside the timed region"})
         cfg["fp64_check"] = fp64
+        cfg["error_vs_phantom"] = err_headline
         if net is not None:
-            cfg.update(warm_start=True, sirt_iters=sirt_iters, stage_ms=stages,
-                       workload="learned warm start: SIRT-%d -> BF16 U-Net -> CGLS to "
+            first = "filtered back projection" if sirt_iters == 0 else "SIRT-%d" % sirt_iters
+            cfg.update(warm_start=True, network_input=first, stage_ms=stages,
+                       workload="learned warm start: %s -> BF16 U-Net -> CGLS to "
                                 "||A^T r||/||A^T b|| <= 1e-3 (max 200 it), square-pixel "
                                 "projector, 1024^2 x 512 slices, 1200 angles over [0,180), "
                                 "random-sphere cylinder r=500 px with 200 spheres, Poisson 5e3 "
-                                "photons" % sirt_iters,
-                       plain_cgls=plain,
+                                "photons" % first,
+                       plain_cgls=plain, fbp_cgls=fbp_only, sirt_net_cgls=sirt_net,
                        speedup_vs_plain=(value / plain["slices_per_s"]) if plain else None,
                        weights=os.path.relpath(args.weights, ROOT),
-                       weights_meta={k: meta.get(k) for k in ("sets", "steps", "final_loss")})
+                       weights_meta={k: meta.get(k) for k in ("input", "sets", "steps",
+                                                              "final_loss")})
         out = {"metric": METRIC, "value": value, "unit": "slices/s", "n_gpus": world,
                "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_step,
                "higher_is_better": True, "scaling": "weak", "vs_baseline": None,

@@ -83,6 +83,19 @@ int arecgb_project(arecgb_plan *plan, const float *d_x, float *d_q, double *d_no
 int arecgb_backproject(arecgb_plan *plan, const float *d_s, float *d_g, double *d_norm2,
                        void *stream);
 
+/* Filtered back projection, a cheap first reconstruction (no counterpart in
+ * the reference): d_x = (pi / nangles) A^T (h * d_b), with h the discrete
+ * Ram-Lak ramp filter along detector bins (h(0) = 1/4, h(d) = -1/(pi d)^2 for
+ * odd d, 0 for even d != 0) applied as a linear convolution (bins off the
+ * detector are zero).  Device layouts; d_work: a sinogram-sized device buffer
+ * that receives the filtered sinogram.  d_atb_norm2 (device, optional):
+ * ||A^T d_b||^2 as well, by one more back projection (the cold start's
+ * denominator of the CGLS stopping test). */
+int arecgb_fbp(arecgb_plan *plan, const float *d_b, float *d_x, float *d_work,
+               double *d_atb_norm2, void *stream);
+/* The ramp filter alone: d_f = (pi / nangles) h * d_s (sinogram layouts). */
+int arecgb_ramp_filter(arecgb_plan *plan, const float *d_s, float *d_f, void *stream);
+
 /* CGLS on device arrays (replaces cyl_cgls[_KB|_SQ], areccgls.cpp:12,245,
  * areccgls_KB.cpp:12).  b: sinogram (device layout); x: volume, used as the
  * initial guess when warm != 0.  rnorm_ref > 0 fixes the denominator of the
@@ -386,10 +399,12 @@ typedef struct arecgb_problem {
  * memory, so the problems are packed into waves whose workspace fits
  * budget_bytes (first fit, largest first; a problem above the budget runs
  * alone).  Per wave: a plan per problem (without the optional projector
- * tables), with n_nets > 0 the learned warm start per problem (SIRT of
- * sirt_iters iterations at step sirt_lam_scale / (nangles nx), then the
- * smallest of the networks `nets` whose images hold the problem's width: the
- * same parameters at several image sizes), then one batched CGLS of all the
+ * tables), with n_nets > 0 the learned warm start per problem (the
+ * network's input: SIRT of sirt_iters iterations at step sirt_lam_scale /
+ * (nangles nx), or with sirt_iters = 0 the filtered back projection
+ * (arecgb_fbp); then the smallest of the networks `nets` whose images hold the
+ * problem's width: the same parameters at several image sizes), then one
+ * batched CGLS of all the
  * wave's problems, one CUDA graph launch per iteration, each to
  * ||A^T r|| / ||A^T b|| <= tol (max maxit iterations).  info[i] (may be NULL)
  * receives problem i's CGLS summary and wave_of[i] (may be NULL) its wave.
@@ -404,10 +419,11 @@ int arecgb_solve_uneven(const arecgb_problem *probs, int n, size_t budget_bytes,
  * in the reference, whose cyl_cgls_SQ is the net == NULL case):
  *   b_host [nangles][ny][nx] float (cyl_cgls_SQ's `images.data`), read;
  *   x_host [nrays][ny] float (its `xvol->data`), written.
- * With net != NULL: SIRT from zero (sirt_iters iterations of step sirt_lam),
- * the network's warm start, then CGLS to ||A^T r|| / ||A^T b|| <= tol with the
- * denominator ||A^T b|| of the cold start (at most maxit iterations); with
- * net == NULL: CGLS from zero.  The copies are cudaMemcpyAsync on `stream`
+ * With net != NULL: the network's input (SIRT from zero, sirt_iters
+ * iterations of step sirt_lam, or with sirt_iters = 0 the filtered back
+ * projection, arecgb_fbp), the network's warm start, then CGLS to
+ * ||A^T r|| / ||A^T b|| <= tol with the denominator ||A^T b|| of the cold
+ * start (at most maxit iterations); with net == NULL: CGLS from zero.  The copies are cudaMemcpyAsync on `stream`
  * (full speed from page-locked memory).  Device buffers belong to the plan,
  * allocated on first use and kept; the call returns after x_host is written.
  * info (may be NULL) receives the CGLS summary. */

@@ -213,8 +213,9 @@ def test_solve_uneven_waves_match_single_solves(gb):
     """arecgb_solve_uneven: five cylinders of uneven radius, slices and angles
     under a budget that forces several waves give exactly the results of
     solving each alone (plans without tables compute the same values), with
-    and without the learned warm start (SIRT -> U-Net -> CGLS with the cold
-    start's denominator, as the single-problem pipeline does)."""
+    and without the learned warm start (first reconstruction -> U-Net -> CGLS
+    with the cold start's denominator, as the single-problem pipeline does), for
+    both shipped networks (filtered back projection input, SIRT input)."""
     import torch
 
     from arec3d_gb300 import synthetic as syn
@@ -223,7 +224,9 @@ def test_solve_uneven_waves_match_single_solves(gb):
     rng = np.random.default_rng(55)
     specs = [(60.5, 24, 90), (31.5, 8, 40), (90.0, 40, 120), (47.5, 16, 64), (20.0, 8, 30)]
     probs, singles = [], []
-    net, _ = ws.load(gb, ws.DEFAULT_WEIGHTS, 184, 4)
+    net_fbp, _ = ws.load(gb, ws.DEFAULT_WEIGHTS, 184, 4)
+    net_sirt, _ = ws.load(gb, ws.DEFAULT_WEIGHTS.replace(".npz", "_sirt4.npz"), 184, 4)
+    assert (net_fbp.input, net_sirt.input) == ("fbp", "sirt")
     for radius, ny, na in specs:
         ang = syn.uniform_angles(na)
         plan = gb.Plan(gb.SQ, radius, ny, ang)
@@ -235,7 +238,8 @@ def test_solve_uneven_waves_match_single_solves(gb):
         probs.append(dict(radius=radius, ny=ny, angles=ang, b=qd, x=empty_vol(plan)))
     nxv = [gb.cylinder_info(r, ny)[:2] for r, ny, _ in specs]
     assert [(p.nx, p.nrays) for p, _ in singles] == nxv
-    for use_net in (False, True):
+    for net in (None, net_fbp, net_sirt):
+        use_net = net is not None
         budget = 1 << 20  # 1 MiB of workspace: every problem its own wave
         infos, waves = gb.solve_uneven(probs, budget, maxit=30, tol=1e-3,
                                        nets=[net] if use_net else None)
@@ -253,5 +257,5 @@ def test_solve_uneven_waves_match_single_solves(gb):
                                          nets=[net] if use_net else None)
         assert set(waves2) == {0}
         assert [i.iterations for i in infos2] == [i.iterations for i in infos]
-        print("uneven batch (%s): iterations %s" % ("warm" if use_net else "plain",
+        print("uneven batch (%s): iterations %s" % (net.input if use_net else "plain",
                                                     [i.iterations for i in infos]))
