@@ -17,7 +17,11 @@
 #include <math.h>
 #include <string.h>
 
+#include <stdio.h>
+#include <stdlib.h>
+
 #include <algorithm>
+#include <chrono>
 #include <numeric>
 #include <string>
 #include <vector>
@@ -151,10 +155,24 @@ int arecgb_solve_uneven(const arecgb_problem *probs, int n, size_t budget_bytes,
             }
         }
     }
+    // ARECGB_PROGRESS=1: one line per wave on stderr (problems, seconds of
+    // plan creation, warm start and batched CGLS; the phases then synchronise)
+    const char *prog_env = getenv("ARECGB_PROGRESS");
+    const bool progress = prog_env && prog_env[0] == '1';
+    using clk = std::chrono::steady_clock;
+    auto lap = [&](clk::time_point &t) {
+        if (progress) cudaStreamSynchronize(st);
+        const auto now = clk::now();
+        const double s_ = std::chrono::duration<double>(now - t).count();
+        t = now;
+        return s_;
+    };
     int rc = 0;
     for (size_t w = 0; !rc && w < waves.size(); w++) {
         const std::vector<int> &wv = waves[w];
         const int m = (int)wv.size();
+        clk::time_point t_w = clk::now();
+        double t_plan = 0, t_warm = 0, t_cgls = 0;
         std::vector<Plan *> plans(m, nullptr);
         std::vector<const float *> bs(m);
         std::vector<float *> xs(m);
@@ -168,6 +186,7 @@ int arecgb_solve_uneven(const arecgb_problem *probs, int n, size_t budget_bytes,
             xs[j] = q.d_x;
             if (wave_of) wave_of[wv[j]] = (int)w;
         }
+        t_plan = lap(t_w);
         // the learned warm start, problem by problem: the network's input (SIRT
         // at the step the network was trained with, or with sirt_iters = 0 the
         // filtered back projection), then x0 = net(input) scaled back
@@ -211,9 +230,15 @@ int arecgb_solve_uneven(const arecgb_problem *probs, int n, size_t budget_bytes,
                                        img[0], img[1], st);
             warm[j] = 1;
         }
+        t_warm = lap(t_w);
         if (!rc)
             rc = cgls_batch(plans.data(), bs.data(), xs.data(), warm.data(), m, maxit, tol,
                             rref.data(), nullptr, inf.data(), st, nullptr);
+        t_cgls = lap(t_w);
+        if (progress)
+            fprintf(stderr, "arecgb_solve_uneven: wave %zu of %zu, %d problems (%.1f GB): plans "
+                    "%.2f s, warm start %.2f s, CGLS %.2f s\n", w + 1, waves.size(), m,
+                    load[w] / 1e9, t_plan, t_warm, t_cgls);
         for (int j = 0; j < m; j++) {
             if (info && !rc) info[wv[j]] = inf[j];
             plan_destroy(plans[j]);

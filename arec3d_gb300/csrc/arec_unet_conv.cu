@@ -185,14 +185,18 @@ static int launch_conv(const __nv_bfloat16 *X, const __nv_bfloat16 *Wt, const fl
 // reads directly.  Four stages: thread 0 of warp 0 issues the loads, thread 0
 // of warp 1 the MMAs; each stage's commit frees it for the loads four chunks
 // later.  All four warps run the epilogue from TMEM.
-constexpr int kTmaStages = 4;
-
+//
+// A block lives a few microseconds (9 or 18 chunks, each waiting on an L2
+// load), so throughput comes from blocks resident per SM: the narrow layers
+// take two stages (21-25 KB of shared memory: 8-10 blocks per SM within the
+// 512 TMEM columns), the wide ones four.
 template <int COUT>
 struct TmaCfg {
+    static constexpr int STAGES = COUT <= 64 ? 2 : 4;
     static constexpr int A_BYTES = 128 * 64;  // 128 pixels x 32 channels
     static constexpr int B_BYTES = COUT * 64;
     static constexpr int STAGE = A_BYTES + B_BYTES;  // a multiple of 1024
-    static constexpr int SMEM = kTmaStages * STAGE + 1024;
+    static constexpr int SMEM = STAGES * STAGE + 1024;
     static constexpr uint32_t NCOLS = COUT < 32 ? 32 : COUT;
 };
 
@@ -203,7 +207,7 @@ __global__ void __launch_bounds__(128)
                        int Wd, int Cin, int relu, int ystride, int *err) {
     using Cfg = TmaCfg<COUT>;
     extern __shared__ unsigned char sm_raw[];
-    __shared__ __align__(8) uint64_t full[kTmaStages], empty[kTmaStages], done;
+    __shared__ __align__(8) uint64_t full[Cfg::STAGES], empty[Cfg::STAGES], done;
     __shared__ uint32_t tmem_base;
     const uint32_t raw = umma::smem_addr(sm_raw);
     unsigned char *sm = sm_raw + ((1024u - (raw & 1023u)) & 1023u);  // 1024-byte aligned stages
@@ -217,7 +221,7 @@ __global__ void __launch_bounds__(128)
         umma::tmem_relinquish();
     }
     if (tid == 0) {
-        for (int st = 0; st < kTmaStages; st++) {
+        for (int st = 0; st < Cfg::STAGES; st++) {
             umma::mbar_init(&full[st], 1);
             umma::mbar_init(&empty[st], 1);
         }
@@ -233,9 +237,9 @@ __global__ void __launch_bounds__(128)
     if (warp == 0 && lane == 0) {
         bool ok = true;
         for (int c = 0; c < nchunks && ok; c++) {
-            const int st = c % kTmaStages;
-            if (c >= kTmaStages &&
-                !umma::mbar_wait(&empty[st], (uint32_t)(c / kTmaStages - 1) & 1u, kWaitLimit)) {
+            const int st = c % Cfg::STAGES;
+            if (c >= Cfg::STAGES &&
+                !umma::mbar_wait(&empty[st], (uint32_t)(c / Cfg::STAGES - 1) & 1u, kWaitLimit)) {
                 ok = false;
                 atomicOr(err, 4);
                 break;
@@ -249,8 +253,8 @@ __global__ void __launch_bounds__(128)
     } else if (warp == 1 && lane == 0) {
         constexpr uint32_t idesc = umma::idesc_bf16(128, COUT);
         for (int c = 0; c < nchunks; c++) {
-            const int st = c % kTmaStages;
-            if (!umma::mbar_wait(&full[st], (uint32_t)(c / kTmaStages) & 1u, kWaitLimit)) {
+            const int st = c % Cfg::STAGES;
+            if (!umma::mbar_wait(&full[st], (uint32_t)(c / Cfg::STAGES) & 1u, kWaitLimit)) {
                 atomicOr(err, 4);
                 break;
             }

@@ -466,6 +466,10 @@ def uneven_batch(args, gb, syn, ws, timed):
         x = torch.zeros(nr, ys, device="cuda")
         problems.append(dict(radius=radius, ny=ny, angles=angles, b=b, x=x, nx=nx, na=na))
         slices += ny
+        if (i + 1) % 8 == 0:
+            torch.cuda.synchronize()
+            print("config 5: %d problems generated, %.1f s" % (i + 1, time.perf_counter() - t0),
+                  file=sys.stderr, flush=True)
     torch.cuda.synchronize()
     gen_s = time.perf_counter() - t0
     nets = []
@@ -534,7 +538,8 @@ def unet_only(args):
     ms = e0.elapsed_time(e1) / args.launches
     flops = 2 * 188928 * 16 * NX * NX  # multiply-adds of the 3x3 layers per pixel x 2
     print(json.dumps({"unet_only": True, "ms_per_16_images": ms,
-                      "tensor_tflops": flops / (ms / 1e3) / 1e12}))
+                      "tensor_tflops": flops / (ms / 1e3) / 1e12,
+                      "checksum": float(y.double().sum())}))
 
 
 def kernels_only(args):
@@ -600,6 +605,8 @@ def main():
     ap.add_argument("--angles", type=int, default=NA, help="angles for --kernels-only")
     ap.add_argument("--nx", type=int, default=NX, help="detector bins for --kernels-only")
     ap.add_argument("--plain", action="store_true", help="plain CGLS only (no warm start)")
+    ap.add_argument("--profile-step", action="store_true",
+                    help="after the warm-up, run one headline step and exit (for ncu)")
     ap.add_argument("--config", type=int, default=0, choices=[0, 1, 3, 5],
                     help="measure another benchmark configuration instead of the headline")
     ap.add_argument("--batch-problems", type=int, default=64, help="problems for --config 5")
@@ -644,7 +651,15 @@ def main():
         import torch.distributed as dist
 
         dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    # the e2e leg's page-locked host buffers, allocated first: on the GPU machine's
+    # virtual machine a page-locked buffer allocated after gigabytes of host
+    # traffic uploaded at a fraction of the speed of one allocated early
     gb.build()
+    b_host = x_host = None
+    if not args.no_e2e and not args.profile_step:
+        _, nr0, _ = gb.cylinder_info(0.5 * (NX - 1), NY)
+        b_host = torch.empty(NA, NY, NX, dtype=torch.float32, pin_memory=True)
+        x_host = torch.empty(nr0, NY, dtype=torch.float32, pin_memory=True)
     plan, b, angles = make_problem(gb, seed=1000 + rank)
     x = torch.zeros(plan.nrays, plan.ys, dtype=torch.float32, device="cuda")
     stream = torch.cuda.current_stream()
@@ -705,6 +720,14 @@ def main():
     for _ in range(args.warmup):
         solve()
     stage_ev.clear()
+    if args.profile_step:  # one more step alone, for a launch list (no timing, no JSON)
+        n0 = gb.launch_count()
+        torch.cuda.synchronize()
+        info = solve()
+        torch.cuda.synchronize()
+        print(json.dumps({"profile_step": True, "launches": gb.launch_count() - n0,
+                          "iterations": info.iterations}))
+        return
     # timed region: the headline pipeline, with projector timing and clocks
     clocks = ClockSampler(local)
     clocks.start()
@@ -786,21 +809,21 @@ def main():
                 "fp_calls": fp_calls, "bp_calls": bp_calls,
                 # projections per step: the timed (non-graph) calls plus one forward and
                 # one back projection per CGLS iteration replayed from the CUDA graph
-                "projector_ms_per_step": (fp_avg * (fp_calls / args.steps + n_it) +
-                                          bp_avg * (bp_calls / args.steps + n_it)) * 1e3,
-                "projector_share_of_step": (fp_avg * (fp_calls / args.steps + n_it) +
-                                            bp_avg * (bp_calls / args.steps + n_it)) * 1e3 /
-                ms_step}
+                # (the first iteration runs eagerly and is among the timed calls)
+                "projector_ms_per_step": (fp_avg * (fp_calls / args.steps + max(n_it - 1, 0)) +
+                                          bp_avg * (bp_calls / args.steps + max(n_it - 1, 0)))
+                * 1e3,
+                "projector_share_of_step": (fp_avg * (fp_calls / args.steps + max(n_it - 1, 0)) +
+                                            bp_avg * (bp_calls / args.steps + max(n_it - 1, 0)))
+                * 1e3 / ms_step}
 
     # End to end through one C-ABI call over page-locked host buffers in the
     # reference's layouts (arecgb_reconstruct_host): every step the sinogram
-    # [angle][slice][bin] goes up, SIRT -> warm start -> CGLS run, and the
+    # [angle][slice][bin] goes up, the warm start and CGLS run, and the
     # volume [ray][slice] comes back; host-clock time around the call.
     e2e = None
     if not args.no_e2e:
-        b_host = torch.empty(NA, NY, NX, dtype=torch.float32, pin_memory=True)
         b_host.copy_(b[:, :, :NY].permute(0, 2, 1))
-        x_host = torch.empty(plan.nrays, NY, dtype=torch.float32, pin_memory=True)
 
         def e2e_step():
             return plan.reconstruct_host(b_host, x_host, net, sirt_iters, lam, MAXIT, TOL,
