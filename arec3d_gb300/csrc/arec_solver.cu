@@ -591,6 +591,8 @@ int cgls_batch(Plan *const *plans, const float *const *d_b, float *const *d_x, c
             }
         }
         per_iter = launch_count() - c0;
+        // the captured launches run only when the graph is replayed (counted there)
+        count_launches(-(int)per_iter);
     }
     // replay until every problem has stopped
     int batch = 1;
