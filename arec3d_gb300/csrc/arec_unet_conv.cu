@@ -295,6 +295,136 @@ __global__ void __launch_bounds__(128)
     if (warp == 0) umma::tmem_dealloc(tmem, Cfg::NCOLS);
 }
 
+// Several output rows per block (TMA path, narrow layers): R consecutive rows
+// of one image x 128 pixels x COUT channels, one accumulator per row in TMEM
+// (R x COUT columns).  K runs over (column shift dx, 32-channel chunk): one
+// TMA box brings the R + 2 input rows the R output rows need, shifted by dx
+// (rows outside the image arrive as zeros), and three more the weights of
+// the taps (dy, dx), dy = 0, 1, 2; output row r then takes input row r + dy
+// with tap (dy, dx).  Each input row is loaded 3 (R + 2) / R times per output
+// row instead of 9 times, and a block's fixed costs are shared by R rows.
+template <int COUT, int R>
+struct RowsCfg {
+    static constexpr int STAGES = 2;
+    static constexpr int A_ROW = 128 * 64;              // one input row tile: 128 px x 32 ch
+    static constexpr int A_BYTES = (R + 2) * A_ROW;
+    static constexpr int B_TAP = COUT * 64;             // one tap's weights for 32 channels
+    static constexpr int STAGE = A_BYTES + 3 * B_TAP;   // a multiple of 1024
+    static constexpr int SMEM = STAGES * STAGE + 1024;
+    static constexpr uint32_t NCOLS = R * COUT;          // a power of two in [32, 512]
+};
+
+template <int COUT, int R>
+__global__ void __launch_bounds__(128)
+    conv3x3_rows_kernel(const __grid_constant__ CUtensorMap tmX,
+                        const __grid_constant__ CUtensorMap tmW, const float *__restrict__ bias,
+                        __nv_bfloat16 *__restrict__ Y, int H, int Wd, int Cin, int relu,
+                        int ystride, int *err) {
+    using Cfg = RowsCfg<COUT, R>;
+    static_assert(Cfg::NCOLS >= 32 && Cfg::NCOLS <= 512 && (Cfg::NCOLS & (Cfg::NCOLS - 1)) == 0,
+                  "TMEM columns: a power of two in [32, 512]");
+    static_assert(Cfg::STAGE % 1024 == 0, "stages stay 1024-byte aligned");
+    extern __shared__ unsigned char sm_raw[];
+    __shared__ __align__(8) uint64_t full[Cfg::STAGES], empty[Cfg::STAGES], done;
+    __shared__ uint32_t tmem_base;
+    const uint32_t raw = umma::smem_addr(sm_raw);
+    unsigned char *sm = sm_raw + ((1024u - (raw & 1023u)) & 1023u);  // 1024-byte aligned stages
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    const int wtiles = Wd / 128, hgroups = H / R;
+    const int b = blockIdx.x;
+    const int wt = b % wtiles, hg = (b / wtiles) % hgroups, n = b / (wtiles * hgroups);
+    const int h0 = hg * R, w0 = wt * 128;
+
+    if (warp == 0) {
+        umma::tmem_alloc(&tmem_base, Cfg::NCOLS);
+        umma::tmem_relinquish();
+    }
+    if (tid == 0) {
+        for (int st = 0; st < Cfg::STAGES; st++) {
+            umma::mbar_init(&full[st], 1);
+            umma::mbar_init(&empty[st], 1);
+        }
+        umma::mbar_init(&done, 1);
+        umma::mbar_fence_init();
+    }
+    umma::fence_before_sync();
+    __syncthreads();
+    umma::fence_after_sync();
+    const uint32_t tmem = tmem_base;
+    const int cchunks = Cin / kConvKC, nchunks = 3 * cchunks;  // (dx, channel chunk)
+
+    if (warp == 0 && lane == 0) {
+        for (int c = 0; c < nchunks; c++) {
+            const int st = c % Cfg::STAGES;
+            if (c >= Cfg::STAGES &&
+                !umma::mbar_wait(&empty[st], (uint32_t)(c / Cfg::STAGES - 1) & 1u, kWaitLimit)) {
+                atomicOr(err, 4);
+                break;
+            }
+            const int dx = c / cchunks, c0 = (c % cchunks) * kConvKC;
+            unsigned char *A = sm + st * Cfg::STAGE;
+            umma::mbar_arrive_expect_tx(&full[st], (uint32_t)Cfg::STAGE);
+            umma::tma_load_4d(A, &tmX, c0, w0 + dx - 1, h0 - 1, n, &full[st]);
+#pragma unroll
+            for (int dy = 0; dy < 3; dy++)
+                umma::tma_load_3d(A + Cfg::A_BYTES + dy * Cfg::B_TAP, &tmW, c0, 3 * dy + dx, 0,
+                                  &full[st]);
+        }
+    } else if (warp == 1 && lane == 0) {
+        constexpr uint32_t idesc = umma::idesc_bf16(128, COUT);
+        for (int c = 0; c < nchunks; c++) {
+            const int st = c % Cfg::STAGES;
+            if (!umma::mbar_wait(&full[st], (uint32_t)(c / Cfg::STAGES) & 1u, kWaitLimit)) {
+                atomicOr(err, 4);
+                break;
+            }
+            umma::fence_after_sync();
+            const uint32_t a = umma::smem_addr(sm + st * Cfg::STAGE), bw = a + Cfg::A_BYTES;
+#pragma unroll
+            for (int r = 0; r < R; r++)
+#pragma unroll
+                for (int dy = 0; dy < 3; dy++)
+#pragma unroll
+                    for (int k = 0; k < 2; k++)
+                        umma::mma_bf16(tmem + (uint32_t)(r * COUT),
+                                       umma::smem_desc_sw64(a + (r + dy) * Cfg::A_ROW + 32 * k),
+                                       umma::smem_desc_sw64(bw + dy * Cfg::B_TAP + 32 * k), idesc,
+                                       (c > 0 || dy > 0 || k > 0) ? 1u : 0u);
+            umma::mma_commit(&empty[st]);
+        }
+        umma::mma_commit(&done);  // arrives when every MMA above has completed
+    }
+    __syncwarp();
+    const bool dok = __all_sync(0xffffffffu, umma::mbar_wait(&done, 0, kWaitLimit));
+    umma::fence_after_sync();
+    if (!dok && lane == 0) atomicOr(err, 4);
+    if (dok) {
+#pragma unroll 1
+        for (int r = 0; r < R; r++) {
+            const size_t p = ((size_t)n * H + h0 + r) * Wd + w0 + tid;  // TMEM lane = pixel
+#pragma unroll 1
+            for (int cc = 0; cc < COUT / 32; cc++) {
+                float v[32];
+                umma::tmem_ld32(tmem + ((uint32_t)(32 * warp) << 16) + (uint32_t)(r * COUT + cc * 32),
+                                v);
+                __align__(16) __nv_bfloat16 out[32];
+#pragma unroll
+                for (int i = 0; i < 32; i++) {
+                    float t = v[i] + (bias ? bias[cc * 32 + i] : 0.f);
+                    if (relu) t = fmaxf(t, 0.f);
+                    out[i] = __float2bfloat16(t);
+                }
+                uint4 *dst = reinterpret_cast<uint4 *>(Y + p * ystride + cc * 32);
+#pragma unroll
+                for (int q = 0; q < 4; q++) dst[q] = reinterpret_cast<const uint4 *>(out)[q];
+            }
+        }
+    }
+    umma::fence_before_sync();
+    __syncthreads();
+    if (warp == 0) umma::tmem_dealloc(tmem, Cfg::NCOLS);
+}
+
 typedef CUresult (*EncodeTiledFn)(CUtensorMap *, CUtensorMapDataType, cuuint32_t, void *,
                                   const cuuint64_t *, const cuuint64_t *, const cuuint32_t *,
                                   const cuuint32_t *, CUtensorMapInterleave, CUtensorMapSwizzle,
@@ -343,13 +473,13 @@ bool encode_sino_map(CUtensorMap *m, const float *base, int ys, int nx, int na, 
 // Tensor maps of one convolution; false if the CUDA driver refuses them (the
 // caller then uses the gather kernel).
 static bool conv_tensor_maps(const __nv_bfloat16 *x, const __nv_bfloat16 *w, int N, int H, int Wd,
-                             int Cin, int Cout, CUtensorMap *tx, CUtensorMap *tw) {
+                             int Cin, int Cout, CUtensorMap *tx, CUtensorMap *tw, int box_rows = 1) {
     EncodeTiledFn enc = encode_tiled();
     if (!enc) return false;
     const cuuint64_t xd[4] = {(cuuint64_t)Cin, (cuuint64_t)Wd, (cuuint64_t)H, (cuuint64_t)N};
     const cuuint64_t xs[3] = {(cuuint64_t)Cin * 2, (cuuint64_t)Wd * Cin * 2,
                               (cuuint64_t)H * Wd * Cin * 2};
-    const cuuint32_t xb[4] = {(cuuint32_t)kConvKC, 128, 1, 1};
+    const cuuint32_t xb[4] = {(cuuint32_t)kConvKC, 128, (cuuint32_t)box_rows, 1};
     const cuuint32_t one[4] = {1, 1, 1, 1};
     if (enc(tx, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 4, (void *)x, xd, xs, xb, one,
             CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_64B,
@@ -380,6 +510,27 @@ static int launch_conv_tma(const CUtensorMap &tx, const CUtensorMap &tw, const f
     return 0;
 }
 
+template <int COUT, int R>
+static int launch_conv_rows(const CUtensorMap &tx, const CUtensorMap &tw, const float *bias,
+                            __nv_bfloat16 *Y, int N, int H, int Wd, int Cin, int relu, int ystride,
+                            int *err, cudaStream_t st) {
+    using Cfg = RowsCfg<COUT, R>;
+    static bool configured = false;
+    if (!configured) {
+        ARECGB_CUDA(cudaFuncSetAttribute(conv3x3_rows_kernel<COUT, R>,
+                                         cudaFuncAttributeMaxDynamicSharedMemorySize, Cfg::SMEM));
+        configured = true;
+    }
+    conv3x3_rows_kernel<COUT, R><<<N * (H / R) * (Wd / 128), 128, Cfg::SMEM, st>>>(
+        tx, tw, bias, Y, H, Wd, Cin, relu, ystride, err);
+    ARECGB_CUDA(cudaGetLastError());
+    return 0;
+}
+
+// Output rows per block of the multi-row TMA kernel: 4 for 32 output channels,
+// 2 for 64 (two blocks per SM fit in shared memory), else 1 (the one-row kernel).
+static int conv_rows_for(int Cout) { return Cout == 32 ? 4 : (Cout == 64 ? 2 : 1); }
+
 // layout: 0 = TMA path when the width is a multiple of 128, else the gather
 //         kernel with (LBO 128, SBO 256) [K-halves 128 B apart, row groups 256 B
 //         apart]; 1 = the gather kernel with the two offsets exchanged (for
@@ -398,6 +549,13 @@ int conv3x3_bf16(const void *X, const void *Wt, const float *bias, void *Y, int 
     const int P = N * H * Wd;
     if (layout == 0 && Wd % 128 == 0) {
         CUtensorMap tx, tw;
+        const int R = conv_rows_for(Cout);
+        if (R > 1 && H % R == 0 && conv_tensor_maps(x, w, N, H, Wd, Cin, Cout, &tx, &tw, R + 2)) {
+            if (Cout == 32)
+                return launch_conv_rows<32, 4>(tx, tw, bias, y, N, H, Wd, Cin, relu, ystride, err, st);
+            if (Cout == 64)
+                return launch_conv_rows<64, 2>(tx, tw, bias, y, N, H, Wd, Cin, relu, ystride, err, st);
+        }
         if (conv_tensor_maps(x, w, N, H, Wd, Cin, Cout, &tx, &tw)) {
 #define ARECGB_CONV_TMA(C) \
     if (Cout == C) return launch_conv_tma<C>(tx, tw, bias, y, H, Wd, Cin, P, relu, ystride, err, st);

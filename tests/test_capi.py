@@ -161,3 +161,29 @@ def test_argument_errors_before_any_device_call(lib):
     assert L.arecgb_plan_table_bytes(None) == 0
     L.arecgb_cgls_batch.argtypes = [vp, vp, vp, ip, C.c_int, C.c_int, C.c_float, vp, vp, vp]
     assert L.arecgb_cgls_batch(None, None, None, None, 0, 10, 1e-3, None, None, None) == ERR_ARG
+
+
+def test_warm_start_entry_argument_errors(lib):
+    """The filtered back projection and the uneven scheduler reject bad
+    arguments before any device call: null plan or buffers, a negative SIRT
+    depth (0 selects the filtered back projection as the network's input)."""
+    L = lib.lib()
+    ERR_ARG = -90
+    vp = C.c_void_p
+    L.arecgb_fbp.argtypes = [vp, vp, vp, vp, vp, vp]
+    L.arecgb_ramp_filter.argtypes = [vp, vp, vp, vp]
+    assert L.arecgb_fbp(None, None, None, None, None, None) == ERR_ARG
+    assert L.arecgb_last_error().decode().startswith("arecgb_fbp")
+    assert L.arecgb_ramp_filter(None, None, None, None) == ERR_ARG
+    assert L.arecgb_last_error().decode().startswith("arecgb_ramp_filter")
+    prob = lib.Problem(3, 10.0, 4, 4, np.zeros(4, np.float32).ctypes.data_as(C.POINTER(C.c_float)),
+                       None, None)
+    info = (lib.SolveInfo * 1)()
+    for sirt_iters in (-1,):
+        rc = L.arecgb_solve_uneven(C.byref(prob), 1, 1 << 30, None, 0, sirt_iters, 1.0, 10,
+                                   C.c_float(1e-3), info, None, None)
+        assert rc == ERR_ARG
+    # a problem without device buffers is rejected, with or without a network
+    rc = L.arecgb_solve_uneven(C.byref(prob), 1, 1 << 30, None, 0, 0, 1.0, 10, C.c_float(1e-3),
+                               info, None, None)
+    assert rc == ERR_ARG and "bad problem 0" in L.arecgb_last_error().decode()

@@ -143,9 +143,14 @@ def _compare(gb, size, batch, params, x, dout):
 
 
 @pytest.mark.parametrize("cin,cout,shape", [(32, 32, (1, 3, 128)), (64, 128, (2, 2, 256)),
-                                            (256, 32, (1, 4, 128)), (128, 256, (1, 2, 128))])
+                                            (256, 32, (1, 4, 128)), (128, 256, (1, 2, 128)),
+                                            (32, 32, (2, 8, 256)), (64, 32, (1, 12, 128)),
+                                            (32, 64, (2, 6, 128)), (128, 64, (1, 4, 256))])
 def test_conv3x3_tma_path(gb, cin, cout, shape):
-    """Widths that are multiples of 128 take the TMA path (layout 0); layout 2
+    """Widths that are multiples of 128 take the TMA path (layout 0): 32 output
+    channels and heights divisible by 4, or 64 output channels and even heights,
+    take the kernel that computes several rows per block (the image's first and
+    last rows read zeros from outside it); the rest the one-row kernel.  Layout 2
     forces the gather kernel on the same data."""
     import torch
 
