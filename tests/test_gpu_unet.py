@@ -263,3 +263,39 @@ def test_multiscale_loss_against_oracle(gb):
     print("multi-scale loss %.6e (oracle %.6e); update direction agrees on %.4f of %d params"
           % (loss, loss_ref, agree, int(big.sum())))
     assert agree > 0.999
+
+
+@pytest.mark.parametrize("radius,ny,npad", [(31.5, 5, 64), (20.0, 3, 48), (63.5, 9, 128)])
+def test_device_images_match_image_cyl2cb(gb, radius, ny, npad):
+    """The warm start's device conversion between the cylinder [ray][slice] and
+    the network's images [slice][iz][ix] (arecgb_unet_images_from_volume /
+    _to_volume) is ImageCyl2CB / ImageCB2Cyl (AREC3D/AREC3D/arecImage.cpp:
+    88-232) of the reference-compatible host layer, cube [iz][y][ix] ->
+    image y, zero-padded to npad and scaled."""
+    import torch
+
+    from conftest import uniform_angles
+    from devutil import empty_vol, vol_to_dev
+
+    L = gb.lib()
+    plan = gb.Plan(gb.SQ, radius, ny, uniform_angles(4))
+    cyl = gb.arecAllocateCylImage(radius, ny)
+    assert (cyl.nrays, cyl.nx) == (plan.nrays, plan.nx)
+    rng = np.random.default_rng(int(radius))
+    x = rng.standard_normal((plan.nrays, ny)).astype(np.float32)
+    gb.cyl_data(cyl)[:] = x
+    cube = np.zeros((cyl.nz, cyl.ny, cyl.nx), np.float32)
+    assert L.arecgb_ImageCyl2CB(cyl, gb._cb_image(cube), cyl.nx, cyl.ny, cyl.nz) == 0
+    scale = 0.5
+    img = torch.full((ny, npad, npad), 7.0, device="cuda")
+    gb.images_from_volume(plan, vol_to_dev(plan, x), img, npad, 0, ny, scale)
+    imh = img.cpu().numpy()
+    nx = plan.nx
+    np.testing.assert_array_equal(imh[:, :nx, :nx], scale * cube.transpose(1, 0, 2))
+    assert not imh[:, nx:, :].any() and not imh[:, :, nx:].any()
+    # and back: the images of the disk give the cylinder (ImageCB2Cyl)
+    back = empty_vol(plan)
+    gb.images_to_volume(plan, img, back, npad, 0, ny, 1.0 / scale)
+    np.testing.assert_array_equal(back[:, :ny].cpu().numpy(), x)
+    gb.arecImageFree(cyl)
+    plan.close()
