@@ -683,6 +683,19 @@ int arecgb_reconstruct_host(arecgb_plan *plan, const float *b_host, float *x_hos
     if (rc) return rc;
     cudaStream_t st = (cudaStream_t)stream;
     const size_t nsin = (size_t)p->na * p->ny * p->nx;
+    // ARECGB_PROGRESS=1: the phases' seconds on stderr (each phase then synchronises)
+    const char *prog_env = getenv("ARECGB_PROGRESS");
+    const bool progress = prog_env && prog_env[0] == '1';
+    using clk = std::chrono::steady_clock;
+    clk::time_point t_ph = clk::now();
+    double ph[6] = {0, 0, 0, 0, 0, 0};  // upload, layout, input, network, CGLS, download
+    auto lap = [&](int k) {
+        if (!progress) return;
+        cudaStreamSynchronize(st);
+        const auto now = clk::now();
+        ph[k] += std::chrono::duration<double>(now - t_ph).count();
+        t_ph = now;
+    };
     if ((rc = ensure(&p->d_vol[3], vol_floats(p))) || (rc = ensure(&p->d_sin[2], sin_floats(p))) ||
         (rc = ensure_stage(p, nsin)))
         return rc;
@@ -701,9 +714,13 @@ int arecgb_reconstruct_host(arecgb_plan *plan, const float *b_host, float *x_hos
         }
     }
     float *d_b = p->d_sin[2], *d_x = p->d_vol[3];
+    lap(5);  // (allocations on first use: not a phase)
+    ph[5] = 0;
     ARECGB_CUDA(cudaMemcpyAsync(p->d_stage, b_host, sizeof(float) * nsin, cudaMemcpyHostToDevice,
                                 st));
+    lap(0);
     if ((rc = sino_to_device_layout(p->d_stage, d_b, p->na, p->ny, p->nx, p->ys, st))) return rc;
+    lap(1);
     arecgb_solve_info si, ci;
     memset(&si, 0, sizeof(si));
     memset(&ci, 0, sizeof(ci));
@@ -714,22 +731,32 @@ int arecgb_reconstruct_host(arecgb_plan *plan, const float *b_host, float *x_hos
         double *d_n2 = p->d_sred + 2 * kSredBlocks;
         if ((rc = fbp(p, d_b, d_x, p->d_sin[0], d_n2, st))) return rc;
         ARECGB_CUDA(cudaMemcpyAsync(p->h_sred, d_n2, sizeof(double), cudaMemcpyDeviceToHost, st));
+        lap(2);
         if ((rc = arecgb_warm_start(plan, net, d_x, d_x, p->d_img[0], p->d_img[1], st)))
             return rc;
         ARECGB_CUDA(cudaStreamSynchronize(st));
+        lap(3);
         rc = cgls(p, d_b, d_x, 1, maxit, tol, sqrt(p->h_sred[0]), nullptr, &ci, st);
     } else if (net) {
         if ((rc = sirt(p, d_b, d_x, sirt_lam, sirt_iters, 0.0f, nullptr, &si, 0, st))) return rc;
+        lap(2);
         if ((rc = arecgb_warm_start(plan, net, d_x, d_x, p->d_img[0], p->d_img[1], st)))
             return rc;
+        lap(3);
         rc = cgls(p, d_b, d_x, 1, maxit, tol, si.rnorm0, nullptr, &ci, st);
     } else {
         rc = cgls(p, d_b, d_x, 0, maxit, tol, 0.0, nullptr, &ci, st);
     }
     if (rc) return rc;
+    lap(4);
     ARECGB_CUDA(cudaMemcpy2DAsync(x_host, sizeof(float) * p->ny, d_x, sizeof(float) * p->ys,
                                   sizeof(float) * p->ny, p->nrays, cudaMemcpyDeviceToHost, st));
     ARECGB_CUDA(cudaStreamSynchronize(st));
+    lap(5);
+    if (progress)
+        fprintf(stderr, "arecgb_reconstruct_host: upload %.3f s, layout %.3f s, first "
+                "reconstruction %.3f s, network %.3f s, CGLS %.3f s, download %.3f s\n",
+                ph[0], ph[1], ph[2], ph[3], ph[4], ph[5]);
     if (info) *info = ci;
     return 0;
 }

@@ -408,7 +408,8 @@ typedef struct arecgb_problem {
  * wave's problems, one CUDA graph launch per iteration, each to
  * ||A^T r|| / ||A^T b|| <= tol (max maxit iterations).  info[i] (may be NULL)
  * receives problem i's CGLS summary and wave_of[i] (may be NULL) its wave.
- * Synchronises. */
+ * Synchronises.  With ARECGB_PROGRESS=1 in the environment one line per wave
+ * on stderr (problems, workspace, seconds of plans, warm start and CGLS). */
 int arecgb_solve_uneven(const arecgb_problem *probs, int n, size_t budget_bytes,
                         arecgb_unet *const *nets, int n_nets, int sirt_iters,
                         double sirt_lam_scale, int maxit, float tol, arecgb_solve_info *info,
@@ -426,7 +427,10 @@ int arecgb_solve_uneven(const arecgb_problem *probs, int n, size_t budget_bytes,
  * start (at most maxit iterations); with net == NULL: CGLS from zero.  The copies are cudaMemcpyAsync on `stream`
  * (full speed from page-locked memory).  Device buffers belong to the plan,
  * allocated on first use and kept; the call returns after x_host is written.
- * info (may be NULL) receives the CGLS summary. */
+ * info (may be NULL) receives the CGLS summary.  With ARECGB_PROGRESS=1 in
+ * the environment the call prints its phases' seconds on stderr (upload,
+ * layout change, first reconstruction, network, CGLS, download; each phase
+ * then synchronises). */
 int arecgb_reconstruct_host(arecgb_plan *plan, const float *b_host, float *x_host,
                             arecgb_unet *net, int sirt_iters, float sirt_lam, int maxit,
                             float tol, arecgb_solve_info *info, void *stream);
