@@ -496,6 +496,22 @@ def uneven_batch(args, gb, syn, ws, timed):
     e1.record(st)
     torch.cuda.synchronize()
     ms = e0.elapsed_time(e1)
+    seq = None
+    if args.c5_sequential:
+        # the same problems solved one at a time through the same scheduler (a
+        # wave of one, one graph per iteration with a single branch), for the
+        # batched launch's overlap
+        for p in problems:
+            p["x"].zero_()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        seq_it = []
+        for p in problems:
+            inf1, _ = gb.solve_uneven([p], budget, maxit=MAXIT, tol=TOL, nets=nets, stream=st)
+            seq_it.append(inf1[0].iterations)
+        torch.cuda.synchronize()
+        seq = {"ms": (time.perf_counter() - t0) * 1e3,
+               "same_iterations": seq_it == [inf.iterations for inf in infos]}
     out = {"config": 5,
            "workload": "uneven batch: %d cylinders, radius 128-1024 px (problem 0: 1024, 512 "
                        "slices, 1800 angles), detector 2r+16 bins, 32-512 slices, 360-1800 "
@@ -506,6 +522,7 @@ def uneven_batch(args, gb, syn, ws, timed):
            "slices": slices, "waves": max(waves) + 1, "setup_s": gen_s,
            "resident_gb": sum(p["b"].numel() + p["x"].numel() for p in problems) * 4 / 1e9,
            "scale": scale,
+           "sequential": seq,
            "problems": [{"nx": p["nx"], "slices": p["ny"], "angles": p["na"],
                          "iterations": inf.iterations, "rel_final": inf.rel_final, "wave": w}
                         for p, inf, w in zip(problems, infos, waves)]}
@@ -612,6 +629,8 @@ def main():
     ap.add_argument("--batch-problems", type=int, default=64, help="problems for --config 5")
     ap.add_argument("--c5-scale", type=float, default=1.0,
                     help="--config 5: scale radii (and slices below 1) for a smaller test run")
+    ap.add_argument("--c5-sequential", action="store_true",
+                    help="--config 5: also solve the problems one at a time, for comparison")
     ap.add_argument("--c5-budget-gb", type=float, default=0.0,
                     help="--config 5: solver workspace budget (default: most of the free HBM)")
     ap.add_argument("--pairs", type=int, default=720, help="image pairs for --config 3")
