@@ -13,7 +13,10 @@
 //   decoder level 1:    up(g3), u2 128->64  | e2 -> d2a 128->64,  d2b 64->64   = g2
 //   decoder level 0:    up(g2), u1 64->32   | e1 -> d1a 64->32,   d1b 32->32   = g1
 //   output:             1x1 32->1 + the input (residual)
-// "up" is nearest 2x upsampling, "|" channel concatenation ([up-conv, skip]).
+// "up" is nearest 2x upsampling, "|" channel concatenation ([up-conv, skip]):
+// c1b, c2b and c3b write e1, e2, e3 straight into the trailing channels of
+// the concatenation buffers cat1, cat2, cat3, where the pooling and the
+// decoder read them (no copy).
 // The 3x3 convolutions of 32+ input channels, forward and data-gradient, run on
 // the tensor cores (tcgen05, arec_unet_conv.cu); weight gradients, pooling,
 // upsampling, the first and last layers run on CUDA cores (arec_unet_ops.cu).
@@ -56,7 +59,7 @@ struct Net {
     float *pyr = nullptr;
 
     // activations (P0 = maxN*H*W pixels, P1 = P0/4, ...)
-    __nv_bfloat16 *a1, *e1, *q1, *a2, *e2, *q2, *a3, *e3, *q3, *a4, *e4;
+    __nv_bfloat16 *a1, *q1, *a2, *q2, *a3, *q3, *a4, *e4;
     __nv_bfloat16 *up3, *cat3, *f3, *g3, *up2, *cat2, *f2, *g2, *up1, *cat1, *f1, *g1;
     uint8_t *arg1, *arg2, *arg3;
     const float *in = nullptr;  // input of the last forward
@@ -135,8 +138,8 @@ static int create(Net **out, int H, int W, int maxN, int train, uint64_t seed) {
 #define A(ptr, count) \
     if (!rc) rc = alloc(n, &n->ptr, (count));
     A(params, off) A(wbf, off)
-    A(a1, P0 * 32) A(e1, P0 * 32) A(q1, P1 * 32) A(a2, P1 * 64) A(e2, P1 * 64) A(q2, P2 * 64)
-    A(a3, P2 * 128) A(e3, P2 * 128) A(q3, P3 * 128) A(a4, P3 * 256) A(e4, P3 * 256)
+    A(a1, P0 * 32) A(q1, P1 * 32) A(a2, P1 * 64) A(q2, P2 * 64)
+    A(a3, P2 * 128) A(q3, P3 * 128) A(a4, P3 * 256) A(e4, P3 * 256)
     A(up3, P2 * 256) A(cat3, P2 * 256) A(f3, P2 * 128) A(g3, P2 * 128)
     A(up2, P1 * 128) A(cat2, P1 * 128) A(f2, P1 * 64) A(g2, P1 * 64)
     A(up1, P0 * 64) A(cat1, P0 * 64) A(f1, P0 * 32) A(g1, P0 * 32)
@@ -200,36 +203,34 @@ static int forward(Net *n, const float *x, float *y, int N, cudaStream_t st) {
     int rc = 0;
     if (!n->mirrors_fresh && (rc = refresh_mirrors(n, st))) return rc;
     conv_in(x, n->params + n->woff[C1A], n->params + n->boff[C1A], n->a1, N, H, W, 32, st);
-    if ((rc = conv(n, C1B, n->a1, n->e1, N, H, W, st))) return rc;
-    maxpool(n->e1, n->q1, n->arg1, N, H, W, 32, st);
+    // e1 = cat1[:, 32:64), e2 = cat2[:, 64:128), e3 = cat3[:, 128:256)
+    if ((rc = conv(n, C1B, n->a1, n->cat1 + 32, N, H, W, st, 64))) return rc;
+    maxpool(n->cat1 + 32, n->q1, n->arg1, N, H, W, 32, st, 64);
     if ((rc = conv(n, C2A, n->q1, n->a2, N, H1, W1, st))) return rc;
-    if ((rc = conv(n, C2B, n->a2, n->e2, N, H1, W1, st))) return rc;
-    maxpool(n->e2, n->q2, n->arg2, N, H1, W1, 64, st);
+    if ((rc = conv(n, C2B, n->a2, n->cat2 + 64, N, H1, W1, st, 128))) return rc;
+    maxpool(n->cat2 + 64, n->q2, n->arg2, N, H1, W1, 64, st, 128);
     if ((rc = conv(n, C3A, n->q2, n->a3, N, H2, W2, st))) return rc;
-    if ((rc = conv(n, C3B, n->a3, n->e3, N, H2, W2, st))) return rc;
-    maxpool(n->e3, n->q3, n->arg3, N, H2, W2, 128, st);
+    if ((rc = conv(n, C3B, n->a3, n->cat3 + 128, N, H2, W2, st, 256))) return rc;
+    maxpool(n->cat3 + 128, n->q3, n->arg3, N, H2, W2, 128, st, 256);
     if ((rc = conv(n, C4A, n->q3, n->a4, N, H3, W3, st))) return rc;
     if ((rc = conv(n, C4B, n->a4, n->e4, N, H3, W3, st))) return rc;
     // decoder level 2
     upsample(n->e4, n->up3, N, H3, W3, 256, 256, st);
     if ((rc = conv(n, U3, n->up3, n->cat3, N, H2, W2, st, 256))) return rc;
-    chan_copy(n->e3, n->cat3, P2, 128, 256, 128, st);
     if ((rc = conv(n, D3A, n->cat3, n->f3, N, H2, W2, st))) return rc;
     if ((rc = conv(n, D3B, n->f3, n->g3, N, H2, W2, st))) return rc;
     // decoder level 1
     upsample(n->g3, n->up2, N, H2, W2, 128, 128, st);
     if ((rc = conv(n, U2, n->up2, n->cat2, N, H1, W1, st, 128))) return rc;
-    chan_copy(n->e2, n->cat2, P1, 64, 128, 64, st);
     if ((rc = conv(n, D2A, n->cat2, n->f2, N, H1, W1, st))) return rc;
     if ((rc = conv(n, D2B, n->f2, n->g2, N, H1, W1, st))) return rc;
     // decoder level 0
     upsample(n->g2, n->up1, N, H1, W1, 64, 64, st);
     if ((rc = conv(n, U1, n->up1, n->cat1, N, H, W, st, 64))) return rc;
-    chan_copy(n->e1, n->cat1, P0, 32, 64, 32, st);
     if ((rc = conv(n, D1A, n->cat1, n->f1, N, H, W, st))) return rc;
     if ((rc = conv(n, D1B, n->f1, n->g1, N, H, W, st))) return rc;
     conv_out(n->g1, n->params + n->woff[OUT], n->params + n->boff[OUT], x, y, P0, 32, st);
-    count_launches(27);  // conv_in, 16 tensor-core convolutions, 3 pool, 3 upsample, 3 copy, out
+    count_launches(24);  // conv_in, 16 tensor-core convolutions, 3 pool, 3 upsample, out
     ARECGB_CUDA(cudaGetLastError());
     n->in = x;
     n->lastN = N;
@@ -289,17 +290,17 @@ static int backward(Net *n, const float *dout, cudaStream_t st) {
     maxpool_bwd(gY, n->arg3, n->de3, N, H2, W2, 128, st);
     f32_to_bf16(n->de3, gX, P2 * 128, st);
     // encoder level 2
-    if ((rc = conv_bwd(n, C3B, n->a3, n->e3, 128, gX, 128, gY, N, H2, W2, st))) return rc;
+    if ((rc = conv_bwd(n, C3B, n->a3, n->cat3 + 128, 256, gX, 128, gY, N, H2, W2, st))) return rc;
     if ((rc = conv_bwd(n, C3A, n->q2, n->a3, 128, gY, 128, gX, N, H2, W2, st))) return rc;
     maxpool_bwd(gX, n->arg2, n->de2, N, H1, W1, 64, st);
     f32_to_bf16(n->de2, gY, P1 * 64, st);
     // encoder level 1
-    if ((rc = conv_bwd(n, C2B, n->a2, n->e2, 64, gY, 64, gX, N, H1, W1, st))) return rc;
+    if ((rc = conv_bwd(n, C2B, n->a2, n->cat2 + 64, 128, gY, 64, gX, N, H1, W1, st))) return rc;
     if ((rc = conv_bwd(n, C2A, n->q1, n->a2, 64, gX, 64, gY, N, H1, W1, st))) return rc;
     maxpool_bwd(gY, n->arg1, n->de1, N, H, W, 32, st);
     f32_to_bf16(n->de1, gX, P0 * 32, st);
     // encoder level 0
-    if ((rc = conv_bwd(n, C1B, n->a1, n->e1, 32, gX, 32, gY, N, H, W, st))) return rc;
+    if ((rc = conv_bwd(n, C1B, n->a1, n->cat1 + 32, 64, gX, 32, gY, N, H, W, st))) return rc;
     relu_bwd(n->a1, gY, n->gpre, P0 * 32, st);
     conv_in_wgrad(n->in, n->gpre, n->grads + n->woff[C1A], n->grads + n->boff[C1A], N, H, W, 32,
                   st);

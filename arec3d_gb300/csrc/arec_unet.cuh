@@ -25,7 +25,7 @@ void conv_out(const __nv_bfloat16 *h, const float *w, const float *b, const floa
 void conv_out_bwd(const __nv_bfloat16 *h, const float *w, const float *dy, __nv_bfloat16 *dh,
                   float *gw, float *gb, size_t P, int C, cudaStream_t st);
 void maxpool(const __nv_bfloat16 *x, __nv_bfloat16 *y, uint8_t *arg, int N, int H, int W, int C,
-             cudaStream_t st);
+             cudaStream_t st, int xs = 0);
 void maxpool_bwd(const __nv_bfloat16 *dy, const uint8_t *arg, float *dx_acc, int N, int H, int W,
                  int C, cudaStream_t st);
 void upsample(const __nv_bfloat16 *x, __nv_bfloat16 *y, int N, int H, int W, int C, int Cy,

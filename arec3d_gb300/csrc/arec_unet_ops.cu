@@ -172,7 +172,7 @@ __global__ void __launch_bounds__(128)
 // 2x2 max pooling with the arg max (0..3, first of equals) per output; one
 // thread per output pixel and 8 channels (16-byte vectors; C % 8 == 0).
 __global__ void k_maxpool(const __nv_bfloat16 *__restrict__ x, __nv_bfloat16 *__restrict__ y,
-                          uint8_t *__restrict__ arg, int N, int H, int W, int C) {
+                          uint8_t *__restrict__ arg, int N, int H, int W, int C, int xs) {
     const int Ho = H / 2, Wo = W / 2, C8 = C / 8;
     const size_t n_out = (size_t)N * Ho * Wo * C8;
     GRID_STRIDE(i, n_out) {
@@ -186,7 +186,7 @@ __global__ void k_maxpool(const __nv_bfloat16 *__restrict__ x, __nv_bfloat16 *__
 #pragma unroll
         for (int t = 0; t < 4; t++) {
             const size_t pix = top + (size_t)(t >> 1) * W + (t & 1);
-            const uint4 xv = *reinterpret_cast<const uint4 *>(x + pix * C + g * 8);
+            const uint4 xv = *reinterpret_cast<const uint4 *>(x + pix * xs + g * 8);
             const __nv_bfloat16 *xb = reinterpret_cast<const __nv_bfloat16 *>(&xv);
 #pragma unroll
             for (int j = 0; j < 8; j++) {
@@ -530,9 +530,11 @@ void conv_out_bwd(const __nv_bfloat16 *h, const float *w, const float *dy, __nv_
     int blocks = (int)std::min<size_t>(1024, (P + 127) / 128);
     k_conv_out_bwd<<<blocks, 128, 0, st>>>(h, w, dy, dh, gw, gb, P);
 }
+// x: [N][H][W] pixels of xs channels (xs = 0: C), the first C of them pooled
 void maxpool(const __nv_bfloat16 *x, __nv_bfloat16 *y, uint8_t *arg, int N, int H, int W, int C,
-             cudaStream_t st) {
-    k_maxpool<<<blocks_for((size_t)N * H * W * C / 32), 256, 0, st>>>(x, y, arg, N, H, W, C);
+             cudaStream_t st, int xs) {
+    k_maxpool<<<blocks_for((size_t)N * H * W * C / 32), 256, 0, st>>>(x, y, arg, N, H, W, C,
+                                                                      xs > 0 ? xs : C);
 }
 void maxpool_bwd(const __nv_bfloat16 *dy, const uint8_t *arg, float *dx_acc, int N, int H, int W,
                  int C, cudaStream_t st) {
