@@ -62,3 +62,29 @@ def test_reference_arm_other_ranks_exit_quietly():
                         "--steps", "1", "--warmup", "0"], env=env, capture_output=True, text=True,
                        timeout=120)
     assert r.returncode == 0 and r.stdout.strip() == ""
+
+
+def test_reference_arm_json_contract():
+    """`bench.py --impl reference` (the reference's algorithm, plain CGLS, on
+    this host's cores through the oracle's C restatement) prints one JSON line
+    with the benchmark's metric, the reference marker, a cpu_baseline that
+    names its cores and sample, and an e2e object with no host-device bytes.
+    A sample of 2 of the 1200 angles keeps this to seconds."""
+    import json
+
+    out = subprocess.run([sys.executable, os.path.join(ROOT, "bench.py"), "--impl", "reference",
+                          "--steps", "1", "--warmup", "0", "--ref-angle-step", "600"],
+                         capture_output=True, text=True, timeout=600, cwd=ROOT)
+    assert out.returncode == 0, out.stderr[-2000:]
+    lines = [ln for ln in out.stdout.splitlines() if ln.startswith("{")]
+    assert len(lines) == 1
+    d = json.loads(lines[0])
+    import bench
+
+    assert d["metric"] == bench.METRIC and d["impl"] == "reference"
+    assert d["unit"] == "slices/s" and d["higher_is_better"] is True and d["value"] > 0
+    cb = d["cpu_baseline"]
+    assert cb["kind"] == "port" and cb["cores"] >= 1 and cb["value"] == d["value"]
+    assert "2 of the 1200 angles" in cb["sample"] and cb["host"]["nproc"] >= 1
+    assert d["e2e"] == {"value": d["value"], "unit": "slices/s", "h2d_bytes_per_step": 0,
+                        "d2h_bytes_per_step": 0}
