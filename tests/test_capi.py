@@ -187,3 +187,17 @@ def test_warm_start_entry_argument_errors(lib):
     rc = L.arecgb_solve_uneven(C.byref(prob), 1, 1 << 30, None, 0, 0, 1.0, 10, C.c_float(1e-3),
                                info, None, None)
     assert rc == ERR_ARG and "bad problem 0" in L.arecgb_last_error().decode()
+
+
+@pytest.mark.parametrize("r", [0.5, 1.0, 12.0, 31.5, 127.5, 511.5])
+def test_synthetic_cylinder_coords_match_oracle(oc, r):
+    """The benchmark's ground truth (synthetic.sphere_volume) samples the
+    phantom at the pixel centres of the reference's cylinder in its ray order
+    (arecAllocateCylImage, AREC3D/AREC3D/arecImage.cpp:29-86)."""
+    from arec3d_gb300 import synthetic as syn
+
+    nx, nr, cord = oc.cyl(r)
+    cx, cz = syn.cylinder_coords(r)
+    assert cx.size == nr
+    np.testing.assert_array_equal(cx, cord[:, 0] - r)
+    np.testing.assert_array_equal(cz, cord[:, 1] - r)
